@@ -1,0 +1,373 @@
+"""Benchmark of the quantized vector-sparse SDDMM / SpMM path on GB300.
+
+Headline workload: SDDMM L8-R8, A and B 4096 x 64 int8, output mask 4096 x
+4096 with V = 8 column vectors at sparsity 0.9 (uniform vector placement),
+int32 output, signed lanes.  One step = one batched launch over `--batch`
+independent instances (own A, B and output, shared mask), sized so the
+step's data (about 470 MB) exceeds twice the 129 MB L2: no L2 flush is
+needed between steps.  Extra lines of the same JSON object report the L4-R4
+and L16-R8 SDDMM variants and the SpMM L8-R8 configuration (A 1024 x 1024,
+V = 8, sparsity 0.9, B 1024 x 256).
+
+`--impl reference` times the reference's CPU implementation of the path (the
+host SDDMM routine) on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "quantized SpMM/SDDMM TOP/s vs roofline; sparse-attn req/s + p50/p99 latency"
+UNIT = "TOP/s"
+SEQ, HEAD_DIM, VEC, SPARSITY = 4096, 64, 8, 0.9
+
+
+def _peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# workload construction
+# ----------------------------------------------------------------------------
+
+def sddmm_workload(pa: int, pb: int, batch: int, seed: int = 42):
+    from magicube_gb300 import formats, synth
+    mask = synth.uniform_mask(SEQ // VEC, SEQ, VEC, SPARSITY, seed=seed)
+    hm = formats.prepare_sddmm(mask, alignment=8)
+    rng = np.random.default_rng(seed + 1)
+    lhs = rng.integers(0, 256, size=(batch, SEQ * HEAD_DIM * pa // 8), dtype=np.uint8)
+    rhs = rng.integers(0, 256, size=(batch, SEQ * HEAD_DIM * pb // 8), dtype=np.uint8)
+    return mask, hm, lhs, rhs
+
+
+def sddmm_bytes(hm, pa: int, pb: int, batch: int) -> tuple[float, float]:
+    """(algorithmic bytes per launch, ops per launch) of a batched SDDMM."""
+    nnz = hm.mask.nnz_vec
+    per_inst = SEQ * HEAD_DIM * pa / 8 + SEQ * HEAD_DIM * pb / 8 + hm.aligned_nnz * VEC * 4
+    mask_bytes = hm.aligned_nnz * 4 + hm.mask.m_vec * 2 * 4 + hm.mask.m_vec * 4
+    ops = 2.0 * nnz * VEC * HEAD_DIM * batch
+    return per_inst * batch + mask_bytes, ops
+
+
+def time_cuda(fn, steps: int, warmup: int, stream) -> list[float]:
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in evs:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline (the oracle's restatement of the reference's host routine)
+# ----------------------------------------------------------------------------
+
+def cpu_sddmm_sample(hm, lhs0: np.ndarray, rhs0: np.ndarray, rows: int, threads: int = 1) -> tuple[float, float]:
+    """Time the host SDDMM routine over the first `rows` vector-rows of one
+    instance split across `threads` threads; returns (seconds, ops)."""
+    import oracle
+    L = oracle.lib()
+    out = np.zeros(hm.aligned_nnz * VEC, dtype=np.int32)
+    pairs = np.ascontiguousarray(hm.row_offsets)
+    cols = np.ascontiguousarray(hm.col_indices)
+    bounds = [int(x) for x in np.linspace(0, rows, threads + 1)]
+
+    def work(lo: int, hi: int) -> None:
+        if hi <= lo:
+            return
+        L.mco_sddmm_host(int(lhs0.ctypes.data) + lo * VEC * HEAD_DIM, int(rhs0.ctypes.data), int(out.ctypes.data),
+                         hi - lo, VEC, HEAD_DIM, SEQ, 8, 8, int(pairs.ctypes.data) + lo * 2 * 4,
+                         int(cols.ctypes.data), 8, 0, oracle.SIGNED)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for f in [ex.submit(work, bounds[i], bounds[i + 1]) for i in range(threads)]:
+            f.result()  # re-raises a worker's exception
+    dt = time.perf_counter() - t0
+    nnz = int(sum(hm.row_offsets[2 * i + 1] - hm.row_offsets[2 * i] for i in range(rows)))
+    return dt, 2.0 * nnz * VEC * HEAD_DIM
+
+
+def cpu_baseline(steps_budget_s: float = 12.0) -> dict:
+    mask, hm, lhs, rhs = sddmm_workload(8, 8, 1)
+    rows = 64
+    dt, ops = cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, 1)
+    reps = max(1, int(steps_budget_s / max(dt, 1e-3)))
+    tot_t, tot_ops = 0.0, 0.0
+    for _ in range(min(reps, 50)):
+        dt, ops = cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, 1)
+        tot_t += dt
+        tot_ops += ops
+    return {"value": tot_ops / tot_t / 1e12, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"host SDDMM L8-R8 routine (oracle restatement of Host_sddmm_integers), {rows} of "
+                      f"{SEQ // VEC} vector-rows of one 4096x4096x64 V=8 s=0.9 instance, single thread"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    mask, hm, lhs, rhs = sddmm_workload(8, 8, 1)
+    rows = SEQ // VEC  # one full instance per step
+    for _ in range(args.warmup):
+        cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, threads)
+    t, ops = 0.0, 0.0
+    for _ in range(args.steps):
+        dt, o = cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, threads)
+        t += dt
+        ops += o
+    v = ops / t / 1e12
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int8", "data": "synthetic",
+        "config": {"workload": "SDDMM L8-R8 4096x4096x64 V=8 s=0.9 (one instance per step)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "one full 4096x4096x64 V=8 s=0.9 SDDMM instance per step, host routine "
+                                   "(oracle restatement of Host_sddmm_integers) split by vector-rows over "
+                                   f"{threads} threads"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+
+def run_gpu(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    from magicube_gb300 import ops
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    peaks = _peaks()
+
+    def sync_all():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    B = args.batch
+    results = {}
+    launches_per_step = 1
+
+    def sddmm_case(pa, pb, timed_region_clock=False):
+        mask, hm, lhs_h, rhs_h = sddmm_workload(pa, pb, B)
+        dm = ops.DeviceSddmmMask.from_host(hm, dev)
+        lhs = torch.from_numpy(lhs_h).to(dev)
+        rhs = torch.from_numpy(rhs_h).to(dev)
+        out = torch.empty((B, hm.aligned_nnz * VEC), dtype=torch.int32, device=dev)
+        fn = lambda: ops.sddmm(dm, lhs, rhs, HEAD_DIM, pa, pb, signed=True, out=out, batch=B)
+        sync_all()
+        if timed_region_clock:
+            with ClockSampler(local) as cs:
+                ms = time_cuda(fn, args.steps, args.warmup, stream)
+            clocks = cs.summary()
+        else:
+            ms, clocks = time_cuda(fn, args.steps, args.warmup, stream), None
+        sync_all()
+        byts, opc = sddmm_bytes(hm, pa, pb, B)
+        t = max_over_ranks(sum(ms) / 1e3)
+        avg = t / args.steps
+        return {"tops": opc * world * args.steps / t / 1e12, "ms": avg * 1e3, "gbs": byts / avg / 1e9,
+                "bytes": byts, "ops": opc, "clocks": clocks, "mask": hm, "dm": dm, "lhs_h": lhs_h, "rhs_h": rhs_h,
+                "out": out, "lhs": lhs, "rhs": rhs}
+
+    head = sddmm_case(8, 8, timed_region_clock=True)
+
+    # e2e through the C ABI with host buffers: H2D of the step's operands, the
+    # launch, D2H of the step's outputs, all inside the timed region.
+    lhs_pin = torch.from_numpy(head["lhs_h"]).pin_memory()
+    rhs_pin = torch.from_numpy(head["rhs_h"]).pin_memory()
+    out_pin = torch.empty(head["out"].shape, dtype=torch.int32).pin_memory()
+    dm = head["dm"]
+
+    def e2e_step():
+        head["lhs"].copy_(lhs_pin, non_blocking=True)
+        head["rhs"].copy_(rhs_pin, non_blocking=True)
+        ops.sddmm(dm, head["lhs"], head["rhs"], HEAD_DIM, 8, 8, signed=True, out=head["out"], batch=B)
+        out_pin.copy_(head["out"], non_blocking=True)
+
+    e2e_steps = max(3, args.steps // 4)
+    sync_all()
+    ms_e2e = time_cuda(e2e_step, e2e_steps, max(args.warmup, 3), stream)
+    sync_all()
+    t_e2e = max_over_ranks(sum(ms_e2e) / 1e3)
+    e2e = {"value": head["ops"] * world * e2e_steps / t_e2e / 1e12, "unit": UNIT,
+           "h2d_bytes_per_step": int(lhs_pin.numel() + rhs_pin.numel()),
+           "d2h_bytes_per_step": int(out_pin.numel() * 4)}
+    del lhs_pin, rhs_pin, out_pin
+
+    variants = {}
+    if not args.headline_only:
+        for pa, pb, name in [(4, 4, "sddmm_L4R4"), (16, 8, "sddmm_L16R8")]:
+            r = sddmm_case(pa, pb)
+            variants[name] = {"tops": r["tops"], "ms": r["ms"], "gbs": r["gbs"],
+                              "hbm_frac": r["gbs"] / peaks["hbm_gbs"]}
+            del r
+            torch.cuda.empty_cache()
+        variants["spmm_L8R8_1024x1024x256"] = spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks)
+
+    if rank == 0:
+        gbs = head["gbs"]
+        line = {
+            "metric": METRIC, "value": head["tops"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int8", "data": "synthetic",
+            "config": {"workload": "SDDMM L8-R8: A,B 4096x64 int8, mask 4096x4096 V=8 sparsity 0.9 uniform, "
+                                   "int32 out, signed lanes",
+                       "instances_per_step": B, "step_bytes": head["bytes"],
+                       "l2": "inputs+outputs per step exceed 2x L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": gbs / peaks["hbm_gbs"], "traffic": None,
+                         "peak_source": peaks["source"]},
+            "e2e": e2e,
+            "gpu_launches": args.steps * launches_per_step,
+            "clocks": head["clocks"],
+            "variants": variants,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline()
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks) -> dict:
+    """SpMM L8-R8: A 1024x1024 V=8 sparsity 0.9, B 1024x256, batched instances > 2x L2."""
+    import torch
+
+    from magicube_gb300 import formats, ops, synth
+    M = K = 1024
+    N = 256
+    B = 256
+    mask = synth.uniform_mask(M // VEC, K, VEC, SPARSITY, seed=7)
+    rng = np.random.default_rng(8)
+    vals = rng.integers(0, 256, size=mask.nnz_vec * VEC, dtype=np.uint8)
+    h = formats.prepare_spmm(mask, vals, 8, 8)
+    d = ops.DeviceSpmmLhs.from_host(h, dev)
+    d.values = d.values.repeat(B)  # one value set per instance
+    rhs = torch.from_numpy(rng.integers(0, 256, size=(B, K * N), dtype=np.uint8)).to(dev)
+    out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
+    fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size)
+    sync_all()
+    ms = time_cuda(fn, args.steps, args.warmup, stream)
+    sync_all()
+    t = max_over_ranks(sum(ms) / 1e3) / args.steps
+    opc = 2.0 * mask.nnz_vec * VEC * N * B
+    byts = B * (h.values.size + K * N + M * N * 4) + h.aligned_nnz * 4 + mask.m_vec * 12
+    return {"tops": opc * world / t / 1e12, "ms": t * 1e3, "gbs": byts / t / 1e9,
+            "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"], "instances_per_step": B}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--batch", type=int, default=64, help="instances per step")
+    ap.add_argument("--impl", choices=["magicube_gb300", "reference"], default="magicube_gb300")
+    ap.add_argument("--headline-only", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,136 @@
+/*
+ * magicube_gb300.h -- C ABI of the GB300 (sm_103a) quantized vector-sparse
+ * SpMM / SDDMM library (libmagicube_gb300.so).
+ *
+ * All functions return a cudaError_t value as int: 0 on success,
+ * cudaErrorInvalidValue (1) for rejected arguments (mcGetLastErrorString()
+ * says why), or the CUDA error of the launch.  All pointers passed to compute
+ * entry points are device pointers unless stated otherwise; buffers are owned
+ * by the caller.  Nothing here allocates device memory.
+ *
+ * Storage format (identical to the reference's): a sparse M x K matrix is
+ * stored as m_vec = M / V vector-rows of column vectors of V = 2, 4 or 8
+ * rows.  row_offsets holds 2*m_vec ints, the [start, end) range of each
+ * vector-row in the aligned slot arrays; each start is a multiple of the
+ * alignment (SpMM: 16, or 32 when either operand is 4-bit; SDDMM: 8);
+ * column_indices is aligned the same way and padded with -1.
+ */
+#ifndef MAGICUBE_GB300_H
+#define MAGICUBE_GB300_H
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Text of the last argument error on the calling thread ("" if none). */
+const char* mcGetLastErrorString(void);
+/* Library version, e.g. "0.1.0". */
+const char* mcVersion(void);
+
+/* ---- Reference-compatible SpMM entry points --------------------------------
+ * Same arguments, layouts and unsigned-lane semantics as the reference's
+ * spmm::wmmaSpmm_<P> (SpMM/SpMM/include/wmma_spmm.cuh:14-75), launched on the
+ * legacy default stream.  output_matrix is M x N int32 row-major.
+ * Requires n % 64 == 0.  values is the packer's device layout. */
+int mcWmmaSpmm_4b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                  const int* row_offsets, const int* column_indices, const int* values,
+                  const int* rhs_matrix, int* output_matrix);    /* wmma_spmm.cuh:14 */
+int mcWmmaSpmm_8b4b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                    const int* row_offsets, const int* column_indices, const int* values,
+                    const int* rhs_matrix, int* output_matrix);  /* wmma_spmm.cuh:22 */
+int mcWmmaSpmm_16b4b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                     const int* row_offsets, const int* column_indices, const int* values,
+                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:38 */
+int mcWmmaSpmm_8b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                  const int* row_offsets, const int* column_indices, const int* values,
+                  const int* rhs_matrix, int* output_matrix);    /* wmma_spmm.cuh:46 */
+int mcWmmaSpmm_16b8b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                     const int* row_offsets, const int* column_indices, const int* values,
+                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:62 */
+
+/* ---- Reference-compatible SDDMM entry points -------------------------------
+ * Same arguments, layouts and unsigned-lane semantics as the reference's
+ * sddmm::wmmaSddmm_<P> (SDDMM/SDDMM/src/wmma_sddmm.cu:394,439,488), legacy
+ * default stream.  output_values uses the blocked layout
+ * (j/8)*8*V + 8*v + j%8 over the aligned slots (alignment 8); padding slots of
+ * each vector-row's last group of 8 are written as 0.  Requires k % 64 == 0. */
+int mcWmmaSddmm_4b(int m_vec, int k, int n, const int* row_indices, const int* row_offsets,
+                   const int* column_indices, const int* lhs_matrix, const int* rhs_matrix,
+                   int* output_values, int vec_length);         /* wmma_sddmm.cu:394 */
+int mcWmmaSddmm_8b(int m_vec, int k, int n, const int* row_indices, const int* row_offsets,
+                   const int* column_indices, const int* lhs_matrix, const int* rhs_matrix,
+                   int* output_values, int vec_length);         /* wmma_sddmm.cu:439 */
+int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* row_indices, const int* row_offsets,
+                    const int* column_indices, const int* lhs_matrix, const int* rhs_matrix,
+                    int* output_values, int vec_length);        /* wmma_sddmm.cu:488 */
+
+/* ---- Extended entry points: batch, stream, signedness, dequantised output --
+ * These generalise the reference's batched extension kernels
+ * (batched_wmmaSpmm_* in sparse_transformer_magicube/src/cuda/deq_spmm_kernel.cu,
+ * batched_wmmaSddmm_* in deq_sddmm_kernel.cu): batch entries share one mask and
+ * advance each operand by its stride (a zero stride shares the operand).
+ * is_signed = 1 reads every lane as two's complement (16-bit values: signed
+ * high byte, unsigned low byte); 0 reads lanes unsigned, as the reference's
+ * GPU kernels do.  out_half = 1 writes half(float(acc) / scale). */
+typedef struct mcSpmmDesc {
+    int m_vec, vec_length, n, k;
+    int lhs_bits, rhs_bits;     /* (4,4) (8,4) (16,4) (8,8) (16,8) */
+    int is_signed;
+    int out_half;
+    float scale;
+    int batch;                  /* >= 1 */
+    const int* row_indices;
+    const int* row_offsets;
+    const int* column_indices;
+    const void* values;   long long values_stride;  /* bytes */
+    const void* rhs;      long long rhs_stride;     /* bytes */
+    void* out;            long long out_stride;     /* elements */
+} mcSpmmDesc;
+int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream);
+
+typedef struct mcSddmmDesc {
+    int m_vec, vec_length, n, k;
+    int lhs_bits, rhs_bits;     /* (4,4) (8,8) (16,8) (16,16) */
+    int is_signed;
+    int out_half;
+    int out_vecmajor;           /* 0: blocked (j/8)*8V+8v+j%8; 1: j*V+v */
+    float scale;
+    int batch;
+    int row_split;              /* CTAs per vector-row (0 = automatic) */
+    const int* row_indices;
+    const int* row_offsets;
+    const int* column_indices;
+    const void* lhs;      long long lhs_stride;     /* bytes */
+    const void* rhs;      long long rhs_stride;     /* bytes */
+    void* out;            long long out_stride;     /* elements */
+} mcSddmmDesc;
+int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream);
+
+/* ---- Host-side format conversion (host pointers) ---------------------------
+ * The reference's host packer (SpMM/SpMM/spmm_benchmark.cpp:177-377,
+ * SDDMM/SDDMM/sddmm_benchmark.cpp:104-127) as library routines. */
+
+/* Aligned [start, end) pairs from plain CSR offsets (m_vec+1 entries); returns
+ * the aligned slot count (spmm_benchmark.cpp:177-201), or -1 on error. */
+int mcAlignRowOffsets(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs);
+/* Scatter column indices into the aligned slots, padding with -1; shuffle8 = 1
+ * applies the 4-bit-operand order [c0 c2 c4 c6 c1 c3 c5 c7] per group of 8
+ * (spmm_benchmark.cpp:204-222). */
+int mcPadColumnIndices(int m_vec, const int* row_offsets, const int* col_indices,
+                       const int* aligned_pairs, int aligned_nnz, int shuffle8, int* out_cols);
+/* Pack original per-vector values (V lanes of lhs_bits, lane v at bit
+ * v*lhs_bits) into the SpMM device value layout for the (lhs_bits, rhs_bits)
+ * pair: chunk transpose and bit-plane decomposition (spmm_benchmark.cpp:224-377).
+ * out holds aligned_nnz*V*lhs_bits/8 bytes. */
+int mcPackSpmmValues(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
+                     const int* aligned_pairs, int aligned_nnz, const void* values, void* out);
+/* Vector-row processing order: longest first (bm_test_utils.h:222-237), or identity. */
+int mcSortedRowSwizzle(int m_vec, const int* row_offsets, int* row_indices);
+int mcIdentityRowSwizzle(int m_vec, int* row_indices);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MAGICUBE_GB300_H */

@@ -1,0 +1,96 @@
+"""ctypes binding of libmagicube_gb300.so (the C ABI in include/magicube_gb300.h).
+
+The library is loaded from the package directory.  There is no fallback: if
+the shared object is missing every entry point raises, so a run can never
+silently compute on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().with_name("libmagicube_gb300.so")
+
+_c_int, _c_ll, _c_float, _c_vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_float, ctypes.c_void_p
+
+
+class McSpmmDesc(ctypes.Structure):
+    _fields_ = [
+        ("m_vec", _c_int), ("vec_length", _c_int), ("n", _c_int), ("k", _c_int),
+        ("lhs_bits", _c_int), ("rhs_bits", _c_int), ("is_signed", _c_int), ("out_half", _c_int),
+        ("scale", _c_float), ("batch", _c_int),
+        ("row_indices", _c_vp), ("row_offsets", _c_vp), ("column_indices", _c_vp),
+        ("values", _c_vp), ("values_stride", _c_ll),
+        ("rhs", _c_vp), ("rhs_stride", _c_ll),
+        ("out", _c_vp), ("out_stride", _c_ll),
+    ]
+
+
+class McSddmmDesc(ctypes.Structure):
+    _fields_ = [
+        ("m_vec", _c_int), ("vec_length", _c_int), ("n", _c_int), ("k", _c_int),
+        ("lhs_bits", _c_int), ("rhs_bits", _c_int), ("is_signed", _c_int), ("out_half", _c_int),
+        ("out_vecmajor", _c_int), ("scale", _c_float), ("batch", _c_int), ("row_split", _c_int),
+        ("row_indices", _c_vp), ("row_offsets", _c_vp), ("column_indices", _c_vp),
+        ("lhs", _c_vp), ("lhs_stride", _c_ll),
+        ("rhs", _c_vp), ("rhs_stride", _c_ll),
+        ("out", _c_vp), ("out_stride", _c_ll),
+    ]
+
+
+# name -> (restype, argtypes)
+_IP = ctypes.POINTER(ctypes.c_int)
+_SIGNATURES = {
+    "mcGetLastErrorString": (ctypes.c_char_p, []),
+    "mcVersion": (ctypes.c_char_p, []),
+    "mcSpmm": (_c_int, [ctypes.POINTER(McSpmmDesc), _c_vp]),
+    "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
+    "mcAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp]),
+    "mcPadColumnIndices": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_vp]),
+    "mcPackSpmmValues": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_int, _c_vp, _c_vp]),
+    "mcSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp]),
+    "mcIdentityRowSwizzle": (_c_int, [_c_int, _c_vp]),
+}
+for _p in ("4b", "8b4b", "16b4b", "8b", "16b8b"):
+    _SIGNATURES[f"mcWmmaSpmm_{_p}"] = (_c_int, [_c_int, _c_int, _c_int, _c_int] + [_c_vp] * 6)
+for _p in ("4b", "8b", "16b"):
+    _SIGNATURES[f"mcWmmaSddmm_{_p}"] = (_c_int, [_c_int, _c_int, _c_int] + [_c_vp] * 6 + [_c_int])
+
+_lock = threading.Lock()
+_handle: ctypes.CDLL | None = None
+
+
+class MagicubeError(RuntimeError):
+    """A C-ABI call returned a nonzero status."""
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded library (raises if it has not been built)."""
+    global _handle
+    if _handle is None:
+        with _lock:
+            if _handle is None:
+                if not LIB_PATH.exists():
+                    raise ImportError(
+                        f"{LIB_PATH} is missing: build it with `python -m magicube_gb300.build` "
+                        "(the CUDA library is required; there is no CPU fallback)")
+                h = ctypes.CDLL(str(LIB_PATH))
+                for name, (res, args) in _SIGNATURES.items():
+                    fn = getattr(h, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                _handle = h
+    return _handle
+
+
+def check(rc: int, what: str) -> None:
+    """Raise MagicubeError for a nonzero C-ABI status."""
+    if rc != 0:
+        msg = lib().mcGetLastErrorString().decode() or f"CUDA error {rc}"
+        raise MagicubeError(f"{what} failed: {msg} (status {rc})")
+
+
+def exported_symbols() -> list[str]:
+    """Names of every entry point the binding declares."""
+    return sorted(_SIGNATURES)

@@ -1,0 +1,165 @@
+// capi.cpp -- argument checking and the exported C entry points.
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "mc_host.h"
+
+namespace mc {
+
+static thread_local std::string g_last_error;
+
+int fail(int code, const char* msg)
+{
+    g_last_error = msg;
+    return code;
+}
+void clear_error() { g_last_error.clear(); }
+
+static bool aligned(const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+static int check_spmm(const mcSpmmDesc& d)
+{
+    char buf[256];
+    if (d.m_vec < 0 || d.n <= 0 || d.k <= 0) return fail(1, "mcSpmm: m_vec must be >= 0 and n, k > 0");
+    if (!(d.vec_length == 2 || d.vec_length == 4 || d.vec_length == 8))
+        return fail(1, "mcSpmm: vec_length must be 2, 4 or 8");
+    const bool pair_ok = (d.lhs_bits == 4 && d.rhs_bits == 4) || (d.lhs_bits == 8 && d.rhs_bits == 4) ||
+                         (d.lhs_bits == 16 && d.rhs_bits == 4) || (d.lhs_bits == 8 && d.rhs_bits == 8) ||
+                         (d.lhs_bits == 16 && d.rhs_bits == 8);
+    if (!pair_ok) {
+        std::snprintf(buf, sizeof buf, "mcSpmm: unsupported precision pair L%d-R%d", d.lhs_bits, d.rhs_bits);
+        return fail(1, buf);
+    }
+    if (d.n % 64) return fail(1, "mcSpmm: n must be a multiple of 64");
+    if (d.n / 64 > 65535) return fail(1, "mcSpmm: n too large");
+    if (d.batch < 1 || d.batch > 65535) return fail(1, "mcSpmm: batch must be in [1, 65535]");
+    if (d.out_half && !d.is_signed) return fail(1, "mcSpmm: half output requires is_signed = 1");
+    if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSpmm: half output requires a nonzero scale");
+    if (d.m_vec == 0) return 0;
+    if (!d.row_indices || !d.row_offsets || !d.column_indices || !d.values || !d.rhs || !d.out)
+        return fail(1, "mcSpmm: null pointer");
+    if (!aligned(d.values, 4) || d.values_stride % 4) return fail(1, "mcSpmm: values must be 4-byte aligned");
+    if (!aligned(d.rhs, 16) || d.rhs_stride % 16) return fail(1, "mcSpmm: rhs must be 16-byte aligned");
+    if (!aligned(d.out, d.out_half ? 8 : 16) || d.out_stride % 4)
+        return fail(1, "mcSpmm: output must be 16-byte aligned (8 for half) with stride % 4 == 0");
+    if (d.batch > 1 && (d.values_stride < 0 || d.rhs_stride < 0 || d.out_stride < 0))
+        return fail(1, "mcSpmm: negative stride");
+    return 0;
+}
+
+static int check_sddmm(const mcSddmmDesc& d)
+{
+    char buf[256];
+    if (d.m_vec < 0 || d.n <= 0 || d.k <= 0) return fail(1, "mcSddmm: m_vec must be >= 0 and n, k > 0");
+    if (!(d.vec_length == 2 || d.vec_length == 4 || d.vec_length == 8))
+        return fail(1, "mcSddmm: vec_length must be 2, 4 or 8");
+    const bool pair_ok = (d.lhs_bits == 4 && d.rhs_bits == 4) || (d.lhs_bits == 8 && d.rhs_bits == 8) ||
+                         (d.lhs_bits == 16 && d.rhs_bits == 8) || (d.lhs_bits == 16 && d.rhs_bits == 16);
+    if (!pair_ok) {
+        std::snprintf(buf, sizeof buf, "mcSddmm: unsupported precision pair L%d-R%d", d.lhs_bits, d.rhs_bits);
+        return fail(1, buf);
+    }
+    if (d.k % 64) return fail(1, "mcSddmm: k must be a multiple of 64");
+    if (d.batch < 1 || d.batch > 65535) return fail(1, "mcSddmm: batch must be in [1, 65535]");
+    if (d.row_split < 0 || d.row_split > 65535) return fail(1, "mcSddmm: row_split must be in [0, 65535]");
+    if (d.out_half && (!d.is_signed || !d.out_vecmajor))
+        return fail(1, "mcSddmm: half output requires is_signed = 1 and out_vecmajor = 1");
+    if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSddmm: half output requires a nonzero scale");
+    if (d.m_vec == 0) return 0;
+    if (!d.row_indices || !d.row_offsets || !d.column_indices || !d.lhs || !d.rhs || !d.out)
+        return fail(1, "mcSddmm: null pointer");
+    if (!aligned(d.lhs, 16) || d.lhs_stride % 16) return fail(1, "mcSddmm: lhs must be 16-byte aligned");
+    if (!aligned(d.rhs, 16) || d.rhs_stride % 16) return fail(1, "mcSddmm: rhs must be 16-byte aligned");
+    if (!aligned(d.out, 8) || d.out_stride % 2) return fail(1, "mcSddmm: output must be 8-byte aligned");
+    return 0;
+}
+
+}  // namespace mc
+
+extern "C" {
+
+const char* mcGetLastErrorString(void) { return mc::g_last_error.c_str(); }
+const char* mcVersion(void) { return "0.1.0"; }
+
+int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream)
+{
+    mc::clear_error();
+    if (!desc) return mc::fail(1, "mcSpmm: null descriptor");
+    const mcSpmmDesc& d = *desc;
+    if (int rc = mc::check_spmm(d)) return rc;
+    if (d.m_vec == 0) return 0;
+    if (d.rhs_bits == 4) {
+        if (d.lhs_bits == 4) return mc::spmm_launch_4_4(d, stream);
+        if (d.lhs_bits == 8) return mc::spmm_launch_8_4(d, stream);
+        return mc::spmm_launch_16_4(d, stream);
+    }
+    if (d.lhs_bits == 8) return mc::spmm_launch_8_8(d, stream);
+    return mc::spmm_launch_16_8(d, stream);
+}
+
+int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream)
+{
+    mc::clear_error();
+    if (!desc) return mc::fail(1, "mcSddmm: null descriptor");
+    const mcSddmmDesc& d = *desc;
+    if (int rc = mc::check_sddmm(d)) return rc;
+    if (d.m_vec == 0) return 0;
+    if (d.lhs_bits == 4) return mc::sddmm_launch_4_4(d, stream);
+    if (d.lhs_bits == 8) return mc::sddmm_launch_8_8(d, stream);
+    if (d.rhs_bits == 8) return mc::sddmm_launch_16_8(d, stream);
+    return mc::sddmm_launch_16_16(d, stream);
+}
+
+static int legacy_spmm(int lhs_bits, int rhs_bits, int m_vec, int vec_length, int n, int k,
+                       const int* row_indices, const int* row_offsets, const int* column_indices,
+                       const int* values, const int* rhs_matrix, int* output_matrix)
+{
+    mcSpmmDesc d{};
+    d.m_vec = m_vec; d.vec_length = vec_length; d.n = n; d.k = k;
+    d.lhs_bits = lhs_bits; d.rhs_bits = rhs_bits;
+    d.is_signed = 0; d.out_half = 0; d.scale = 1.0f; d.batch = 1;
+    d.row_indices = row_indices; d.row_offsets = row_offsets; d.column_indices = column_indices;
+    d.values = values; d.rhs = rhs_matrix; d.out = output_matrix;
+    return mcSpmm(&d, 0);
+}
+
+int mcWmmaSpmm_4b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                  const int* values, const int* rhs, int* out)
+{ return legacy_spmm(4, 4, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+int mcWmmaSpmm_8b4b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                    const int* values, const int* rhs, int* out)
+{ return legacy_spmm(8, 4, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+int mcWmmaSpmm_16b4b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                     const int* values, const int* rhs, int* out)
+{ return legacy_spmm(16, 4, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+int mcWmmaSpmm_8b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                  const int* values, const int* rhs, int* out)
+{ return legacy_spmm(8, 8, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+int mcWmmaSpmm_16b8b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                     const int* values, const int* rhs, int* out)
+{ return legacy_spmm(16, 8, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+
+static int legacy_sddmm(int bits, int m_vec, int k, int n, const int* row_indices, const int* row_offsets,
+                        const int* column_indices, const int* lhs, const int* rhs, int* out, int vec_length)
+{
+    mcSddmmDesc d{};
+    d.m_vec = m_vec; d.vec_length = vec_length; d.n = n; d.k = k;
+    d.lhs_bits = bits; d.rhs_bits = bits;
+    d.is_signed = 0; d.out_half = 0; d.out_vecmajor = 0; d.scale = 1.0f; d.batch = 1; d.row_split = 0;
+    d.row_indices = row_indices; d.row_offsets = row_offsets; d.column_indices = column_indices;
+    d.lhs = lhs; d.rhs = rhs; d.out = out;
+    return mcSddmm(&d, 0);
+}
+
+int mcWmmaSddmm_4b(int m_vec, int k, int n, const int* ri, const int* ro, const int* ci, const int* lhs,
+                   const int* rhs, int* out, int vec_length)
+{ return legacy_sddmm(4, m_vec, k, n, ri, ro, ci, lhs, rhs, out, vec_length); }
+int mcWmmaSddmm_8b(int m_vec, int k, int n, const int* ri, const int* ro, const int* ci, const int* lhs,
+                   const int* rhs, int* out, int vec_length)
+{ return legacy_sddmm(8, m_vec, k, n, ri, ro, ci, lhs, rhs, out, vec_length); }
+int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* ri, const int* ro, const int* ci, const int* lhs,
+                    const int* rhs, int* out, int vec_length)
+{ return legacy_sddmm(16, m_vec, k, n, ri, ro, ci, lhs, rhs, out, vec_length); }
+
+}  // extern "C"

@@ -1,0 +1,25 @@
+// mc_host.h -- host-side helpers shared by the C-ABI translation units.
+#pragma once
+#include <cuda_runtime_api.h>
+
+#include "../../include/magicube_gb300.h"
+
+namespace mc {
+
+// Records `msg` as the calling thread's last argument error and returns `code`.
+int fail(int code, const char* msg);
+// Clears the calling thread's last argument error.
+void clear_error();
+
+// Per-precision-pair launchers (one translation unit each).
+int spmm_launch_4_4(const mcSpmmDesc& d, cudaStream_t s);
+int spmm_launch_8_4(const mcSpmmDesc& d, cudaStream_t s);
+int spmm_launch_16_4(const mcSpmmDesc& d, cudaStream_t s);
+int spmm_launch_8_8(const mcSpmmDesc& d, cudaStream_t s);
+int spmm_launch_16_8(const mcSpmmDesc& d, cudaStream_t s);
+int sddmm_launch_4_4(const mcSddmmDesc& d, cudaStream_t s);
+int sddmm_launch_8_8(const mcSddmmDesc& d, cudaStream_t s);
+int sddmm_launch_16_8(const mcSddmmDesc& d, cudaStream_t s);
+int sddmm_launch_16_16(const mcSddmmDesc& d, cudaStream_t s);
+
+}  // namespace mc

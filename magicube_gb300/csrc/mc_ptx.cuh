@@ -1,0 +1,172 @@
+// mc_ptx.cuh -- inline-PTX building blocks for the sm_103a integer kernels.
+//
+// sm_103a has no tcgen05 integer MMA (ptxas rejects tcgen05.mma kind::i8 for
+// this target), so the integer contraction runs on the warp-level
+// mma.sync.m16n8k32 s8/u8 forms, accumulating in int32 without saturation
+// (results wrap modulo 2^32, like the CPU oracle).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+namespace mc {
+
+// D += A * B with A 16x32 (row), B 32x8 (col), int32 accumulators.
+// ASIGNED / BSIGNED pick .s8 or .u8 for each operand.
+template <bool ASIGNED, bool BSIGNED>
+__device__ __forceinline__ void mma_k32(int (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                        uint32_t a3, uint32_t b0, uint32_t b1)
+{
+    if constexpr (ASIGNED && BSIGNED) {
+        asm volatile(
+            "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+            : "+r"(d[0]), "+r"(d[1]), "+r"(d[2]), "+r"(d[3])
+            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+    } else if constexpr (ASIGNED && !BSIGNED) {
+        asm volatile(
+            "mma.sync.aligned.m16n8k32.row.col.s32.s8.u8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+            : "+r"(d[0]), "+r"(d[1]), "+r"(d[2]), "+r"(d[3])
+            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+    } else if constexpr (!ASIGNED && BSIGNED) {
+        asm volatile(
+            "mma.sync.aligned.m16n8k32.row.col.s32.u8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+            : "+r"(d[0]), "+r"(d[1]), "+r"(d[2]), "+r"(d[3])
+            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+    } else {
+        asm volatile(
+            "mma.sync.aligned.m16n8k32.row.col.s32.u8.u8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+            : "+r"(d[0]), "+r"(d[1]), "+r"(d[2]), "+r"(d[3])
+            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+    }
+}
+
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
+{
+    uint32_t r;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(a), "r"(b), "r"(sel));
+    return r;
+}
+
+// 4x4 byte transpose: w[i] holds bytes (i,0..3); on return w[c] holds bytes (0..3,c).
+__device__ __forceinline__ void transpose4x4(uint32_t (&w)[4])
+{
+    uint32_t x0 = prmt(w[0], w[1], 0x5140), x1 = prmt(w[0], w[1], 0x7362);
+    uint32_t y0 = prmt(w[2], w[3], 0x5140), y1 = prmt(w[2], w[3], 0x7362);
+    w[0] = prmt(x0, y0, 0x5410);
+    w[1] = prmt(x0, y0, 0x7632);
+    w[2] = prmt(x1, y1, 0x5410);
+    w[3] = prmt(x1, y1, 0x7632);
+}
+
+// Four zero-extended nibbles in bytes -> sign-extended int4 values in bytes.
+__device__ __forceinline__ uint32_t sext_nibble_bytes(uint32_t z)
+{
+    return z | ((z & 0x08080808u) * 0x1Eu);
+}
+
+// 16 packed nibbles (n0 in bits 0..3) of a 16-bit value -> 4 bytes [n0 n1 n2 n3].
+template <bool SIGNED>
+__device__ __forceinline__ uint32_t unpack4_u16(uint32_t x)
+{
+    uint32_t lo = x & 0x0F0Fu, hi = (x >> 4) & 0x0F0Fu;
+    uint32_t r = prmt(lo, hi, 0x5140);
+    return SIGNED ? sext_nibble_bytes(r) : r;
+}
+
+// 8 packed nibbles of a 32-bit word -> two words of bytes (nibbles 0..3, 4..7).
+template <bool SIGNED>
+__device__ __forceinline__ void unpack4_u32(uint32_t x, uint32_t& out0, uint32_t& out1)
+{
+    uint32_t even = x & 0x0F0F0F0Fu, odd = (x >> 4) & 0x0F0F0F0Fu;
+    out0 = prmt(even, odd, 0x5140);
+    out1 = prmt(even, odd, 0x7362);
+    if (SIGNED) { out0 = sext_nibble_bytes(out0); out1 = sext_nibble_bytes(out1); }
+}
+
+// Combine a low-nibble plane word and a high-nibble plane word (each four
+// nibbles in the low 16 bits) into four bytes (hi << 4 | lo).
+__device__ __forceinline__ uint32_t merge_nibble_planes(uint32_t lo16, uint32_t hi16)
+{
+    uint32_t lo = prmt(lo16 & 0x0F0Fu, (lo16 >> 4) & 0x0F0Fu, 0x5140);
+    uint32_t hi = prmt(hi16 & 0x0F0Fu, (hi16 >> 4) & 0x0F0Fu, 0x5140);
+    return lo | (hi << 4);
+}
+
+// Byte mask keeping the first `valid` (clamped to 0..4) bytes of a word.
+__device__ __forceinline__ uint32_t byte_mask(int valid)
+{
+    return valid >= 4 ? 0xffffffffu : (valid <= 0 ? 0u : ((1u << (8 * valid)) - 1u));
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ uint32_t lds32(const void* p)
+{
+    uint32_t v;
+    asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)));
+    return v;
+}
+__device__ __forceinline__ uint32_t lds16(const void* p)
+{
+    unsigned short v;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(v) : "r"(smem_u32(p)));
+    return v;
+}
+
+__device__ __forceinline__ int4 ldg_nc_v4(const void* p)
+{
+    int4 v;
+    asm volatile("ld.global.nc.v4.s32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int2 ldg_nc_v2(const void* p)
+{
+    int2 v;
+    asm volatile("ld.global.nc.v2.s32 {%0,%1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
+// Streaming stores: outputs are written once and not re-read by this kernel.
+__device__ __forceinline__ void stg_cs_v4(void* p, int a, int b, int c, int d)
+{
+    asm volatile("st.global.cs.v4.s32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+__device__ __forceinline__ void stg_cs_v2(void* p, int a, int b)
+{
+    asm volatile("st.global.cs.v2.s32 [%0], {%1,%2};" ::"l"(p), "r"(a), "r"(b) : "memory");
+}
+__device__ __forceinline__ void stg_cs_s32(void* p, int a)
+{
+    asm volatile("st.global.cs.s32 [%0], %1;" ::"l"(p), "r"(a) : "memory");
+}
+
+// Dequantised half output: half(float(acc) / scale), both steps rounded to
+// nearest -- the epilogue of the reference's extension kernels
+// (sparse_transformer_magicube/src/cuda/spmm_utils/output_tile.h:119).
+__device__ __forceinline__ __half deq_half(int acc, float scale)
+{
+    return __float2half_rn(__fdiv_rn(__int2float_rn(acc), scale));
+}
+__device__ __forceinline__ uint32_t pack_half2(int a, int b, float scale)
+{
+    __half2 h = __halves2half2(deq_half(a, scale), deq_half(b, scale));
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+}  // namespace mc

@@ -1,0 +1,287 @@
+// mc_spmm.cuh -- quantized vector-sparse SpMM for sm_103a.
+//
+// C[M x N] = A[M x K] * B[K x N], A stored in the reference's vector-sparse
+// device layout (column vectors of V rows; see mc_oracle.c / the reference
+// packer SpMM/SpMM/spmm_benchmark.cpp:177-377), B dense row-major with PREB-bit
+// lanes.  Same operand layouts as the reference's spmm::wmmaSpmm_* kernels
+// (SpMM/SpMM/src/wmma_spmm.cu), new kernel design:
+//
+//  * One CTA = one vector-row (through row_indices) x WARPS*32 output columns
+//    x one batch entry.  Each warp owns 32 output columns.
+//  * The contraction runs "transposed": the MMA computes C^T tiles, with the
+//    16-row MMA M dimension walking output columns n and the 8-wide MMA N
+//    dimension holding the V rows of the vector.  The reference's
+//    chunk-transposed value layout ([v][slot] per chunk) is then exactly the
+//    col-major B fragment of mma.m16n8k32, loaded with one 32-bit word per
+//    thread straight from global memory.
+//  * 32 gathered rows of B per step are staged by cp.async 16-byte copies
+//    into a 4-stage shared-memory ring (XOR-swizzled, conflict-free reads);
+//    each thread byte-transposes a 4x4 block with prmt to build the A
+//    fragment (4-bit B rows are unpacked to bytes on the way).
+//  * 16-bit lhs values run as two byte planes (u8 low, s8/u8 high) recombined
+//    by an exact shift-add; 4-bit planes are merged/unpacked to int8 in
+//    registers (sm_103a's fast integer MMA path is the 8-bit one).
+//  * Accumulation wraps modulo 2^32 (no .satfinite): results equal the CPU
+//    oracle bit for bit for every input.
+#pragma once
+#include "mc_ptx.cuh"
+
+namespace mc {
+
+struct SpmmParams {
+    int m_vec, n, k;
+    const int* row_indices;   // m_vec entries: processing order of vector-rows
+    const int* row_offsets;   // 2*m_vec: [start, end) of each vector-row
+    const int* col_indices;   // aligned, -1 padded (shuffled by 8 when MMA_K == 32)
+    const uint8_t* values;    // device value layout
+    long long values_stride;  // bytes between batch entries (0 = shared)
+    const uint8_t* rhs;       // K x N packed, row-major
+    long long rhs_stride;     // bytes between batch entries
+    void* out;                // M x N (int32 or half)
+    long long out_stride;     // elements between batch entries
+    float scale;              // dequantisation divisor for half output
+};
+
+template <int PREA, int PREB>
+struct SpmmLayout {
+    static constexpr int MMA_K = (PREA == 4 || PREB == 4) ? 32 : 16;  // slots per value chunk
+    static constexpr int PLANE_BITS = (PREA == 4 || PREB == 4) ? 4 : 8;
+    static constexpr int PLANES = PREA / PLANE_BITS;                   // bit-planes per chunk
+    static constexpr int BYTE_PLANES = PREA == 16 ? 2 : 1;             // int8 MMA operands
+};
+
+// Shared-memory geometry of one staged gathered-row slice.
+template <int PREB, int WARPS>
+struct RhsSmem {
+    static constexpr int RB = WARPS * 32 * PREB / 8;  // packed bytes per row slice
+    static constexpr int CH = RB / 16;                // 16-byte chunks per row slice
+    static constexpr int STRIDE = (PREB == 8) ? (CH == 8 ? 128 : 80) : (CH == 4 ? 64 : 48);
+    static constexpr int STAGE_BYTES = 32 * STRIDE;
+    __device__ __forceinline__ static int swz(int r, int c)
+    {
+        if constexpr (PREB == 8) {
+            if constexpr (CH == 8) return c ^ (((r >> 2) & 3) << 1);
+            else return c ^ (((r >> 3) & 1) << 1);
+        } else {
+            if constexpr (CH == 4) return c ^ ((r >> 2) & 3);
+            else return c ^ ((r >> 3) & 1);
+        }
+    }
+};
+
+// Logical slot -> stored position of its column index.  With MMA_K == 32 the
+// reference stores each group of 8 as [c0 c2 c4 c6 c1 c3 c5 c7]
+// (spmm_benchmark.cpp:218-222).
+template <int MMA_K>
+__device__ __forceinline__ int col_slot(int j)
+{
+    if constexpr (MMA_K == 32) return (j & ~7) | ((j & 1) << 2) | ((j & 7) >> 1);
+    else return j;
+}
+
+template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT>
+__global__ void __launch_bounds__(WARPS * 32)
+spmm_kernel(const SpmmParams p)
+{
+    using L = SpmmLayout<PREA, PREB>;
+    using S = RhsSmem<PREB, WARPS>;
+    constexpr int STAGES = 4;
+    constexpr int NT = WARPS * 32;
+    constexpr int THREADS = WARPS * 32;
+    constexpr int CHUNKS_PER_THREAD = (32 * S::CH) / THREADS;  // 2 for 8-bit B, 1 for 4-bit B
+    constexpr int BP = L::BYTE_PLANES;
+    constexpr int PLANE_BYTES = V * L::MMA_K * L::PLANE_BITS / 8;
+    constexpr int CHUNK_BYTES = PLANE_BYTES * L::PLANES;
+
+    __shared__ __align__(128) uint8_t rhs_s[STAGES * S::STAGE_BYTES];
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int row = __ldg(p.row_indices + blockIdx.x);
+    const int n0 = blockIdx.y * NT;
+    const int b = blockIdx.z;
+
+    const int start = __ldg(p.row_offsets + 2 * row);
+    const int nnz = __ldg(p.row_offsets + 2 * row + 1) - start;
+    const int steps = (nnz + 31) >> 5;
+
+    const uint8_t* values = p.values + (long long)b * p.values_stride;
+    const uint8_t* rhs = p.rhs + (long long)b * p.rhs_stride + (long long)n0 * PREB / 8;
+    const long long rhs_row_bytes = (long long)p.n * PREB / 8;
+    const int* cols = p.col_indices + start;
+
+    // --- staging of gathered B rows -------------------------------------
+    // Thread copies chunk q = tid + i*THREADS of the 32 x CH chunk grid.
+    int qrow[CHUNKS_PER_THREAD], qch[CHUNKS_PER_THREAD];
+#pragma unroll
+    for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
+        int q = tid + i * THREADS;
+        qrow[i] = q / S::CH;
+        qch[i] = q % S::CH;
+    }
+    auto fetch_cols = [&](int s, int (&c)[CHUNKS_PER_THREAD]) {
+#pragma unroll
+        for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
+            int j = s * 32 + qrow[i];
+            c[i] = (s < steps && j < nnz) ? __ldg(cols + col_slot<L::MMA_K>(j)) : -1;
+        }
+    };
+    auto issue_stage = [&](int s, const int (&c)[CHUNKS_PER_THREAD]) {
+        uint8_t* st = rhs_s + (s % STAGES) * S::STAGE_BYTES;
+#pragma unroll
+        for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
+            if (c[i] >= 0) {
+                const uint8_t* src = rhs + (long long)c[i] * rhs_row_bytes + qch[i] * 16;
+                cp_async16(st + qrow[i] * S::STRIDE + S::swz(qrow[i], qch[i]) * 16, src);
+            }
+        }
+    };
+
+    // --- value fragments (MMA B operand) --------------------------------
+    // vals[bp][h]: byte plane bp, half h (slots 16h + 4t .. +3) for v = g.
+    auto load_vals = [&](int s, uint32_t (&vals)[BP][2]) {
+#pragma unroll
+        for (int bp = 0; bp < BP; ++bp) { vals[bp][0] = 0u; vals[bp][1] = 0u; }
+        if (g >= V || s >= steps) return;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int jrel = s * 32 + 16 * h + 4 * t;  // first slot of this word
+            const int valid = nnz - jrel;
+            if (valid <= 0) continue;
+            const uint32_t keep = byte_mask(valid);
+            const int slot = start + jrel;
+            if constexpr (L::MMA_K == 16) {
+                // 8-bit planes: element (v, j) at byte v*16 + j of its plane.
+                const uint8_t* chunk = values + (long long)(slot >> 4) * CHUNK_BYTES;
+                const int off = g * 16 + (slot & 15);
+#pragma unroll
+                for (int bp = 0; bp < BP; ++bp)
+                    vals[bp][h] = __ldg(reinterpret_cast<const uint32_t*>(chunk + bp * PLANE_BYTES + off)) & keep;
+            } else {
+                // 4-bit planes: element (v, j) at nibble v*32 + j of its plane.
+                const uint8_t* chunk = values + (long long)(slot >> 5) * CHUNK_BYTES;
+                const int off = g * 16 + ((slot & 31) >> 1);
+                uint32_t nib[L::PLANES];
+#pragma unroll
+                for (int pl = 0; pl < L::PLANES; ++pl)
+                    nib[pl] = __ldg(reinterpret_cast<const unsigned short*>(chunk + pl * PLANE_BYTES + off));
+                if constexpr (PREA == 4) {
+                    vals[0][h] = unpack4_u16<SIGNED>(nib[0]) & keep;
+                } else if constexpr (PREA == 8) {
+                    vals[0][h] = merge_nibble_planes(nib[0], nib[1]) & keep;
+                } else {
+                    vals[0][h] = merge_nibble_planes(nib[0], nib[1]) & keep;
+                    vals[1][h] = merge_nibble_planes(nib[2], nib[3]) & keep;
+                }
+            }
+        }
+    };
+
+    int acc[BP][2][4];
+#pragma unroll
+    for (int bp = 0; bp < BP; ++bp)
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[bp][m][e] = 0;
+
+    // Pipeline prologue: column indices run one stage ahead of the copies.
+    int cnext[CHUNKS_PER_THREAD];
+    {
+        int c[CHUNKS_PER_THREAD];
+#pragma unroll
+        for (int s = 0; s < STAGES - 1; ++s) {
+            fetch_cols(s, c);
+            issue_stage(s, c);
+            cp_async_commit();
+        }
+        fetch_cols(STAGES - 1, cnext);
+    }
+    uint32_t vcur[BP][2], vnext[BP][2];
+    load_vals(0, vcur);
+
+    // Column byte (8-bit B) or nibble pair (4-bit B) this thread reads.
+    const int ncol = warp * 32 + 4 * g;
+
+#pragma unroll 1
+    for (int s = 0; s < steps; ++s) {
+        cp_async_wait<STAGES - 2>();
+        __syncthreads();
+        {
+            const int sn = s + STAGES - 1;
+            issue_stage(sn, cnext);
+            cp_async_commit();
+            fetch_cols(sn + 1, cnext);
+        }
+        load_vals(s + 1, vnext);
+
+        const uint8_t* st = rhs_s + (s % STAGES) * S::STAGE_BYTES;
+        uint32_t tr[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = 16 * h + 4 * t + i;
+                if constexpr (PREB == 8) {
+                    const int c = ncol >> 4;
+                    tr[h][i] = lds32(st + r * S::STRIDE + S::swz(r, c) * 16 + (ncol & 15));
+                } else {
+                    const int byte = ncol >> 1;
+                    const int c = byte >> 4;
+                    tr[h][i] = unpack4_u16<SIGNED>(lds16(st + r * S::STRIDE + S::swz(r, c) * 16 + (byte & 15)));
+                }
+            }
+            transpose4x4(tr[h]);
+        }
+        // tr[h][c]: slots 16h+4t..+3 of output column ncol + c.
+#pragma unroll
+        for (int bp = 0; bp < BP; ++bp) {
+            // Only the most significant byte plane of a signed value is signed.
+            const bool top = (bp == BP - 1);
+            if (SIGNED && top) {
+                mma_k32<SIGNED, true>(acc[bp][0], tr[0][0], tr[0][1], tr[1][0], tr[1][1], vcur[bp][0], vcur[bp][1]);
+                mma_k32<SIGNED, true>(acc[bp][1], tr[0][2], tr[0][3], tr[1][2], tr[1][3], vcur[bp][0], vcur[bp][1]);
+            } else {
+                mma_k32<SIGNED, false>(acc[bp][0], tr[0][0], tr[0][1], tr[1][0], tr[1][1], vcur[bp][0], vcur[bp][1]);
+                mma_k32<SIGNED, false>(acc[bp][1], tr[0][2], tr[0][3], tr[1][2], tr[1][3], vcur[bp][0], vcur[bp][1]);
+            }
+        }
+#pragma unroll
+        for (int bp = 0; bp < BP; ++bp) { vcur[bp][0] = vnext[bp][0]; vcur[bp][1] = vnext[bp][1]; }
+    }
+    cp_async_wait<0>();
+
+    // Epilogue.  acc[.][m][e]: column ncol + 2m + (e >> 1), vector lane 2t + (e & 1).
+    int res[2][4];
+#pragma unroll
+    for (int e2 = 0; e2 < 2; ++e2) {
+        // vector lane v = 2t + e2, columns ncol .. ncol+3
+        int c4[4] = {acc[0][0][e2], acc[0][0][2 + e2], acc[0][1][e2], acc[0][1][2 + e2]};
+        if constexpr (BP == 2) {
+            int h4[4] = {acc[1][0][e2], acc[1][0][2 + e2], acc[1][1][e2], acc[1][1][2 + e2]};
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                c4[q] = (int)((uint32_t)c4[q] + ((uint32_t)h4[q] << 8));
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) res[e2][q] = c4[q];
+    }
+#pragma unroll
+    for (int e2 = 0; e2 < 2; ++e2) {
+        const int v = 2 * t + e2;
+        if (v >= V) continue;
+        const long long o = (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + ncol;
+        if constexpr (HALF_OUT) {
+            __half* out = reinterpret_cast<__half*>(p.out) + o;
+            uint32_t h0 = pack_half2(res[e2][0], res[e2][1], p.scale);
+            uint32_t h1 = pack_half2(res[e2][2], res[e2][3], p.scale);
+            stg_cs_v2(out, (int)h0, (int)h1);
+        } else {
+            int* out = reinterpret_cast<int*>(p.out) + o;
+            stg_cs_v4(out, res[e2][0], res[e2][1], res[e2][2], res[e2][3]);
+        }
+    }
+}
+
+}  // namespace mc

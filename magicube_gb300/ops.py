@@ -1,0 +1,124 @@
+"""Device-side calls of the C ABI on torch tensors (current torch stream).
+
+torch provides device memory and streams only; all compute is the CUDA
+library's.  Operands are raw packed integer payloads (uint8 / int32 tensors).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .formats import SddmmMask, SpmmLhs
+
+
+def _stream_handle(stream: torch.cuda.Stream | None = None) -> ctypes.c_void_p:
+    s = torch.cuda.current_stream() if stream is None else stream
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _to_dev(a: np.ndarray, device) -> torch.Tensor:
+    return torch.from_numpy(np.ascontiguousarray(a)).to(device)
+
+
+@dataclass
+class DeviceSpmmLhs:
+    """An SpMM sparse operand resident on the device."""
+
+    m_vec: int
+    vec_length: int
+    k: int
+    lhs_bits: int
+    rhs_bits: int
+    row_indices: torch.Tensor
+    row_offsets: torch.Tensor
+    col_indices: torch.Tensor
+    values: torch.Tensor
+
+    @classmethod
+    def from_host(cls, h: SpmmLhs, device="cuda") -> "DeviceSpmmLhs":
+        cols = h.col_indices if h.col_indices.size else np.full(1, -1, np.int32)
+        vals = h.values if h.values.size else np.zeros(16, np.uint8)
+        return cls(h.mask.m_vec, h.mask.vec_length, h.mask.ncols, h.lhs_bits, h.rhs_bits,
+                   _to_dev(h.row_indices, device), _to_dev(h.row_offsets, device),
+                   _to_dev(cols, device), _to_dev(vals, device))
+
+
+@dataclass
+class DeviceSddmmMask:
+    """An SDDMM output mask resident on the device."""
+
+    m_vec: int
+    vec_length: int
+    n: int
+    aligned_nnz: int
+    row_indices: torch.Tensor
+    row_offsets: torch.Tensor
+    col_indices: torch.Tensor
+
+    @classmethod
+    def from_host(cls, h: SddmmMask, device="cuda") -> "DeviceSddmmMask":
+        cols = h.col_indices if h.col_indices.size else np.full(1, -1, np.int32)
+        return cls(h.mask.m_vec, h.mask.vec_length, h.mask.ncols, h.aligned_nnz,
+                   _to_dev(h.row_indices, device), _to_dev(h.row_offsets, device), _to_dev(cols, device))
+
+
+def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, out: torch.Tensor | None = None,
+         out_half: bool = False, scale: float = 1.0, batch: int = 1, values_stride: int = 0,
+         rhs_stride: int | None = None, out_stride: int | None = None,
+         stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+    """C = A * B for a batch of `batch` entries (shared mask).
+
+    rhs: packed B, k rows of n*rhs_bits/8 bytes per batch entry, contiguous.
+    Strides are in bytes for values/rhs and elements for out; a zero stride
+    shares the operand across the batch."""
+    M = lhs.m_vec * lhs.vec_length
+    if rhs_stride is None:
+        rhs_stride = lhs.k * n * lhs.rhs_bits // 8 if batch > 1 else 0
+    if out_stride is None:
+        out_stride = M * n if batch > 1 else 0
+    if out is None:
+        out = torch.empty((batch, M, n) if batch > 1 else (M, n),
+                          dtype=torch.float16 if out_half else torch.int32, device=rhs.device)
+    d = _lib.McSpmmDesc(
+        m_vec=lhs.m_vec, vec_length=lhs.vec_length, n=n, k=lhs.k, lhs_bits=lhs.lhs_bits, rhs_bits=lhs.rhs_bits,
+        is_signed=int(signed), out_half=int(out_half), scale=scale, batch=batch,
+        row_indices=lhs.row_indices.data_ptr(), row_offsets=lhs.row_offsets.data_ptr(),
+        column_indices=lhs.col_indices.data_ptr(), values=lhs.values.data_ptr(), values_stride=values_stride,
+        rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride)
+    _lib.check(_lib.lib().mcSpmm(ctypes.byref(d), _stream_handle(stream)), "mcSpmm")
+    return out
+
+
+def sddmm(mask: DeviceSddmmMask, lhs: torch.Tensor, rhs: torch.Tensor, k: int, lhs_bits: int, rhs_bits: int, *,
+          signed: bool = True, vecmajor: bool = False, out: torch.Tensor | None = None, out_half: bool = False,
+          scale: float = 1.0, batch: int = 1, lhs_stride: int | None = None, rhs_stride: int | None = None,
+          out_stride: int | None = None, row_split: int = 0,
+          stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+    """out = (A * B^T) on the mask's stored nonzero vectors.
+
+    lhs: packed A (M rows of k*lhs_bits/8 bytes), rhs: packed B (n rows of
+    k*rhs_bits/8 bytes), per batch entry.  Output: aligned_nnz * V values per
+    batch entry, blocked (alignment 8) or vector-major layout."""
+    M = mask.m_vec * mask.vec_length
+    if lhs_stride is None:
+        lhs_stride = M * k * lhs_bits // 8 if batch > 1 else 0
+    if rhs_stride is None:
+        rhs_stride = mask.n * k * rhs_bits // 8 if batch > 1 else 0
+    per = mask.aligned_nnz * mask.vec_length
+    if out_stride is None:
+        out_stride = per if batch > 1 else 0
+    if out is None:
+        shape = (batch, per) if batch > 1 else (per,)
+        out = torch.zeros(shape, dtype=torch.float16 if out_half else torch.int32, device=lhs.device)
+    d = _lib.McSddmmDesc(
+        m_vec=mask.m_vec, vec_length=mask.vec_length, n=mask.n, k=k, lhs_bits=lhs_bits, rhs_bits=rhs_bits,
+        is_signed=int(signed), out_half=int(out_half), out_vecmajor=int(vecmajor), scale=scale, batch=batch,
+        row_split=row_split, row_indices=mask.row_indices.data_ptr(), row_offsets=mask.row_offsets.data_ptr(),
+        column_indices=mask.col_indices.data_ptr(), lhs=lhs.data_ptr(), lhs_stride=lhs_stride,
+        rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride)
+    _lib.check(_lib.lib().mcSddmm(ctypes.byref(d), _stream_handle(stream)), "mcSddmm")
+    return out

@@ -1,0 +1,93 @@
+"""SDDMM parity on the GPU: the CUDA library against the CPU oracle (bit-exact)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from magicube_gb300 import _lib, formats, ops, synth
+
+pytestmark = pytest.mark.gpu
+
+PAIRS = [(4, 4), (8, 8), (16, 8), (16, 16)]
+RAGGED = [0, 1, 7, 8, 9, 15, 16, 17, 33, 64, 100, 5, 250, 0, 31, 40]
+
+
+def _case(pa, pb, V, K, N, lengths, seed):
+    mask = synth.lengths_mask(lengths, N, V, seed=seed)
+    lhs = synth.random_bytes(mask.rows * K * pa // 8, seed + 1)
+    rhs = synth.random_bytes(N * K * pb // 8, seed + 2)
+    return mask, lhs, rhs
+
+
+@pytest.mark.parametrize("pa,pb", PAIRS)
+@pytest.mark.parametrize("V", [2, 4, 8])
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("K", [64, 192])
+@pytest.mark.parametrize("vecmajor", [False, True])
+def test_sddmm_ragged(cuda, pa, pb, V, signed, K, vecmajor):
+    N = 256
+    mask, lhs, rhs = _case(pa, pb, V, K, N, RAGGED, seed=pa + pb + V + K)
+    align = 16 if vecmajor else 8
+    hm = formats.prepare_sddmm(mask, alignment=align)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, pa, pb,
+                    signed=signed, vecmajor=vecmajor)
+    ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, pa, pb,
+                            oracle.SIGNED if signed else oracle.UNSIGNED, alignment=8,
+                            layout=oracle.OUT_VECMAJOR if vecmajor else oracle.OUT_BLOCKED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", PAIRS)
+def test_sddmm_batched(cuda, pa, pb):
+    V, K, N, B = 8, 64, 512, 3
+    mask = synth.normal_mask(16, N, V, 0.8, seed=3)
+    hm = formats.prepare_sddmm(mask)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    lhs_all = [synth.random_bytes(mask.rows * K * pa // 8, 30 + b) for b in range(B)]
+    rhs_all = [synth.random_bytes(N * K * pb // 8, 40 + b) for b in range(B)]
+    out = ops.sddmm(dm, torch.from_numpy(np.concatenate(lhs_all)).to(cuda),
+                    torch.from_numpy(np.concatenate(rhs_all)).to(cuda), K, pa, pb, signed=True, batch=B)
+    for b in range(B):
+        ref = oracle.sddmm_host(lhs_all[b], rhs_all[b], hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N,
+                                pa, pb, oracle.SIGNED)
+        np.testing.assert_array_equal(out[b].cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", [(4, 4), (8, 8)])
+def test_sddmm_half_vecmajor(cuda, pa, pb):
+    V, K, N, scale = 8, 64, 256, 36.0 * 36.0
+    mask, lhs, rhs = _case(pa, pb, V, K, N, RAGGED, seed=9)
+    hm = formats.prepare_sddmm(mask, alignment=16)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, pa, pb, signed=True,
+                    vecmajor=True, out_half=True, scale=scale)
+    acc = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, pa, pb, oracle.SIGNED,
+                            layout=oracle.OUT_VECMAJOR)
+    ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
+    got = out.cpu().numpy()
+    # padding slots (never written by either side) are compared only where the oracle wrote
+    written = np.zeros(acc.size, bool)
+    for i in range(mask.m_vec):
+        s, e = hm.row_offsets[2 * i], hm.row_offsets[2 * i + 1]
+        written[s * V:e * V] = True
+    np.testing.assert_array_equal(got[written].view(np.uint16), ref[written].view(np.uint16))
+
+
+@pytest.mark.parametrize("name,bits", [("4b", 4), ("8b", 8), ("16b", 16)])
+def test_reference_entry_points(cuda, name, bits):
+    """mcWmmaSddmm_<P>: reference argument list, unsigned lanes, blocked output."""
+    V, K, N = 8, 128, 256
+    mask, lhs, rhs = _case(bits, bits, V, K, N, RAGGED, seed=13)
+    hm = formats.prepare_sddmm(mask)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    lt, rt = torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda)
+    out = torch.zeros(hm.aligned_nnz * V, dtype=torch.int32, device=cuda)
+    torch.cuda.synchronize()
+    fn = getattr(_lib.lib(), f"mcWmmaSddmm_{name}")
+    _lib.check(fn(mask.m_vec, K, N, dm.row_indices.data_ptr(), dm.row_offsets.data_ptr(), dm.col_indices.data_ptr(),
+                  lt.data_ptr(), rt.data_ptr(), out.data_ptr(), V), name)
+    torch.cuda.synchronize()
+    ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, bits, bits,
+                            oracle.UNSIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)

@@ -1,0 +1,65 @@
+"""The C-ABI library: loads, exports every entry point the public header
+declares, and rejects bad arguments before touching a GPU.  CPU only."""
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from magicube_gb300 import _lib
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "magicube_gb300.h"
+
+
+def declared_functions() -> list[str]:
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    return sorted(set(re.findall(r"\b(mc[A-Z]\w*)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.lib()
+    names = declared_functions()
+    assert len(names) >= 17
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    assert set(declared_functions()) <= set(_lib.exported_symbols())
+
+
+def test_version():
+    assert _lib.lib().mcVersion().decode().count(".") == 2
+
+
+@pytest.mark.parametrize("field,value,msg", [
+    ("vec_length", 3, b"vec_length"), ("n", 100, b"multiple of 64"), ("lhs_bits", 4, b"precision"),
+    ("batch", 0, b"batch"), ("out_half", 1, b"is_signed")])
+def test_spmm_argument_errors(field, value, msg):
+    d = _lib.McSpmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1, scale=1.0)
+    setattr(d, field, value)
+    if field == "lhs_bits":
+        d.rhs_bits = 8
+    assert _lib.lib().mcSpmm(ctypes.byref(d), None) == 1
+    assert msg in _lib.lib().mcGetLastErrorString()
+
+
+@pytest.mark.parametrize("field,value,msg", [
+    ("k", 96, b"multiple of 64"), ("vec_length", 16, b"vec_length"), ("rhs_bits", 4, b"precision"),
+    ("out_half", 1, b"half output")])
+def test_sddmm_argument_errors(field, value, msg):
+    d = _lib.McSddmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1, scale=1.0)
+    setattr(d, field, value)
+    assert _lib.lib().mcSddmm(ctypes.byref(d), None) == 1
+    assert msg in _lib.lib().mcGetLastErrorString()
+
+
+def test_null_pointers_rejected():
+    d = _lib.McSpmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1)
+    assert _lib.lib().mcSpmm(ctypes.byref(d), None) == 1
+    assert b"null" in _lib.lib().mcGetLastErrorString()
+
+
+def test_empty_matrix_is_a_no_op():
+    d = _lib.McSpmmDesc(m_vec=0, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1)
+    assert _lib.lib().mcSpmm(ctypes.byref(d), None) == 0

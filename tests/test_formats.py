@@ -1,0 +1,55 @@
+"""Host-side format code: .smtx round trip and packer edge cases.  CPU only."""
+import numpy as np
+import pytest
+
+import oracle
+from magicube_gb300 import formats, smtx, synth
+
+
+def test_smtx_round_trip(tmp_path):
+    m = synth.normal_mask(33, 500, 4, 0.7, seed=3)
+    smtx.write(tmp_path / "m.smtx", m)
+    r = smtx.read(tmp_path / "m.smtx", 4)
+    assert (r.m_vec, r.ncols) == (33, 500)
+    np.testing.assert_array_equal(r.row_offsets, m.row_offsets)
+    np.testing.assert_array_equal(r.col_indices, m.col_indices)
+
+
+def test_smtx_rejects_malformed(tmp_path):
+    p = tmp_path / "bad.smtx"
+    p.write_text("2, 10, 3\n0 2 1\n1 2 3\n")
+    with pytest.raises(ValueError):
+        smtx.read(p, 2)
+    p.write_text("1, 4, 2\n0 2\n1 9\n")
+    with pytest.raises(ValueError):
+        smtx.read(p, 2)
+
+
+@pytest.mark.parametrize("alignment", [8, 16, 32])
+def test_alignment_edges(alignment):
+    m = synth.lengths_mask([0, 1, alignment - 1, alignment, alignment + 1, 0], 256, 8, seed=1)
+    pairs, n = formats.align_row_offsets(m, alignment)
+    assert n % alignment == 0
+    assert np.all(pairs[0::2] % alignment == 0)
+    np.testing.assert_array_equal(pairs[1::2] - pairs[0::2], m.row_lengths())
+
+
+@pytest.mark.parametrize("pa,pb", [(4, 4), (8, 4), (16, 4), (8, 8), (16, 8)])
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_pack_then_decode_equals_oracle(pa, pb, V):
+    """Packer + the oracle's device-layout decoder == oracle on the original layout."""
+    K, N = 128, 64
+    m = synth.lengths_mask([0, 1, 31, 32, 33, 100, 7], K, V, seed=pa + pb + V)
+    vals = synth.random_bytes(m.nnz_vec * V * pa // 8, 1)
+    rhs = synth.random_bytes(K * N * pb // 8, 2)
+    h = formats.prepare_spmm(m, vals, pa, pb)
+    for mode in (oracle.UNSIGNED, oracle.SIGNED):
+        a = oracle.spmm_host(vals, rhs, m.row_offsets, m.col_indices, m.m_vec, V, K, N, pa, pb, mode)
+        b = oracle.spmm_device(h.row_offsets, h.col_indices, h.values, rhs, m.m_vec, V, K, N, pa, pb, mode)
+        np.testing.assert_array_equal(a, b)
+
+
+def test_empty_matrix_packs():
+    m = synth.lengths_mask([0, 0, 0], 64, 4, seed=1)
+    h = formats.prepare_spmm(m, np.zeros(0, np.uint8), 8, 8)
+    assert h.aligned_nnz == 0 and h.values.size == 0

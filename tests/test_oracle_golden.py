@@ -1,0 +1,76 @@
+"""The oracle and the host packer against fixtures produced by the reference
+itself (tests/golden, see make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import load, names, unpack_spmm_values
+from magicube_gb300 import formats
+from magicube_gb300.formats import VectorSparse
+
+
+@pytest.mark.parametrize("name", names("routine_spmm_"))
+def test_oracle_literal_equals_reference_spmm_routine(name):
+    """compute_ref_integers (reference, compiled from its sources) on full-range
+    random data == the oracle's literal mode, bit for bit."""
+    d = load(name)
+    got = oracle.spmm_host(d["values"], d["rhs"], d["row_offsets"], d["col_indices"], int(d["m_vec"]), int(d["V"]),
+                           int(d["K"]), int(d["N"]), int(d["preA"]), int(d["preB"]), oracle.LITERAL)
+    np.testing.assert_array_equal(got.ravel(), d["out"])
+
+
+@pytest.mark.parametrize("name", names("routine_spmm_"))
+def test_reference_top_lane_quirk_is_visible(name):
+    """On full-range data the reference routine's sign-extended top rhs lane
+    makes it differ from purely unsigned lanes (the GPU kernels' semantics)."""
+    d = load(name)
+    args = (d["values"], d["rhs"], d["row_offsets"], d["col_indices"], int(d["m_vec"]), int(d["V"]), int(d["K"]),
+            int(d["N"]), int(d["preA"]), int(d["preB"]))
+    lit = oracle.spmm_host(*args, oracle.LITERAL)
+    uns = oracle.spmm_host(*args, oracle.UNSIGNED)
+    if int(d["row_offsets"][-1]) > 0:
+        assert not np.array_equal(lit, uns)
+
+
+@pytest.mark.parametrize("name", names("routine_sddmm_"))
+def test_oracle_literal_equals_reference_sddmm_routine(name):
+    d = load(name)
+    got = oracle.sddmm_host(d["lhs"], d["rhs"], d["row_offsets"], d["col_indices"], int(d["m_vec"]), int(d["V"]),
+                            int(d["K"]), int(d["N"]), int(d["bits"]), int(d["bits"]), oracle.LITERAL)
+    np.testing.assert_array_equal(got, d["out"])
+
+
+@pytest.mark.parametrize("name", names("ref_spmm_"))
+def test_packer_and_oracle_against_reference_spmm_program(name):
+    """A run of the reference's spmm_benchmark: its host packer's device arrays
+    equal ours, and its result (verified PASS by the reference itself against
+    its host routine) equals the oracle on the recovered original values."""
+    d = load(name)
+    assert str(d["verdict"]) == "PASS"
+    V, K, N, pa, pb = (int(d[k]) for k in ("V", "K", "N", "preA", "preB"))
+    mask = VectorSparse(int(d["m_vec"]), V, K, d["csr_row_offsets"], d["csr_col_indices"])
+    chunk = formats.spmm_chunk(pa, pb)
+    pairs, n = formats.align_row_offsets(mask, chunk)
+    np.testing.assert_array_equal(pairs, d["row_offsets"])
+    np.testing.assert_array_equal(formats.pad_column_indices(mask, pairs, n, chunk == 32), d["col_indices"])
+    np.testing.assert_array_equal(formats.sorted_row_swizzle(mask), d["row_indices"])
+    orig = unpack_spmm_values(d["values"], pairs, mask.row_offsets, V, pa, pb)
+    np.testing.assert_array_equal(formats.pack_spmm_values(mask, pairs, n, orig, pa, pb), d["values"])
+    got = oracle.spmm_host(orig, d["rhs"], mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
+                           oracle.LITERAL)
+    np.testing.assert_array_equal(got.ravel(), d["out"])
+
+
+@pytest.mark.parametrize("name", names("ref_sddmm_"))
+def test_oracle_against_reference_sddmm_program(name):
+    d = load(name)
+    assert str(d["verdict"]) == "PASS"
+    V, K, N, bits = (int(d[k]) for k in ("V", "K", "N", "bits"))
+    mask = VectorSparse(int(d["m_vec"]), V, N, d["csr_row_offsets"], d["csr_col_indices"])
+    pairs, n = formats.align_row_offsets(mask, 8)
+    np.testing.assert_array_equal(pairs, d["row_offsets"])
+    np.testing.assert_array_equal(formats.pad_column_indices(mask, pairs, n, False), d["col_indices"])
+    np.testing.assert_array_equal(formats.sorted_row_swizzle(mask), d["row_indices"])
+    got = oracle.sddmm_host(d["lhs"], d["rhs"], pairs, d["col_indices"], mask.m_vec, V, K, N, bits, bits,
+                            oracle.LITERAL)
+    np.testing.assert_array_equal(got, d["out"])

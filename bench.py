@@ -30,6 +30,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+MMA_NAMES = {1: "int8mma", 2: "f16mma"}
 METRIC = "quantized SpMM/SDDMM TOP/s vs roofline; sparse-attn req/s + p50/p99 latency"
 UNIT = "TOP/s"
 SEQ, HEAD_DIM, VEC, SPARSITY = 4096, 64, 8, 0.9
@@ -242,13 +243,14 @@ def run_gpu(args) -> None:
     results = {}
     launches_per_step = 1
 
-    def sddmm_case(pa, pb, timed_region_clock=False):
+    def sddmm_case(pa, pb, timed_region_clock=False, mma=args.mma, variant=0):
         mask, hm, lhs_h, rhs_h = sddmm_workload(pa, pb, B)
         dm = ops.DeviceSddmmMask.from_host(hm, dev)
         lhs = torch.from_numpy(lhs_h).to(dev)
         rhs = torch.from_numpy(rhs_h).to(dev)
         out = torch.empty((B, hm.aligned_nnz * VEC), dtype=torch.int32, device=dev)
-        fn = lambda: ops.sddmm(dm, lhs, rhs, HEAD_DIM, pa, pb, signed=True, out=out, batch=B)
+        fn = lambda: ops.sddmm(dm, lhs, rhs, HEAD_DIM, pa, pb, signed=True, out=out, batch=B, mma_kind=mma,
+                                    variant=variant)
         sync_all()
         if timed_region_clock:
             with ClockSampler(local) as cs:
@@ -276,7 +278,8 @@ def run_gpu(args) -> None:
     def e2e_step():
         head["lhs"].copy_(lhs_pin, non_blocking=True)
         head["rhs"].copy_(rhs_pin, non_blocking=True)
-        ops.sddmm(dm, head["lhs"], head["rhs"], HEAD_DIM, 8, 8, signed=True, out=head["out"], batch=B)
+        ops.sddmm(dm, head["lhs"], head["rhs"], HEAD_DIM, 8, 8, signed=True, out=head["out"], batch=B,
+                  mma_kind=args.mma)
         out_pin.copy_(head["out"], non_blocking=True)
 
     e2e_steps = max(3, args.steps // 4)
@@ -291,13 +294,19 @@ def run_gpu(args) -> None:
 
     variants = {}
     if not args.headline_only:
-        for pa, pb, name in [(4, 4, "sddmm_L4R4"), (16, 8, "sddmm_L16R8")]:
-            r = sddmm_case(pa, pb)
+        alt = 1 if args.mma == 2 else 2
+        for pa, pb, name, mma, var in [(4, 4, "sddmm_L4R4", args.mma, 0), (16, 8, "sddmm_L16R8", args.mma, 0),
+                                       (8, 8, f"sddmm_L8R8_{MMA_NAMES[alt]}", alt, 0),
+                                       (8, 8, "sddmm_L8R8_per_row_kernel", args.mma, 1)]:
+            r = sddmm_case(pa, pb, mma=mma, variant=var)
             variants[name] = {"tops": r["tops"], "ms": r["ms"], "gbs": r["gbs"],
                               "hbm_frac": r["gbs"] / peaks["hbm_gbs"]}
             del r
             torch.cuda.empty_cache()
-        variants["spmm_L8R8_1024x1024x256"] = spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks)
+        for mma, var, tag in ((args.mma, 0, MMA_NAMES[args.mma]), (alt, 0, MMA_NAMES[alt]),
+                              (args.mma, 1, "per_row_kernel")):
+            variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
+                args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
 
     if rank == 0:
         gbs = head["gbs"]
@@ -307,6 +316,7 @@ def run_gpu(args) -> None:
             "vs_baseline": None, "dtype": "int8", "data": "synthetic",
             "config": {"workload": "SDDMM L8-R8: A,B 4096x64 int8, mask 4096x4096 V=8 sparsity 0.9 uniform, "
                                    "int32 out, signed lanes",
+                       "tensor_path": MMA_NAMES[args.mma],
                        "instances_per_step": B, "step_bytes": head["bytes"],
                        "l2": "inputs+outputs per step exceed 2x L2 (no flush)", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -324,7 +334,7 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
-def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks) -> dict:
+def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma: int, variant: int = 0) -> dict:
     """SpMM L8-R8: A 1024x1024 V=8 sparsity 0.9, B 1024x256, batched instances > 2x L2."""
     import torch
 
@@ -340,7 +350,8 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks) -> d
     d.values = d.values.repeat(B)  # one value set per instance
     rhs = torch.from_numpy(rng.integers(0, 256, size=(B, K * N), dtype=np.uint8)).to(dev)
     out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
-    fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size)
+    fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size, mma_kind=mma,
+                          variant=variant)
     sync_all()
     ms = time_cuda(fn, args.steps, args.warmup, stream)
     sync_all()
@@ -359,10 +370,13 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=64, help="instances per step")
     ap.add_argument("--impl", choices=["magicube_gb300", "reference"], default="magicube_gb300")
     ap.add_argument("--headline-only", action="store_true")
+    ap.add_argument("--mma", choices=["int8", "f16"], default="int8",
+                    help="tensor path (both are bit-exact; see include/magicube_gb300.h)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    args.mma = 2 if args.mma == "f16" else 1
     if args.impl == "reference":
         run_reference(args)
     else:

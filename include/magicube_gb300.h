@@ -66,6 +66,27 @@ int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* row_indices, const int* 
                     const int* column_indices, const int* lhs_matrix, const int* rhs_matrix,
                     int* output_values, int vec_length);        /* wmma_sddmm.cu:488 */
 
+/* ---- Tensor path ------------------------------------------------------------
+ * Both tensor paths give bit-identical integer results.
+ * MC_MMA_INT8: mma.sync m16n8k32 s8/u8 with int32 accumulation.
+ * MC_MMA_F16:  operand bytes converted exactly to f16, mma.sync m16n8k16 with
+ *              f32 accumulation flushed into int32 every 256 products (every
+ *              partial sum is an integer below 2^24, so nothing rounds); on
+ *              sm_103a the f16 tensor rate is several times the int8 one.
+ * MC_MMA_DEFAULT selects the library default (mcSetDefaultMmaKind). */
+enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2 };
+/* Sets the default tensor path; returns the previous one (or -1 if invalid). */
+int mcSetDefaultMmaKind(int kind);
+
+/* ---- Kernel variant ---------------------------------------------------------
+ * MC_KERNEL_PER_ROW: one CTA per (vector-row, column tile / row split, batch
+ *                    entry); any k.
+ * MC_KERNEL_STREAM:  persistent CTAs (SpMM) or warps (SDDMM) that stream many
+ *                    vector-rows through one software pipeline; SpMM needs
+ *                    16-byte aligned values, SDDMM needs k == 64.
+ * MC_KERNEL_AUTO:    the streaming kernel where it applies, else per-row. */
+enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2 };
+
 /* ---- Extended entry points: batch, stream, signedness, dequantised output --
  * These generalise the reference's batched extension kernels
  * (batched_wmmaSpmm_* in sparse_transformer_magicube/src/cuda/deq_spmm_kernel.cu,
@@ -87,6 +108,8 @@ typedef struct mcSpmmDesc {
     const void* values;   long long values_stride;  /* bytes */
     const void* rhs;      long long rhs_stride;     /* bytes */
     void* out;            long long out_stride;     /* elements */
+    int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
+    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM */
 } mcSpmmDesc;
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream);
 
@@ -105,6 +128,8 @@ typedef struct mcSddmmDesc {
     const void* lhs;      long long lhs_stride;     /* bytes */
     const void* rhs;      long long rhs_stride;     /* bytes */
     void* out;            long long out_stride;     /* elements */
+    int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
+    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM */
 } mcSddmmDesc;
 int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream);
 

@@ -24,6 +24,7 @@ class McSpmmDesc(ctypes.Structure):
         ("values", _c_vp), ("values_stride", _c_ll),
         ("rhs", _c_vp), ("rhs_stride", _c_ll),
         ("out", _c_vp), ("out_stride", _c_ll),
+        ("mma_kind", _c_int), ("kernel_variant", _c_int),
     ]
 
 
@@ -36,14 +37,19 @@ class McSddmmDesc(ctypes.Structure):
         ("lhs", _c_vp), ("lhs_stride", _c_ll),
         ("rhs", _c_vp), ("rhs_stride", _c_ll),
         ("out", _c_vp), ("out_stride", _c_ll),
+        ("mma_kind", _c_int), ("kernel_variant", _c_int),
     ]
 
+
+MMA_DEFAULT, MMA_INT8, MMA_F16 = 0, 1, 2
+KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM = 0, 1, 2
 
 # name -> (restype, argtypes)
 _IP = ctypes.POINTER(ctypes.c_int)
 _SIGNATURES = {
     "mcGetLastErrorString": (ctypes.c_char_p, []),
     "mcVersion": (ctypes.c_char_p, []),
+    "mcSetDefaultMmaKind": (_c_int, [_c_int]),
     "mcSpmm": (_c_int, [ctypes.POINTER(McSpmmDesc), _c_vp]),
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
     "mcAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp]),

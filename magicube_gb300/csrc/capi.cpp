@@ -1,4 +1,5 @@
 // capi.cpp -- argument checking and the exported C entry points.
+#include <atomic>
 #include <cstdint>
 #include <cstdio>
 #include <string>
@@ -8,6 +9,9 @@
 namespace mc {
 
 static thread_local std::string g_last_error;
+static std::atomic<int> g_default_mma{MC_MMA_INT8};
+
+int default_mma_kind() { return g_default_mma.load(std::memory_order_relaxed); }
 
 int fail(int code, const char* msg)
 {
@@ -36,6 +40,9 @@ static int check_spmm(const mcSpmmDesc& d)
     if (d.batch < 1 || d.batch > 65535) return fail(1, "mcSpmm: batch must be in [1, 65535]");
     if (d.out_half && !d.is_signed) return fail(1, "mcSpmm: half output requires is_signed = 1");
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSpmm: half output requires a nonzero scale");
+    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16) return fail(1, "mcSpmm: invalid mma_kind");
+    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_STREAM)
+        return fail(1, "mcSpmm: invalid kernel_variant");
     if (d.m_vec == 0) return 0;
     if (!d.row_indices || !d.row_offsets || !d.column_indices || !d.values || !d.rhs || !d.out)
         return fail(1, "mcSpmm: null pointer");
@@ -66,6 +73,9 @@ static int check_sddmm(const mcSddmmDesc& d)
     if (d.out_half && (!d.is_signed || !d.out_vecmajor))
         return fail(1, "mcSddmm: half output requires is_signed = 1 and out_vecmajor = 1");
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSddmm: half output requires a nonzero scale");
+    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16) return fail(1, "mcSddmm: invalid mma_kind");
+    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_STREAM)
+        return fail(1, "mcSddmm: invalid kernel_variant");
     if (d.m_vec == 0) return 0;
     if (!d.row_indices || !d.row_offsets || !d.column_indices || !d.lhs || !d.rhs || !d.out)
         return fail(1, "mcSddmm: null pointer");
@@ -81,6 +91,12 @@ extern "C" {
 
 const char* mcGetLastErrorString(void) { return mc::g_last_error.c_str(); }
 const char* mcVersion(void) { return "0.1.0"; }
+
+int mcSetDefaultMmaKind(int kind)
+{
+    if (kind != MC_MMA_INT8 && kind != MC_MMA_F16) return -1;
+    return mc::g_default_mma.exchange(kind);
+}
 
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream)
 {

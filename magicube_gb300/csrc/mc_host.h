@@ -6,6 +6,10 @@
 
 namespace mc {
 
+// Tensor path used by a call whose descriptor asks for MC_MMA_DEFAULT.
+int default_mma_kind();
+inline int resolve_mma_kind(int k) { return k == MC_MMA_DEFAULT ? default_mma_kind() : k; }
+
 // Records `msg` as the calling thread's last argument error and returns `code`.
 int fail(int code, const char* msg);
 // Clears the calling thread's last argument error.

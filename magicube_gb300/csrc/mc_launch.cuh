@@ -4,19 +4,77 @@
 #pragma once
 #include "mc_host.h"
 #include "mc_sddmm.cuh"
+#include "mc_sddmm_stream.cuh"
 #include "mc_spmm.cuh"
+#include "mc_spmm_stream.cuh"
 
 namespace mc {
+
+// Number of SMs of the current device (cached per device).
+inline int sm_count()
+{
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
+// Persistent grid: resident CTAs of `kernel` over all SMs, capped by the work.
+template <typename K>
+inline int persistent_ctas(K kernel, int threads, long long work_ctas)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    long long n = (long long)per_sm * sm_count();
+    if (n > work_ctas) n = work_ctas;
+    if (n > 0x7fffffffLL) n = 0x7fffffffLL;
+    return n < 1 ? 1 : (int)n;
+}
+
+template <int V, int PA, int PB, bool S, bool H, int W, bool F>
+int spmm_launch_stream(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
+{
+    const long long ntasks = (long long)d.m_vec * d.batch;
+    if (ntasks > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
+    const int ny = d.n / (W * 32);
+    auto kern = spmm_stream_kernel<V, PA, PB, S, W, H, F>;
+    // resident CTAs over all SMs, split across the ny column tiles
+    const long long resident = persistent_ctas(kern, W * 32, 0x7fffffffLL);
+    long long gx = (resident + ny - 1) / ny;
+    if (gx > ntasks) gx = ntasks;
+    dim3 grid((unsigned)(gx < 1 ? 1 : gx), (unsigned)ny, 1);
+    kern<<<grid, W * 32, 0, s>>>(p, (int)ntasks);
+    return (int)cudaGetLastError();
+}
 
 template <int V, int PA, int PB, bool S, bool H>
 int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
+    const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
+    const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
+    if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
+        return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");
+    if (d.kernel_variant != MC_KERNEL_PER_ROW && stream_ok) {
+        if (d.n % 128 == 0)
+            return f16 ? spmm_launch_stream<V, PA, PB, S, H, 4, true>(d, p, s)
+                       : spmm_launch_stream<V, PA, PB, S, H, 4, false>(d, p, s);
+        return f16 ? spmm_launch_stream<V, PA, PB, S, H, 2, true>(d, p, s)
+                   : spmm_launch_stream<V, PA, PB, S, H, 2, false>(d, p, s);
+    }
     if (d.n % 128 == 0) {
         dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 128), (unsigned)d.batch);
-        spmm_kernel<V, PA, PB, S, 4, H><<<grid, 128, 0, s>>>(p);
+        if (f16) spmm_kernel<V, PA, PB, S, 4, H, true><<<grid, 128, 0, s>>>(p);
+        else spmm_kernel<V, PA, PB, S, 4, H, false><<<grid, 128, 0, s>>>(p);
     } else {
         dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 64), (unsigned)d.batch);
-        spmm_kernel<V, PA, PB, S, 2, H><<<grid, 64, 0, s>>>(p);
+        if (f16) spmm_kernel<V, PA, PB, S, 2, H, true><<<grid, 64, 0, s>>>(p);
+        else spmm_kernel<V, PA, PB, S, 2, H, false><<<grid, 64, 0, s>>>(p);
     }
     return (int)cudaGetLastError();
 }
@@ -43,11 +101,31 @@ int spmm_launch(const mcSpmmDesc& d, cudaStream_t s)
 #undef MC_V
 }
 
+template <int V, int PA, int PB, bool S, bool VM, bool H, bool F>
+int sddmm_launch_stream(const mcSddmmDesc& d, const SddmmParams& p, cudaStream_t s)
+{
+    const long long ntasks = (long long)d.m_vec * d.batch;
+    if (ntasks > 0x7fffffffLL) return fail(1, "mcSddmm: m_vec * batch too large");
+    auto kern = sddmm_stream_kernel<V, PA, PB, S, VM, H, 4, F>;
+    const int nx = persistent_ctas(kern, 128, (ntasks + 3) / 4);
+    kern<<<dim3((unsigned)nx), 128, 0, s>>>(p, (int)ntasks);
+    return (int)cudaGetLastError();
+}
+
 template <int V, int PA, int PB, bool S, bool VM, bool H>
 int sddmm_launch_v(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaStream_t s)
 {
+    const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
+    if (d.kernel_variant == MC_KERNEL_STREAM && d.k != 64)
+        return fail(1, "mcSddmm: the streaming kernel needs k == 64");
+    if (d.kernel_variant != MC_KERNEL_PER_ROW && d.k == 64)
+        return f16 ? sddmm_launch_stream<V, PA, PB, S, VM, H, true>(d, p, s)
+                   : sddmm_launch_stream<V, PA, PB, S, VM, H, false>(d, p, s);
     dim3 grid((unsigned)d.m_vec, (unsigned)split, (unsigned)d.batch);
-    sddmm_kernel<V, PA, PB, S, VM, H, 4><<<grid, 128, 0, s>>>(p);
+    if (f16)
+        sddmm_kernel<V, PA, PB, S, VM, H, 4, true><<<grid, 128, 0, s>>>(p);
+    else
+        sddmm_kernel<V, PA, PB, S, VM, H, 4, false><<<grid, 128, 0, s>>>(p);
     return (int)cudaGetLastError();
 }
 

@@ -40,6 +40,16 @@ __device__ __forceinline__ void mma_k32(int (&d)[4], uint32_t a0, uint32_t a1, u
     }
 }
 
+// D += A * B with A 16x16 (row), B 16x8 (col), f16 operands, f32 accumulators.
+__device__ __forceinline__ void mma_f16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                        uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
 __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel)
 {
     uint32_t r;
@@ -91,6 +101,29 @@ __device__ __forceinline__ uint32_t merge_nibble_planes(uint32_t lo16, uint32_t 
     uint32_t hi = prmt(hi16 & 0x0F0Fu, (hi16 >> 4) & 0x0F0Fu, 0x5140);
     return lo | (hi << 4);
 }
+
+// Exact int8 / uint8 -> f16 conversion of the four bytes of a word into two
+// f16x2 registers (bytes 0,1 and bytes 2,3).  A byte u placed under the f16
+// pattern 0x64 is the half 1024 + u (exact: f16 has an 11-bit significand);
+// signed bytes are first biased by 128 (xor 0x80).  Subtracting the bias is
+// exact because every intermediate is an integer below 2048.
+__device__ __forceinline__ uint32_t hsub2(uint32_t a, uint32_t b)
+{
+    uint32_t r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(b));
+    return r;
+}
+template <bool SIGNED>
+__device__ __forceinline__ void bytes_to_h2(uint32_t w, uint32_t& lo, uint32_t& hi)
+{
+    const uint32_t x = SIGNED ? (w ^ 0x80808080u) : w;
+    const uint32_t bias = SIGNED ? 0x64806480u : 0x64006400u;  // f16x2 (1152, 1152) or (1024, 1024)
+    lo = hsub2(prmt(x, 0x64646464u, 0x5140), bias);
+    hi = hsub2(prmt(x, 0x64646464u, 0x5342), bias);
+}
+
+// f32 accumulator holding an exact integer -> int32.
+__device__ __forceinline__ int f2i_exact(float f) { return __float2int_rn(f); }
 
 // Byte mask keeping the first `valid` (clamped to 0..4) bytes of a word.
 __device__ __forceinline__ uint32_t byte_mask(int valid)

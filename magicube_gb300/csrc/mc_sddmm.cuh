@@ -69,7 +69,13 @@ __device__ __forceinline__ void load_kfrag(const uint8_t* row, int kb, int t, ui
 template <int BITS>
 struct BytePlanes { static constexpr int N = BITS == 16 ? 2 : 1; };
 
-template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS>
+// F16: run the contraction on the f16 tensor path (mma.m16n8k16, f32
+// accumulators) instead of the int8 one.  Every operand byte is converted
+// exactly to f16; products are exact in f32 and the f32 partial sums are
+// integers bounded by 256 * 255^2 < 2^24 between flushes into the int32
+// accumulators (every 256 k elements), so no rounding ever happens and the
+// result is the same integer as the int8 path's.
+template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool F16>
 __global__ void __launch_bounds__(WARPS * 32)
 sddmm_kernel(const SddmmParams p)
 {
@@ -93,6 +99,17 @@ sddmm_kernel(const SddmmParams p)
     // Rows of A for k block 0 (lane g holds vector lane v = g).
     uint32_t a0[2][4] = {};
     if (g < V) load_kfrag<PREA, SIGNED>(lhs_row, 0, t, a0);
+    // ... and their f16 form for the F16 path.
+    uint32_t a0h[PA][8];
+    if constexpr (F16) {
+#pragma unroll
+        for (int lb = 0; lb < PA; ++lb)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (SIGNED && lb == PA - 1) bytes_to_h2<true>(a0[lb][q], a0h[lb][2 * q], a0h[lb][2 * q + 1]);
+                else bytes_to_h2<false>(a0[lb][q], a0h[lb][2 * q], a0h[lb][2 * q + 1]);
+            }
+    }
 
 #pragma unroll 1
     for (int ti = blockIdx.y * WARPS + warp; ti < ntiles; ti += gridDim.y * WARPS) {
@@ -100,12 +117,64 @@ sddmm_kernel(const SddmmParams p)
         const int c0 = jl0 < nnz ? __ldg(cols + jl0) : -1;
         const int c1 = jl1 < nnz ? __ldg(cols + jl1) : -1;
         int acc[PB][PA][4] = {};
+        float facc[PB][PA][4] = {};
 
 #pragma unroll 1
         for (int kb = 0; kb < kblocks; ++kb) {
             uint32_t r0[2][4] = {}, r1[2][4] = {};
             if (c0 >= 0) load_kfrag<PREB, SIGNED>(rhs + (long long)c0 * rhs_row_bytes, kb, t, r0);
             if (c1 >= 0) load_kfrag<PREB, SIGNED>(rhs + (long long)c1 * rhs_row_bytes, kb, t, r1);
+            if constexpr (F16) {
+                uint32_t ah[PA][8];
+                if (kb == 0) {
+#pragma unroll
+                    for (int lb = 0; lb < PA; ++lb)
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) ah[lb][e] = a0h[lb][e];
+                } else {
+                    uint32_t av[2][4] = {};
+                    if (g < V) load_kfrag<PREA, SIGNED>(lhs_row, kb, t, av);
+#pragma unroll
+                    for (int lb = 0; lb < PA; ++lb)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            if (SIGNED && lb == PA - 1) bytes_to_h2<true>(av[lb][q], ah[lb][2 * q], ah[lb][2 * q + 1]);
+                            else bytes_to_h2<false>(av[lb][q], ah[lb][2 * q], ah[lb][2 * q + 1]);
+                        }
+                }
+#pragma unroll
+                for (int rb = 0; rb < PB; ++rb) {
+                    uint32_t h0[8], h1[8];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        if (SIGNED && rb == PB - 1) {
+                            bytes_to_h2<true>(r0[rb][q], h0[2 * q], h0[2 * q + 1]);
+                            bytes_to_h2<true>(r1[rb][q], h1[2 * q], h1[2 * q + 1]);
+                        } else {
+                            bytes_to_h2<false>(r0[rb][q], h0[2 * q], h0[2 * q + 1]);
+                            bytes_to_h2<false>(r1[rb][q], h1[2 * q], h1[2 * q + 1]);
+                        }
+                    }
+#pragma unroll
+                    for (int lb = 0; lb < PA; ++lb)
+#pragma unroll
+                        for (int m = 0; m < 4; ++m)
+                            mma_f16(facc[rb][lb], h0[2 * m], h1[2 * m], h0[2 * m + 1], h1[2 * m + 1], ah[lb][2 * m],
+                                    ah[lb][2 * m + 1]);
+                }
+                if ((kb & 3) == 3 || kb == kblocks - 1) {
+#pragma unroll
+                    for (int rb = 0; rb < PB; ++rb)
+#pragma unroll
+                        for (int lb = 0; lb < PA; ++lb)
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                acc[rb][lb][e] = (int)((uint32_t)acc[rb][lb][e] + (uint32_t)f2i_exact(facc[rb][lb][e]));
+                                facc[rb][lb][e] = 0.f;
+                            }
+                }
+                continue;
+            }
             uint32_t av[2][4];
             if (kb == 0) {
 #pragma unroll

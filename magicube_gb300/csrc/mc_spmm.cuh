@@ -79,7 +79,11 @@ __device__ __forceinline__ int col_slot(int j)
     else return j;
 }
 
-template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT>
+// F16: contraction on the f16 tensor path (mma.m16n8k16, f32 accumulators):
+// operand bytes are converted exactly to f16 and the f32 partial sums, which
+// stay integers below 2^24, are flushed into int32 every 256 vector slots, so
+// the result is the same integer as the int8 path's.
+template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT, bool F16>
 __global__ void __launch_bounds__(WARPS * 32)
 spmm_kernel(const SpmmParams p)
 {
@@ -179,12 +183,13 @@ spmm_kernel(const SpmmParams p)
     };
 
     int acc[BP][2][4];
+    float facc[BP][2][4];
 #pragma unroll
     for (int bp = 0; bp < BP; ++bp)
 #pragma unroll
         for (int m = 0; m < 2; ++m)
 #pragma unroll
-            for (int e = 0; e < 4; ++e) acc[bp][m][e] = 0;
+            for (int e = 0; e < 4; ++e) { acc[bp][m][e] = 0; facc[bp][m][e] = 0.f; }
 
     // Pipeline prologue: column indices run one stage ahead of the copies.
     int cnext[CHUNKS_PER_THREAD];
@@ -232,7 +237,51 @@ spmm_kernel(const SpmmParams p)
                     tr[h][i] = unpack4_u16<SIGNED>(lds16(st + r * S::STRIDE + S::swz(r, c) * 16 + (byte & 15)));
                 }
             }
-            transpose4x4(tr[h]);
+            if constexpr (!F16) transpose4x4(tr[h]);
+        }
+        if constexpr (F16) {
+            // tr[h][i]: bytes of output columns ncol..ncol+3 in slot 16h+4t+i.
+            // Convert each row to f16 pairs, then transpose at half granularity:
+            // ah[h][c][0] = slots (16h+4t, +1), ah[h][c][1] = slots (+2, +3) of column ncol+c.
+            uint32_t ah[2][4][2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                uint32_t P[4], Q[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) bytes_to_h2<SIGNED>(tr[h][i], P[i], Q[i]);
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    ah[h][0][q] = prmt(P[2 * q], P[2 * q + 1], 0x5410);
+                    ah[h][1][q] = prmt(P[2 * q], P[2 * q + 1], 0x7632);
+                    ah[h][2][q] = prmt(Q[2 * q], Q[2 * q + 1], 0x5410);
+                    ah[h][3][q] = prmt(Q[2 * q], Q[2 * q + 1], 0x7632);
+                }
+            }
+#pragma unroll
+            for (int bp = 0; bp < BP; ++bp) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    uint32_t vlo, vhi;
+                    if (SIGNED && bp == BP - 1) bytes_to_h2<true>(vcur[bp][h], vlo, vhi);
+                    else bytes_to_h2<false>(vcur[bp][h], vlo, vhi);
+                    mma_f16(facc[bp][0], ah[h][0][0], ah[h][1][0], ah[h][0][1], ah[h][1][1], vlo, vhi);
+                    mma_f16(facc[bp][1], ah[h][2][0], ah[h][3][0], ah[h][2][1], ah[h][3][1], vlo, vhi);
+                }
+            }
+            if ((s & 7) == 7 || s == steps - 1) {
+#pragma unroll
+                for (int bp = 0; bp < BP; ++bp)
+#pragma unroll
+                    for (int m = 0; m < 2; ++m)
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            acc[bp][m][e] = (int)((uint32_t)acc[bp][m][e] + (uint32_t)f2i_exact(facc[bp][m][e]));
+                            facc[bp][m][e] = 0.f;
+                        }
+            }
+#pragma unroll
+            for (int bp = 0; bp < BP; ++bp) { vcur[bp][0] = vnext[bp][0]; vcur[bp][1] = vnext[bp][1]; }
+            continue;
         }
         // tr[h][c]: slots 16h+4t..+3 of output column ncol + c.
 #pragma unroll

@@ -68,7 +68,7 @@ class DeviceSddmmMask:
 
 def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, out: torch.Tensor | None = None,
          out_half: bool = False, scale: float = 1.0, batch: int = 1, values_stride: int = 0,
-         rhs_stride: int | None = None, out_stride: int | None = None,
+         rhs_stride: int | None = None, out_stride: int | None = None, mma_kind: int = 0, variant: int = 0,
          stream: torch.cuda.Stream | None = None) -> torch.Tensor:
     """C = A * B for a batch of `batch` entries (shared mask).
 
@@ -88,7 +88,8 @@ def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, 
         is_signed=int(signed), out_half=int(out_half), scale=scale, batch=batch,
         row_indices=lhs.row_indices.data_ptr(), row_offsets=lhs.row_offsets.data_ptr(),
         column_indices=lhs.col_indices.data_ptr(), values=lhs.values.data_ptr(), values_stride=values_stride,
-        rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride)
+        rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride, mma_kind=mma_kind,
+        kernel_variant=variant)
     _lib.check(_lib.lib().mcSpmm(ctypes.byref(d), _stream_handle(stream)), "mcSpmm")
     return out
 
@@ -96,7 +97,7 @@ def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, 
 def sddmm(mask: DeviceSddmmMask, lhs: torch.Tensor, rhs: torch.Tensor, k: int, lhs_bits: int, rhs_bits: int, *,
           signed: bool = True, vecmajor: bool = False, out: torch.Tensor | None = None, out_half: bool = False,
           scale: float = 1.0, batch: int = 1, lhs_stride: int | None = None, rhs_stride: int | None = None,
-          out_stride: int | None = None, row_split: int = 0,
+          out_stride: int | None = None, row_split: int = 0, mma_kind: int = 0, variant: int = 0,
           stream: torch.cuda.Stream | None = None) -> torch.Tensor:
     """out = (A * B^T) on the mask's stored nonzero vectors.
 
@@ -119,6 +120,7 @@ def sddmm(mask: DeviceSddmmMask, lhs: torch.Tensor, rhs: torch.Tensor, k: int, l
         is_signed=int(signed), out_half=int(out_half), out_vecmajor=int(vecmajor), scale=scale, batch=batch,
         row_split=row_split, row_indices=mask.row_indices.data_ptr(), row_offsets=mask.row_offsets.data_ptr(),
         column_indices=mask.col_indices.data_ptr(), lhs=lhs.data_ptr(), lhs_stride=lhs_stride,
-        rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride)
+        rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride, mma_kind=mma_kind,
+        kernel_variant=variant)
     _lib.check(_lib.lib().mcSddmm(ctypes.byref(d), _stream_handle(stream)), "mcSddmm")
     return out

@@ -24,18 +24,68 @@ def _case(pa, pb, V, K, N, lengths, seed):
 @pytest.mark.parametrize("signed", [False, True])
 @pytest.mark.parametrize("K", [64, 192])
 @pytest.mark.parametrize("vecmajor", [False, True])
-def test_sddmm_ragged(cuda, pa, pb, V, signed, K, vecmajor):
+@pytest.mark.parametrize("mma", [_lib.MMA_INT8, _lib.MMA_F16])
+@pytest.mark.parametrize("variant", [_lib.KERNEL_PER_ROW, _lib.KERNEL_AUTO])
+def test_sddmm_ragged(cuda, pa, pb, V, signed, K, vecmajor, mma, variant):
     N = 256
     mask, lhs, rhs = _case(pa, pb, V, K, N, RAGGED, seed=pa + pb + V + K)
     align = 16 if vecmajor else 8
     hm = formats.prepare_sddmm(mask, alignment=align)
     dm = ops.DeviceSddmmMask.from_host(hm, cuda)
     out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, pa, pb,
-                    signed=signed, vecmajor=vecmajor)
+                    signed=signed, vecmajor=vecmajor, mma_kind=mma, variant=variant)
     ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, pa, pb,
                             oracle.SIGNED if signed else oracle.UNSIGNED, alignment=8,
                             layout=oracle.OUT_VECMAJOR if vecmajor else oracle.OUT_BLOCKED)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", PAIRS)
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("fill", [0x00, 0xFF, 0x80, 0x7F, "alt"])
+@pytest.mark.parametrize("mma", [_lib.MMA_INT8, _lib.MMA_F16])
+def test_sddmm_extreme_values_large_k(cuda, pa, pb, signed, fill, mma):
+    """Extreme lane values with K = 1024 (four f32 flush intervals on the f16 path)."""
+    V, K, N = 8, 1024, 128
+    mask = synth.lengths_mask([128, 3, 17, 0, 64, 8, 100, 1], N, V, seed=19)
+    nl, nr = mask.rows * K * pa // 8, N * K * pb // 8
+    if fill == "alt":
+        lhs = np.tile(np.array([0x80, 0x7F], np.uint8), nl // 2 + 1)[:nl]
+        rhs = np.tile(np.array([0x7F, 0x80, 0xFF, 0x00], np.uint8), nr // 4 + 1)[:nr]
+    else:
+        lhs, rhs = np.full(nl, fill, np.uint8), np.full(nr, fill, np.uint8)
+    hm = formats.prepare_sddmm(mask)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, pa, pb, signed=signed,
+                    mma_kind=mma)
+    ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, pa, pb,
+                            oracle.SIGNED if signed else oracle.UNSIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", PAIRS)
+@pytest.mark.parametrize("V", [2, 8])
+@pytest.mark.parametrize("mma", [_lib.MMA_INT8, _lib.MMA_F16])
+@pytest.mark.parametrize("vecmajor", [False, True])
+def test_sddmm_streaming_many_tasks(cuda, pa, pb, V, mma, vecmajor):
+    """Far more tasks than resident warps: each warp streams many rows."""
+    K, N, B = 64, 1024, 4
+    lengths = np.random.default_rng(pa + pb + V).integers(0, 60, size=1024)
+    lengths[::29] = 0
+    lengths[3] = 1024
+    mask = synth.lengths_mask(lengths, N, V, seed=29)
+    hm = formats.prepare_sddmm(mask, alignment=16 if vecmajor else 8)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    lhs_all = [synth.random_bytes(mask.rows * K * pa // 8, 70 + b) for b in range(B)]
+    rhs_all = [synth.random_bytes(N * K * pb // 8, 80 + b) for b in range(B)]
+    out = ops.sddmm(dm, torch.from_numpy(np.concatenate(lhs_all)).to(cuda),
+                    torch.from_numpy(np.concatenate(rhs_all)).to(cuda), K, pa, pb, signed=True, batch=B,
+                    vecmajor=vecmajor, mma_kind=mma, variant=_lib.KERNEL_STREAM)
+    for b in range(B):
+        ref = oracle.sddmm_host(lhs_all[b], rhs_all[b], hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N,
+                                pa, pb, oracle.SIGNED,
+                                layout=oracle.OUT_VECMAJOR if vecmajor else oracle.OUT_BLOCKED)
+        np.testing.assert_array_equal(out[b].cpu().numpy(), ref)
 
 
 @pytest.mark.parametrize("pa,pb", PAIRS)

@@ -25,12 +25,62 @@ def _case(pa, pb, V, K, N, lengths, seed):
 @pytest.mark.parametrize("V", [2, 4, 8])
 @pytest.mark.parametrize("signed", [False, True])
 @pytest.mark.parametrize("N", [64, 256])
-def test_spmm_ragged(cuda, pa, pb, V, signed, N):
+@pytest.mark.parametrize("mma", [_lib.MMA_INT8, _lib.MMA_F16])
+@pytest.mark.parametrize("variant", [_lib.KERNEL_PER_ROW, _lib.KERNEL_STREAM])
+def test_spmm_ragged(cuda, pa, pb, V, signed, N, mma, variant):
     K = 256
     mask, vals, rhs = _case(pa, pb, V, K, N, RAGGED, seed=pa * 100 + pb * 10 + V)
     h = formats.prepare_spmm(mask, vals, pa, pb)
     d = ops.DeviceSpmmLhs.from_host(h, cuda)
-    out = ops.spmm(d, torch.from_numpy(rhs).to(cuda), N, signed=signed)
+    out = ops.spmm(d, torch.from_numpy(rhs).to(cuda), N, signed=signed, mma_kind=mma, variant=variant)
+    ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
+                           oracle.SIGNED if signed else oracle.UNSIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", PAIRS)
+@pytest.mark.parametrize("V", [2, 8])
+@pytest.mark.parametrize("mma", [_lib.MMA_INT8, _lib.MMA_F16])
+def test_spmm_streaming_many_tasks(cuda, pa, pb, V, mma):
+    """Far more (batch entry, vector-row) tasks than resident CTAs: every CTA
+    streams many rows, including empty and long ones, through its pipeline."""
+    K, N, B = 512, 128, 4
+    lengths = np.random.default_rng(pa * 10 + pb + V).integers(0, 70, size=1024)
+    lengths[::37] = 0
+    lengths[5] = 512
+    mask = synth.lengths_mask(lengths, K, V, seed=23)
+    vals_all = [synth.random_bytes(mask.nnz_vec * V * pa // 8, 50 + b) for b in range(B)]
+    rhs_all = [synth.random_bytes(K * N * pb // 8, 60 + b) for b in range(B)]
+    packed = [formats.prepare_spmm(mask, v, pa, pb) for v in vals_all]
+    d = ops.DeviceSpmmLhs.from_host(packed[0], cuda)
+    d.values = torch.from_numpy(np.concatenate([p.values for p in packed])).to(cuda)
+    out = ops.spmm(d, torch.from_numpy(np.concatenate(rhs_all)).to(cuda), N, signed=True, batch=B,
+                   values_stride=packed[0].values.size, mma_kind=mma, variant=_lib.KERNEL_STREAM)
+    for b in range(B):
+        ref = oracle.spmm_host(vals_all[b], rhs_all[b], mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N,
+                               pa, pb, oracle.SIGNED)
+        np.testing.assert_array_equal(out[b].cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", PAIRS)
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("fill", [0x00, 0xFF, 0x80, 0x7F, "alt"])
+@pytest.mark.parametrize("mma", [_lib.MMA_INT8, _lib.MMA_F16])
+def test_spmm_extreme_values_long_rows(cuda, pa, pb, signed, fill, mma):
+    """All lanes at an extreme of their range, rows up to 2048 nonzeros: the
+    largest partial sums either tensor path can see (f16 path: f32 partial
+    sums near 2^24 before each flush into int32)."""
+    V, K, N = 8, 2048, 64
+    mask = synth.lengths_mask([2048, 1000, 257, 256, 255, 0, 31, 1], K, V, seed=17)
+    nv, nr = mask.nnz_vec * V * pa // 8, K * N * pb // 8
+    if fill == "alt":
+        vals = np.tile(np.array([0x80, 0x7F], np.uint8), nv // 2 + 1)[:nv]
+        rhs = np.tile(np.array([0x7F, 0x80, 0xFF, 0x00], np.uint8), nr // 4 + 1)[:nr]
+    else:
+        vals, rhs = np.full(nv, fill, np.uint8), np.full(nr, fill, np.uint8)
+    h = formats.prepare_spmm(mask, vals, pa, pb)
+    d = ops.DeviceSpmmLhs.from_host(h, cuda)
+    out = ops.spmm(d, torch.from_numpy(rhs).to(cuda), N, signed=signed, mma_kind=mma)
     ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
                            oracle.SIGNED if signed else oracle.UNSIGNED)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)

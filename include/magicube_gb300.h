@@ -81,10 +81,11 @@ int mcSetDefaultMmaKind(int kind);
 /* ---- Kernel variant ---------------------------------------------------------
  * MC_KERNEL_PER_ROW: one CTA per (vector-row, column tile / row split, batch
  *                    entry); any k.
- * MC_KERNEL_STREAM:  persistent CTAs (SpMM) or warps (SDDMM) that stream many
- *                    vector-rows through one software pipeline; SpMM needs
- *                    16-byte aligned values, SDDMM needs k == 64.
- * MC_KERNEL_AUTO:    the streaming kernel where it applies, else per-row. */
+ * MC_KERNEL_STREAM:  the pipelined kernels: SpMM -- persistent CTAs that
+ *                    stream many vector-rows through one cp.async ring (needs
+ *                    16-byte aligned values); SDDMM -- the k == 64 kernel with
+ *                    two tiles in flight per warp (needs k == 64).
+ * MC_KERNEL_AUTO:    the pipelined kernel where it applies, else per-row. */
 enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2 };
 
 /* ---- Extended entry points: batch, stream, signedness, dequantised output --

@@ -102,13 +102,10 @@ int spmm_launch(const mcSpmmDesc& d, cudaStream_t s)
 }
 
 template <int V, int PA, int PB, bool S, bool VM, bool H, bool F>
-int sddmm_launch_stream(const mcSddmmDesc& d, const SddmmParams& p, cudaStream_t s)
+int sddmm_launch_k64(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaStream_t s)
 {
-    const long long ntasks = (long long)d.m_vec * d.batch;
-    if (ntasks > 0x7fffffffLL) return fail(1, "mcSddmm: m_vec * batch too large");
-    auto kern = sddmm_stream_kernel<V, PA, PB, S, VM, H, 4, F>;
-    const int nx = persistent_ctas(kern, 128, (ntasks + 3) / 4);
-    kern<<<dim3((unsigned)nx), 128, 0, s>>>(p, (int)ntasks);
+    dim3 grid((unsigned)d.m_vec, (unsigned)split, (unsigned)d.batch);
+    sddmm_k64_kernel<V, PA, PB, S, VM, H, 4, F><<<grid, 128, 0, s>>>(p);
     return (int)cudaGetLastError();
 }
 
@@ -119,8 +116,8 @@ int sddmm_launch_v(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaSt
     if (d.kernel_variant == MC_KERNEL_STREAM && d.k != 64)
         return fail(1, "mcSddmm: the streaming kernel needs k == 64");
     if (d.kernel_variant != MC_KERNEL_PER_ROW && d.k == 64)
-        return f16 ? sddmm_launch_stream<V, PA, PB, S, VM, H, true>(d, p, s)
-                   : sddmm_launch_stream<V, PA, PB, S, VM, H, false>(d, p, s);
+        return f16 ? sddmm_launch_k64<V, PA, PB, S, VM, H, true>(d, p, split, s)
+                   : sddmm_launch_k64<V, PA, PB, S, VM, H, false>(d, p, split, s);
     dim3 grid((unsigned)d.m_vec, (unsigned)split, (unsigned)d.batch);
     if (f16)
         sddmm_kernel<V, PA, PB, S, VM, H, 4, true><<<grid, 128, 0, s>>>(p);

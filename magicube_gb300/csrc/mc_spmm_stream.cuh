@@ -193,9 +193,10 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
             if (g < V) {
                 const uint8_t* vs = st + RHS_BYTES;
 #pragma unroll
+                const bool full = step * 32 + 32 <= nnz;  // no slot of this step past the row end
+#pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int valid = nnz - (step * 32 + 16 * h + 4 * t);
-                    const uint32_t keep = byte_mask(valid);
+                    const uint32_t keep = full ? 0xffffffffu : byte_mask(nnz - (step * 32 + 16 * h + 4 * t));
                     if constexpr (L::MMA_K == 16) {
 #pragma unroll
                         for (int bp = 0; bp < BP; ++bp)

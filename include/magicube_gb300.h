@@ -88,6 +88,19 @@ int mcSetDefaultMmaKind(int kind);
  * MC_KERNEL_AUTO:    the pipelined kernel where it applies, else per-row. */
 enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2 };
 
+/* ---- Value layouts of the SpMM sparse operand --------------------------------
+ * MC_VALUES_PACKED:  the reference host packer's layout (what
+ *                    mcPackSpmmValues writes; column indices 8-shuffled when
+ *                    either operand is 4-bit).
+ * MC_VALUES_SOFTMAX: the layout the quantized softmax writes (mcQuantSoftmax;
+ *                    the reference extension's q_softmax): chunks of 16 slots
+ *                    [v][16] for 8-bit values, 32-slot nibble chunks for
+ *                    4-bit, [v][low 16 bytes][high 16 bytes] for 16-bit;
+ *                    column indices unshuffled.
+ * int32 output is provided with MC_VALUES_PACKED, half output with
+ * MC_VALUES_SOFTMAX (the combinations the reference uses). */
+enum { MC_VALUES_PACKED = 0, MC_VALUES_SOFTMAX = 1 };
+
 /* ---- Extended entry points: batch, stream, signedness, dequantised output --
  * These generalise the reference's batched extension kernels
  * (batched_wmmaSpmm_* in sparse_transformer_magicube/src/cuda/deq_spmm_kernel.cu,
@@ -111,6 +124,7 @@ typedef struct mcSpmmDesc {
     void* out;            long long out_stride;     /* elements */
     int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
     int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM */
+    int value_layout;           /* MC_VALUES_PACKED / MC_VALUES_SOFTMAX */
 } mcSpmmDesc;
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream);
 
@@ -134,6 +148,29 @@ typedef struct mcSddmmDesc {
 } mcSddmmDesc;
 int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream);
 
+/* ---- Quantized attention steps ----------------------------------------------
+ * mcQuantize: out = packed trunc(clamp(float(in) * scale)) for `count` half
+ * inputs (count % 8 == 0), 8 bits ([-128, 127]) or 4 bits ([-8, 7]) per lane,
+ * little-endian -- sparse_transformer_magicube/src/cuda/quantization_kernel.cu:14-131. */
+int mcQuantize(const void* in, void* out, long long count, int bits, float scale, cudaStream_t stream);
+
+/* mcQuantSoftmax: row softmax of SDDMM scores over each vector-row's stored
+ * nonzeros, per vector lane: p = exp(score * scaling - max) / sum,
+ * q = trunc(clamp(p * scale)) in `bits` (4, 8, 16) bits, written in the
+ * MC_VALUES_SOFTMAX layout at the aligned slots [start, end) of each row
+ * (padding slots are not written) -- q_softmax_kernel.cu:181-271.  scores are
+ * half, vector-major (j*V + v), as mcSddmm writes with out_half. */
+typedef struct mcSoftmaxDesc {
+    int m_vec, vec_length, batch, bits;
+    float scaling;              /* applied to each score (1/sqrt(head_dim)) */
+    float scale;                /* quantization scale of the probabilities */
+    const int* row_indices;
+    const int* row_offsets;
+    const void* scores;   long long scores_stride;  /* halves between batch entries */
+    void* out;            long long out_stride;     /* bytes between batch entries */
+} mcSoftmaxDesc;
+int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
+
 /* ---- Host-side format conversion (host pointers) ---------------------------
  * The reference's host packer (SpMM/SpMM/spmm_benchmark.cpp:177-377,
  * SDDMM/SDDMM/sddmm_benchmark.cpp:104-127) as library routines. */
@@ -152,6 +189,10 @@ int mcPadColumnIndices(int m_vec, const int* row_offsets, const int* col_indices
  * out holds aligned_nnz*V*lhs_bits/8 bytes. */
 int mcPackSpmmValues(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
                      const int* aligned_pairs, int aligned_nnz, const void* values, void* out);
+/* Same, for either value layout (MC_VALUES_PACKED or MC_VALUES_SOFTMAX). */
+int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
+                       const int* aligned_pairs, int aligned_nnz, const void* values, void* out,
+                       int value_layout);
 /* Vector-row processing order: longest first (bm_test_utils.h:222-237), or identity. */
 int mcSortedRowSwizzle(int m_vec, const int* row_offsets, int* row_indices);
 int mcIdentityRowSwizzle(int m_vec, int* row_indices);

@@ -24,7 +24,7 @@ class McSpmmDesc(ctypes.Structure):
         ("values", _c_vp), ("values_stride", _c_ll),
         ("rhs", _c_vp), ("rhs_stride", _c_ll),
         ("out", _c_vp), ("out_stride", _c_ll),
-        ("mma_kind", _c_int), ("kernel_variant", _c_int),
+        ("mma_kind", _c_int), ("kernel_variant", _c_int), ("value_layout", _c_int),
     ]
 
 
@@ -41,8 +41,19 @@ class McSddmmDesc(ctypes.Structure):
     ]
 
 
+class McSoftmaxDesc(ctypes.Structure):
+    _fields_ = [
+        ("m_vec", _c_int), ("vec_length", _c_int), ("batch", _c_int), ("bits", _c_int),
+        ("scaling", _c_float), ("scale", _c_float),
+        ("row_indices", _c_vp), ("row_offsets", _c_vp),
+        ("scores", _c_vp), ("scores_stride", _c_ll),
+        ("out", _c_vp), ("out_stride", _c_ll),
+    ]
+
+
 MMA_DEFAULT, MMA_INT8, MMA_F16 = 0, 1, 2
 KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM = 0, 1, 2
+VALUES_PACKED, VALUES_SOFTMAX = 0, 1
 
 # name -> (restype, argtypes)
 _IP = ctypes.POINTER(ctypes.c_int)
@@ -52,9 +63,12 @@ _SIGNATURES = {
     "mcSetDefaultMmaKind": (_c_int, [_c_int]),
     "mcSpmm": (_c_int, [ctypes.POINTER(McSpmmDesc), _c_vp]),
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
+    "mcQuantize": (_c_int, [_c_vp, _c_vp, _c_ll, _c_int, _c_float, _c_vp]),
+    "mcQuantSoftmax": (_c_int, [ctypes.POINTER(McSoftmaxDesc), _c_vp]),
     "mcAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp]),
     "mcPadColumnIndices": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_vp]),
     "mcPackSpmmValues": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_int, _c_vp, _c_vp]),
+    "mcPackSpmmValuesEx": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_int]),
     "mcSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp]),
     "mcIdentityRowSwizzle": (_c_int, [_c_int, _c_vp]),
 }

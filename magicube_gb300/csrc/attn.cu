@@ -1,0 +1,224 @@
+// attn.cu -- the element-wise steps around the integer SDDMM / SpMM of the
+// quantized sparse attention: symmetric quantization of half activations and
+// the quantized row softmax.
+//
+//  * mcQuantize: q = trunc(clamp(float(x) * scale, lo, hi)), packed
+//    little-endian, 8 or 4 bits per lane -- the reference's
+//    quantizationKernel_{8b,4b} (sparse_transformer_magicube/src/cuda/
+//    quantization_kernel.cu:14-131), for any element count divisible by 8.
+//  * mcQuantSoftmax: per vector-row and vector lane, over the row's stored
+//    nonzeros, p = exp(x * scaling - max) / sum, q = trunc(clamp(p * scale)),
+//    written in the value layout the SpMM reads (MC_VALUES_SOFTMAX) -- the
+//    reference's csrSoftmaxKernel_ (q_softmax_kernel.cu:181-271).  One warp per
+//    vector-row; three passes over the row (max, sum, write) read the scores
+//    from L1/L2.  The maximum starts from -inf for every lane (the reference
+//    starts lanes 1..V-1 from 0, which only shifts the exponent's argument).
+#include <cfloat>
+#include <cstdint>
+
+#include "mc_host.h"
+#include "mc_ptx.cuh"
+
+namespace mc {
+
+template <int BITS>
+__global__ void __launch_bounds__(256) quantize_kernel(const __half* __restrict__ in, uint8_t* __restrict__ out,
+                                                        long long groups, float scale)
+{
+    constexpr float LO = BITS == 8 ? -128.f : -8.f, HI = BITS == 8 ? 127.f : 7.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < groups;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int4 raw = ldg_nc_v4(in + 8 * i);
+        const __half* h = reinterpret_cast<const __half*>(&raw);
+        uint32_t q[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            float f = __half2float(h[e]) * scale;
+            f = fminf(fmaxf(f, LO), HI);
+            q[e] = (uint32_t)(int)f;  // truncation toward zero, as a C cast
+        }
+        if constexpr (BITS == 8) {
+            uint32_t w0 = (q[0] & 0xff) | (q[1] & 0xff) << 8 | (q[2] & 0xff) << 16 | (q[3] & 0xff) << 24;
+            uint32_t w1 = (q[4] & 0xff) | (q[5] & 0xff) << 8 | (q[6] & 0xff) << 16 | (q[7] & 0xff) << 24;
+            *reinterpret_cast<uint2*>(out + 8 * i) = make_uint2(w0, w1);
+        } else {
+            uint32_t w = 0;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) w |= (q[e] & 0xf) << (4 * e);
+            *reinterpret_cast<uint32_t*>(out + 4 * i) = w;
+        }
+    }
+}
+
+struct SoftmaxParams {
+    int m_vec, batch;
+    const int* row_indices;
+    const int* row_offsets;
+    const __half* scores;     // per batch entry: aligned_nnz * V halves, vector-major
+    long long scores_stride;  // halves
+    uint8_t* out;             // per batch entry: aligned_nnz * V * BITS / 8 bytes
+    long long out_stride;     // bytes
+    float scaling, scale;
+};
+
+template <int V>
+__device__ __forceinline__ void load_vec(const __half* p, float (&x)[V], float s)
+{
+    if constexpr (V == 8) {
+        int4 r = *reinterpret_cast<const int4*>(p);
+        const __half* h = reinterpret_cast<const __half*>(&r);
+#pragma unroll
+        for (int v = 0; v < 8; ++v) x[v] = __half2float(h[v]) * s;
+    } else if constexpr (V == 4) {
+        int2 r = *reinterpret_cast<const int2*>(p);
+        const __half* h = reinterpret_cast<const __half*>(&r);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) x[v] = __half2float(h[v]) * s;
+    } else {
+        int r = *reinterpret_cast<const int*>(p);
+        const __half* h = reinterpret_cast<const __half*>(&r);
+        x[0] = __half2float(h[0]) * s;
+        x[1] = __half2float(h[1]) * s;
+    }
+}
+
+template <int V, int BITS>
+__global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams p)
+{
+    constexpr float LO = BITS == 16 ? -32768.f : (BITS == 8 ? -128.f : -8.f);
+    constexpr float HI = BITS == 16 ? 32767.f : (BITS == 8 ? 127.f : 7.f);
+    const int lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (r >= p.m_vec) return;
+    const int b = blockIdx.y;
+    const int row = __ldg(p.row_indices + r);
+    const int start = __ldg(p.row_offsets + 2 * row);
+    const int nnz = __ldg(p.row_offsets + 2 * row + 1) - start;
+    const __half* sc = p.scores + (long long)b * p.scores_stride + (long long)start * V;
+    uint8_t* out = p.out + (long long)b * p.out_stride + (long long)start * V * BITS / 8;
+
+    float mx[V], sum[V], x[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) { mx[v] = -FLT_MAX; sum[v] = 0.f; }
+    for (int j = lane; j < nnz; j += 32) {
+        load_vec<V>(sc + (long long)j * V, x, p.scaling);
+#pragma unroll
+        for (int v = 0; v < V; ++v) mx[v] = fmaxf(mx[v], x[v]);
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx[v] = fmaxf(mx[v], __shfl_xor_sync(0xffffffffu, mx[v], o));
+    for (int j = lane; j < nnz; j += 32) {
+        load_vec<V>(sc + (long long)j * V, x, p.scaling);
+#pragma unroll
+        for (int v = 0; v < V; ++v) sum[v] += __expf(x[v] - mx[v]);
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
+
+    // Every lane of the warp runs the same number of iterations (the loop
+    // bound is rounded up to the warp) so the 4-bit pairing shuffle is safe.
+    const int nround = (nnz + 31) & ~31;
+    for (int j = lane; j < nround; j += 32) {
+        int q[V];
+        const bool in = j < nnz;
+        if (in) {
+            load_vec<V>(sc + (long long)j * V, x, p.scaling);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                float f = __expf(x[v] - mx[v]) / sum[v] * p.scale;
+                f = fminf(fmaxf(f, LO), HI);
+                q[v] = (int)f;
+            }
+        } else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) q[v] = 0;
+        }
+        if constexpr (BITS == 8) {
+            if (in) {
+                uint8_t* o = out + (j >> 4) * V * 16 + (j & 15);
+#pragma unroll
+                for (int v = 0; v < V; ++v) o[v * 16] = (uint8_t)q[v];
+            }
+        } else if constexpr (BITS == 16) {
+            if (in) {
+                uint8_t* o = out + (j >> 4) * V * 32 + (j & 15);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    o[v * 32] = (uint8_t)(q[v] & 0xff);
+                    o[v * 32 + 16] = (uint8_t)((q[v] >> 8) & 0xff);
+                }
+            }
+        } else {
+            // nonzeros j (even lane) and j+1 (odd lane) share a byte: low, high nibble
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const int hi = __shfl_down_sync(0xffffffffu, q[v], 1);
+                if (in && !(j & 1)) {
+                    uint8_t* o = out + (j >> 5) * V * 16 + v * 16 + ((j & 31) >> 1);
+                    const int hv = (j + 1 < nnz) ? hi : 0;
+                    *o = (uint8_t)((q[v] & 0xf) | ((hv & 0xf) << 4));
+                }
+            }
+        }
+    }
+}
+
+}  // namespace mc
+
+extern "C" int mcQuantize(const void* in, void* out, long long count, int bits, float scale, cudaStream_t stream)
+{
+    mc::clear_error();
+    if (bits != 8 && bits != 4) return mc::fail(1, "mcQuantize: bits must be 4 or 8");
+    if (count < 0 || count % 8) return mc::fail(1, "mcQuantize: count must be a non-negative multiple of 8");
+    if (count == 0) return 0;
+    if (!in || !out || reinterpret_cast<uintptr_t>(in) % 16 || reinterpret_cast<uintptr_t>(out) % 8)
+        return mc::fail(1, "mcQuantize: input must be 16-byte and output 8-byte aligned");
+    const long long groups = count / 8;
+    long long blocks = (groups + 255) / 256;
+    if (blocks > 152LL * 32) blocks = 152LL * 32;
+    if (bits == 8)
+        mc::quantize_kernel<8><<<(unsigned)blocks, 256, 0, stream>>>(static_cast<const __half*>(in),
+                                                                      static_cast<uint8_t*>(out), groups, scale);
+    else
+        mc::quantize_kernel<4><<<(unsigned)blocks, 256, 0, stream>>>(static_cast<const __half*>(in),
+                                                                      static_cast<uint8_t*>(out), groups, scale);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mcQuantSoftmax(const mcSoftmaxDesc* d, cudaStream_t stream)
+{
+    mc::clear_error();
+    if (!d) return mc::fail(1, "mcQuantSoftmax: null descriptor");
+    if (!(d->vec_length == 2 || d->vec_length == 4 || d->vec_length == 8))
+        return mc::fail(1, "mcQuantSoftmax: vec_length must be 2, 4 or 8");
+    if (!(d->bits == 4 || d->bits == 8 || d->bits == 16)) return mc::fail(1, "mcQuantSoftmax: bits must be 4, 8 or 16");
+    if (d->m_vec < 0 || d->batch < 1 || d->batch > 65535) return mc::fail(1, "mcQuantSoftmax: bad m_vec or batch");
+    if (d->m_vec == 0) return 0;
+    if (!d->row_indices || !d->row_offsets || !d->scores || !d->out) return mc::fail(1, "mcQuantSoftmax: null pointer");
+    if (reinterpret_cast<uintptr_t>(d->scores) % 16 || d->scores_stride % 8)
+        return mc::fail(1, "mcQuantSoftmax: scores must be 16-byte aligned, stride a multiple of 8 halves");
+    mc::SoftmaxParams p;
+    p.m_vec = d->m_vec; p.batch = d->batch;
+    p.row_indices = d->row_indices; p.row_offsets = d->row_offsets;
+    p.scores = static_cast<const __half*>(d->scores); p.scores_stride = d->scores_stride;
+    p.out = static_cast<uint8_t*>(d->out); p.out_stride = d->out_stride;
+    p.scaling = d->scaling; p.scale = d->scale;
+    dim3 grid((unsigned)((d->m_vec + 3) / 4), (unsigned)d->batch);
+#define MC_SM(V, B) mc::quant_softmax_kernel<V, B><<<grid, 128, 0, stream>>>(p)
+#define MC_SMV(B)                                           \
+    switch (d->vec_length) {                                \
+        case 2: MC_SM(2, B); break;                         \
+        case 4: MC_SM(4, B); break;                         \
+        default: MC_SM(8, B); break;                        \
+    }
+    if (d->bits == 4) { MC_SMV(4) }
+    else if (d->bits == 8) { MC_SMV(8) }
+    else { MC_SMV(16) }
+#undef MC_SMV
+#undef MC_SM
+    return (int)cudaGetLastError();
+}

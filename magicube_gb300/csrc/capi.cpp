@@ -39,6 +39,9 @@ static int check_spmm(const mcSpmmDesc& d)
     if (d.n / 64 > 65535) return fail(1, "mcSpmm: n too large");
     if (d.batch < 1 || d.batch > 65535) return fail(1, "mcSpmm: batch must be in [1, 65535]");
     if (d.out_half && !d.is_signed) return fail(1, "mcSpmm: half output requires is_signed = 1");
+    if (d.value_layout != (d.out_half ? MC_VALUES_SOFTMAX : MC_VALUES_PACKED))
+        return fail(1, "mcSpmm: half output is built for the softmax value layout and int32 output for the "
+                       "packer layout");
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSpmm: half output requires a nonzero scale");
     if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16) return fail(1, "mcSpmm: invalid mma_kind");
     if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_STREAM)

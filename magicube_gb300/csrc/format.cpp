@@ -88,32 +88,46 @@ extern "C" int mcPadColumnIndices(int m_vec, const int* row_offsets, const int* 
 extern "C" int mcPackSpmmValues(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
                                 const int* aligned_pairs, int aligned_nnz, const void* values, void* out)
 {
+    return mcPackSpmmValuesEx(m_vec, vec_length, lhs_bits, rhs_bits, row_offsets, aligned_pairs, aligned_nnz,
+                              values, out, MC_VALUES_PACKED);
+}
+
+extern "C" int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
+                                  const int* aligned_pairs, int aligned_nnz, const void* values, void* out,
+                                  int value_layout)
+{
     const int V = vec_length;
     if (m_vec < 0 || !(V == 2 || V == 4 || V == 8) || !valid_pair(lhs_bits, rhs_bits) || !row_offsets ||
-        !aligned_pairs || !out || aligned_nnz < 0)
+        !aligned_pairs || !out || aligned_nnz < 0 ||
+        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX))
         return mc::fail(1, "mcPackSpmmValues: invalid arguments");
     const int mma_k = (lhs_bits == 4 || rhs_bits == 4) ? 32 : 16;
     if (aligned_nnz % mma_k) return mc::fail(1, "mcPackSpmmValues: aligned_nnz not a multiple of the chunk size");
-    const int plane_bits = mma_k == 32 ? 4 : 8;
+    // Chunk of `chunk` slots holding `planes` planes of `plane_bits`; element
+    // (v, jj) of plane pl sits at element index pl*plane_elems + v*vstride + jj.
+    const bool softmax = value_layout == MC_VALUES_SOFTMAX;
+    const int chunk = softmax ? (lhs_bits == 4 ? 32 : 16) : mma_k;
+    const int plane_bits = chunk == 32 ? 4 : 8;
     const int planes = lhs_bits / plane_bits;
-    const long long plane_bytes = (long long)V * mma_k * plane_bits / 8;
-    const long long chunk_bytes = plane_bytes * planes;
+    const bool interleaved = softmax && lhs_bits == 16;  // [v][plane][16]
+    const long long chunk_bytes = (long long)V * chunk * lhs_bits / 8;
+    const long long plane_elems = interleaved ? chunk : (long long)V * chunk;
+    const long long vstride = interleaved ? (long long)planes * chunk : chunk;
     const uint8_t* src = static_cast<const uint8_t*>(values);
     uint8_t* dst = static_cast<uint8_t*>(out);
-    std::memset(dst, 0, (size_t)(aligned_nnz / mma_k) * (size_t)chunk_bytes);
+    std::memset(dst, 0, (size_t)(aligned_nnz / chunk) * (size_t)chunk_bytes);
     const uint32_t pmask = (1u << plane_bits) - 1u;
     for (int i = 0; i < m_vec; ++i) {
         const int b = row_offsets[i], e = row_offsets[i + 1];
         for (int j = b; j < e; ++j) {
             const long long slot = (long long)aligned_pairs[2 * i] + (j - b);
             if (slot >= aligned_nnz) return mc::fail(1, "mcPackSpmmValues: aligned_nnz too small");
-            uint8_t* chunk = dst + (slot / mma_k) * chunk_bytes;
-            const int jj = (int)(slot % mma_k);
+            uint8_t* cbase = dst + (slot / chunk) * chunk_bytes;
+            const int jj = (int)(slot % chunk);
             for (int v = 0; v < V; ++v) {
                 const uint32_t x = get_bits(src, (long long)j * V + v, lhs_bits);
                 for (int pl = 0; pl < planes; ++pl)
-                    or_bits(chunk + pl * plane_bytes, (long long)v * mma_k + jj, plane_bits,
-                            (x >> (pl * plane_bits)) & pmask);
+                    or_bits(cbase, pl * plane_elems + v * vstride + jj, plane_bits, (x >> (pl * plane_bits)) & pmask);
             }
         }
     }

@@ -37,13 +37,13 @@ inline int persistent_ctas(K kernel, int threads, long long work_ctas)
     return n < 1 ? 1 : (int)n;
 }
 
-template <int V, int PA, int PB, bool S, bool H, int W, bool F>
+template <int V, int PA, int PB, bool S, bool H, int W, bool F, bool E>
 int spmm_launch_stream(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
     const long long ntasks = (long long)d.m_vec * d.batch;
     if (ntasks > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
     const int ny = d.n / (W * 32);
-    auto kern = spmm_stream_kernel<V, PA, PB, S, W, H, F>;
+    auto kern = spmm_stream_kernel<V, PA, PB, S, W, H, F, E>;
     // resident CTAs over all SMs, split across the ny column tiles
     const long long resident = persistent_ctas(kern, W * 32, 0x7fffffffLL);
     long long gx = (resident + ny - 1) / ny;
@@ -53,28 +53,32 @@ int spmm_launch_stream(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     return (int)cudaGetLastError();
 }
 
+// H (half output) is compiled only with the softmax value layout (E), the
+// combination the extension's batched SpMM uses; int32 output only with the
+// packer layout.
 template <int V, int PA, int PB, bool S, bool H>
 int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
+    constexpr bool E = H;
     const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
     const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
     if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
         return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");
     if (d.kernel_variant != MC_KERNEL_PER_ROW && stream_ok) {
         if (d.n % 128 == 0)
-            return f16 ? spmm_launch_stream<V, PA, PB, S, H, 4, true>(d, p, s)
-                       : spmm_launch_stream<V, PA, PB, S, H, 4, false>(d, p, s);
-        return f16 ? spmm_launch_stream<V, PA, PB, S, H, 2, true>(d, p, s)
-                   : spmm_launch_stream<V, PA, PB, S, H, 2, false>(d, p, s);
+            return f16 ? spmm_launch_stream<V, PA, PB, S, H, 4, true, E>(d, p, s)
+                       : spmm_launch_stream<V, PA, PB, S, H, 4, false, E>(d, p, s);
+        return f16 ? spmm_launch_stream<V, PA, PB, S, H, 2, true, E>(d, p, s)
+                   : spmm_launch_stream<V, PA, PB, S, H, 2, false, E>(d, p, s);
     }
     if (d.n % 128 == 0) {
         dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 128), (unsigned)d.batch);
-        if (f16) spmm_kernel<V, PA, PB, S, 4, H, true><<<grid, 128, 0, s>>>(p);
-        else spmm_kernel<V, PA, PB, S, 4, H, false><<<grid, 128, 0, s>>>(p);
+        if (f16) spmm_kernel<V, PA, PB, S, 4, H, true, E><<<grid, 128, 0, s>>>(p);
+        else spmm_kernel<V, PA, PB, S, 4, H, false, E><<<grid, 128, 0, s>>>(p);
     } else {
         dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 64), (unsigned)d.batch);
-        if (f16) spmm_kernel<V, PA, PB, S, 2, H, true><<<grid, 64, 0, s>>>(p);
-        else spmm_kernel<V, PA, PB, S, 2, H, false><<<grid, 64, 0, s>>>(p);
+        if (f16) spmm_kernel<V, PA, PB, S, 2, H, true, E><<<grid, 64, 0, s>>>(p);
+        else spmm_kernel<V, PA, PB, S, 2, H, false, E><<<grid, 64, 0, s>>>(p);
     }
     return (int)cudaGetLastError();
 }

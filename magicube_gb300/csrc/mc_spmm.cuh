@@ -42,13 +42,34 @@ struct SpmmParams {
     float scale;              // dequantisation divisor for half output
 };
 
-template <int PREA, int PREB>
+// Value layouts.  PACKED (EXT = false): the reference host packer's layout
+// (spmm_benchmark.cpp:224-377): chunks of MMA_K slots holding PLANES bit-planes
+// of PLANE_BITS each, plane-major, each plane [v][slot]; column indices of
+// 4-bit-operand pairs 8-shuffled.  SOFTMAX (EXT = true): the layout the
+// extension's quantized softmax writes (q_softmax_kernel.cu:133-176,258-269)
+// and its batched SpMM reads: it depends on the lhs width only -- 8-bit
+// [v][16 slots] per 16-slot chunk, 4-bit nibbles [v][32 slots] per 32-slot
+// chunk, 16-bit [v][low 16 bytes][high 16 bytes] per 16-slot chunk; column
+// indices unshuffled.
+template <int PREA, int PREB, bool EXT = false>
 struct SpmmLayout {
-    static constexpr int MMA_K = (PREA == 4 || PREB == 4) ? 32 : 16;  // slots per value chunk
-    static constexpr int PLANE_BITS = (PREA == 4 || PREB == 4) ? 4 : 8;
-    static constexpr int PLANES = PREA / PLANE_BITS;                   // bit-planes per chunk
-    static constexpr int BYTE_PLANES = PREA == 16 ? 2 : 1;             // int8 MMA operands
+    static constexpr int MMA_K = (PREA == 4 || PREB == 4) ? 32 : 16;     // row alignment in slots
+    static constexpr int VCHUNK = EXT ? (PREA == 4 ? 32 : 16) : MMA_K;   // slots per value chunk
+    static constexpr int PLANE_BITS = VCHUNK == 32 ? 4 : 8;
+    static constexpr int PLANES = PREA / PLANE_BITS;                     // bit-planes per chunk
+    static constexpr int BYTE_PLANES = PREA == 16 ? 2 : 1;               // int8 MMA operands
+    static constexpr bool INTERLEAVED = EXT && PREA == 16;               // [v][plane][16]
+    static constexpr bool SHUFFLED_COLS = !EXT && MMA_K == 32;
 };
+
+// Byte offset, inside one VCHUNK == 16 value chunk, of the word holding slots
+// 4t..4t+3 of vector lane g in byte plane bp.
+template <int V, int PREA, int PREB, bool EXT>
+__device__ __forceinline__ int vword16(int g, int t, int bp)
+{
+    if constexpr (SpmmLayout<PREA, PREB, EXT>::INTERLEAVED) return g * 32 + bp * 16 + 4 * t;
+    else return bp * V * 16 + g * 16 + 4 * t;
+}
 
 // Shared-memory geometry of one staged gathered-row slice.
 template <int PREB, int WARPS>
@@ -72,10 +93,10 @@ struct RhsSmem {
 // Logical slot -> stored position of its column index.  With MMA_K == 32 the
 // reference stores each group of 8 as [c0 c2 c4 c6 c1 c3 c5 c7]
 // (spmm_benchmark.cpp:218-222).
-template <int MMA_K>
+template <bool SHUFFLED>
 __device__ __forceinline__ int col_slot(int j)
 {
-    if constexpr (MMA_K == 32) return (j & ~7) | ((j & 1) << 2) | ((j & 7) >> 1);
+    if constexpr (SHUFFLED) return (j & ~7) | ((j & 1) << 2) | ((j & 7) >> 1);
     else return j;
 }
 
@@ -83,18 +104,18 @@ __device__ __forceinline__ int col_slot(int j)
 // operand bytes are converted exactly to f16 and the f32 partial sums, which
 // stay integers below 2^24, are flushed into int32 every 256 vector slots, so
 // the result is the same integer as the int8 path's.
-template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT, bool F16>
+template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT, bool F16, bool EXT>
 __global__ void __launch_bounds__(WARPS * 32)
 spmm_kernel(const SpmmParams p)
 {
-    using L = SpmmLayout<PREA, PREB>;
+    using L = SpmmLayout<PREA, PREB, EXT>;
     using S = RhsSmem<PREB, WARPS>;
     constexpr int STAGES = 4;
     constexpr int NT = WARPS * 32;
     constexpr int THREADS = WARPS * 32;
     constexpr int CHUNKS_PER_THREAD = (32 * S::CH) / THREADS;  // 2 for 8-bit B, 1 for 4-bit B
     constexpr int BP = L::BYTE_PLANES;
-    constexpr int PLANE_BYTES = V * L::MMA_K * L::PLANE_BITS / 8;
+    constexpr int PLANE_BYTES = V * L::VCHUNK * L::PLANE_BITS / 8;
     constexpr int CHUNK_BYTES = PLANE_BYTES * L::PLANES;
 
     __shared__ __align__(128) uint8_t rhs_s[STAGES * S::STAGE_BYTES];
@@ -128,7 +149,7 @@ spmm_kernel(const SpmmParams p)
 #pragma unroll
         for (int i = 0; i < CHUNKS_PER_THREAD; ++i) {
             int j = s * 32 + qrow[i];
-            c[i] = (s < steps && j < nnz) ? __ldg(cols + col_slot<L::MMA_K>(j)) : -1;
+            c[i] = (s < steps && j < nnz) ? __ldg(cols + col_slot<L::SHUFFLED_COLS>(j)) : -1;
         }
     };
     auto issue_stage = [&](int s, const int (&c)[CHUNKS_PER_THREAD]) {
@@ -155,13 +176,12 @@ spmm_kernel(const SpmmParams p)
             if (valid <= 0) continue;
             const uint32_t keep = byte_mask(valid);
             const int slot = start + jrel;
-            if constexpr (L::MMA_K == 16) {
+            if constexpr (L::VCHUNK == 16) {
                 // 8-bit planes: element (v, j) at byte v*16 + j of its plane.
                 const uint8_t* chunk = values + (long long)(slot >> 4) * CHUNK_BYTES;
-                const int off = g * 16 + (slot & 15);
 #pragma unroll
                 for (int bp = 0; bp < BP; ++bp)
-                    vals[bp][h] = __ldg(reinterpret_cast<const uint32_t*>(chunk + bp * PLANE_BYTES + off)) & keep;
+                    vals[bp][h] = __ldg(reinterpret_cast<const uint32_t*>(chunk + vword16<V, PREA, PREB, EXT>(g, t, bp))) & keep;
             } else {
                 // 4-bit planes: element (v, j) at nibble v*32 + j of its plane.
                 const uint8_t* chunk = values + (long long)(slot >> 5) * CHUNK_BYTES;

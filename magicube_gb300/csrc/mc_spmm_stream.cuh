@@ -56,18 +56,18 @@ struct StreamTask {
     int task, step, row, b, start, nnz, steps;
 };
 
-template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT, bool F16>
+template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT, bool F16, bool EXT>
 __global__ void __launch_bounds__(WARPS * 32)
 spmm_stream_kernel(const SpmmParams p, const int ntasks)
 {
-    using L = SpmmLayout<PREA, PREB>;
+    using L = SpmmLayout<PREA, PREB, EXT>;
     using S = StreamRhs<PREB, WARPS>;
     constexpr int STAGES = 4;
     constexpr int NT = WARPS * 32;
     constexpr int THREADS = WARPS * 32;
     constexpr int CPT = (32 * S::CH) / THREADS;  // rhs chunks per thread per stage
     constexpr int BP = L::BYTE_PLANES;
-    constexpr int PLANE_BYTES = V * L::MMA_K * L::PLANE_BITS / 8;
+    constexpr int PLANE_BYTES = V * L::VCHUNK * L::PLANE_BITS / 8;
     constexpr int CHUNK_BYTES = PLANE_BYTES * L::PLANES;
     constexpr int SLOT_BYTES = V * PREA / 8;         // value bytes per vector slot
     constexpr int VALS_BYTES = 32 * SLOT_BYTES;      // value bytes per step
@@ -114,7 +114,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
 #pragma unroll
         for (int i = 0; i < CPT; ++i) {
             const int j = c.step * 32 + qrow[i];
-            col[i] = (c.task < ntasks && j < c.nnz) ? __ldg(p.col_indices + c.start + col_slot<L::MMA_K>(j)) : -1;
+            col[i] = (c.task < ntasks && j < c.nnz) ? __ldg(p.col_indices + c.start + col_slot<L::SHUFFLED_COLS>(j)) : -1;
         }
     };
     auto issue = [&](const StreamTask& c, const int (&col)[CPT], int slot) {
@@ -197,10 +197,10 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const uint32_t keep = full ? 0xffffffffu : byte_mask(nnz - (step * 32 + 16 * h + 4 * t));
-                    if constexpr (L::MMA_K == 16) {
+                    if constexpr (L::VCHUNK == 16) {
 #pragma unroll
                         for (int bp = 0; bp < BP; ++bp)
-                            vals[bp][h] = lds32(vs + h * CHUNK_BYTES + bp * PLANE_BYTES + g * 16 + 4 * t) & keep;
+                            vals[bp][h] = lds32(vs + h * CHUNK_BYTES + vword16<V, PREA, PREB, EXT>(g, t, bp)) & keep;
                     } else {
                         uint32_t nib[L::PLANES];
 #pragma unroll

@@ -68,16 +68,19 @@ def pad_column_indices(mask: VectorSparse, pairs: np.ndarray, aligned_nnz: int, 
     return out[:aligned_nnz]
 
 
+VALUES_PACKED, VALUES_SOFTMAX = 0, 1
+
+
 def pack_spmm_values(mask: VectorSparse, pairs: np.ndarray, aligned_nnz: int, values: np.ndarray,
-                     lhs_bits: int, rhs_bits: int) -> np.ndarray:
+                     lhs_bits: int, rhs_bits: int, layout: int = VALUES_PACKED) -> np.ndarray:
     """values: uint8 array of nnz_vec * V * lhs_bits / 8 bytes (lane v at bit v*lhs_bits)."""
     ro = np.ascontiguousarray(mask.row_offsets, dtype=np.int32)
     v = np.ascontiguousarray(values, dtype=np.uint8)
     nbytes = aligned_nnz * mask.vec_length * lhs_bits // 8
     out = np.empty(max(nbytes, 4), dtype=np.uint8)
-    _lib.check(_lib.lib().mcPackSpmmValues(mask.m_vec, mask.vec_length, lhs_bits, rhs_bits, _ptr(ro), _ptr(pairs),
-                                           aligned_nnz, _ptr(v) if v.size else None, _ptr(out)),
-               "mcPackSpmmValues")
+    _lib.check(_lib.lib().mcPackSpmmValuesEx(mask.m_vec, mask.vec_length, lhs_bits, rhs_bits, _ptr(ro),
+                                             _ptr(pairs), aligned_nnz, _ptr(v) if v.size else None, _ptr(out), layout),
+               "mcPackSpmmValuesEx")
     return out[:nbytes]
 
 
@@ -107,11 +110,11 @@ class SpmmLhs:
 
 
 def prepare_spmm(mask: VectorSparse, values: np.ndarray, lhs_bits: int, rhs_bits: int,
-                 sort_rows: bool = True) -> SpmmLhs:
+                 sort_rows: bool = True, layout: int = VALUES_PACKED) -> SpmmLhs:
     chunk = spmm_chunk(lhs_bits, rhs_bits)
     pairs, n = align_row_offsets(mask, chunk)
-    cols = pad_column_indices(mask, pairs, n, shuffle8=(chunk == 32))
-    vals = pack_spmm_values(mask, pairs, n, values, lhs_bits, rhs_bits)
+    cols = pad_column_indices(mask, pairs, n, shuffle8=(chunk == 32 and layout == VALUES_PACKED))
+    vals = pack_spmm_values(mask, pairs, n, values, lhs_bits, rhs_bits, layout)
     ri = sorted_row_swizzle(mask) if sort_rows else identity_row_swizzle(mask.m_vec)
     return SpmmLhs(mask, lhs_bits, rhs_bits, ri, pairs, cols, vals, n)
 

@@ -89,7 +89,7 @@ def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, 
         row_indices=lhs.row_indices.data_ptr(), row_offsets=lhs.row_offsets.data_ptr(),
         column_indices=lhs.col_indices.data_ptr(), values=lhs.values.data_ptr(), values_stride=values_stride,
         rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride, mma_kind=mma_kind,
-        kernel_variant=variant)
+        kernel_variant=variant, value_layout=_lib.VALUES_SOFTMAX if out_half else _lib.VALUES_PACKED)
     _lib.check(_lib.lib().mcSpmm(ctypes.byref(d), _stream_handle(stream)), "mcSpmm")
     return out
 

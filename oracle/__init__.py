@@ -39,7 +39,7 @@ def lib() -> ctypes.CDLL:
         h.mco_spmm_host.restype = None
         h.mco_sddmm_host.argtypes = [vp, vp, vp] + [ci] * 6 + [vp, vp, ci, ci, ci]
         h.mco_sddmm_host.restype = None
-        h.mco_spmm_device.argtypes = [vp, vp, vp, vp, vp] + [ci] * 7
+        h.mco_spmm_device.argtypes = [vp, vp, vp, vp, vp] + [ci] * 8
         h.mco_spmm_device.restype = None
         _handle = h
     return _handle
@@ -79,12 +79,12 @@ def sddmm_host(lhs: np.ndarray, rhs: np.ndarray, pairs: np.ndarray, cols: np.nda
 
 
 def spmm_device(pairs: np.ndarray, cols: np.ndarray, dev_values: np.ndarray, rhs: np.ndarray, m_vec: int,
-                V: int, K: int, N: int, preA: int, preB: int, mode: int) -> np.ndarray:
+                V: int, K: int, N: int, preA: int, preB: int, mode: int, layout: int = 0) -> np.ndarray:
     """C (M x N int32) decoded from the SpMM device operand layout."""
     pr = np.ascontiguousarray(pairs, dtype=np.int32)
     cc = np.ascontiguousarray(cols, dtype=np.int32)
     dv = np.ascontiguousarray(dev_values).view(np.uint8)
     rhs = np.ascontiguousarray(rhs).view(np.uint8)
     out = np.empty((m_vec * V, N), dtype=np.int32)
-    lib().mco_spmm_device(_p(pr), _p(cc), _p(dv), _p(rhs), _p(out), m_vec, V, K, N, preA, preB, mode)
+    lib().mco_spmm_device(_p(pr), _p(cc), _p(dv), _p(rhs), _p(out), m_vec, V, K, N, preA, preB, mode, layout)
     return out

@@ -173,16 +173,22 @@ void mco_sddmm_host(const int32_t* lhs, const int32_t* rhs, int32_t* out,
  */
 void mco_spmm_device(const int32_t* row_offsets, const int32_t* col_indices,
                      const uint8_t* values, const int32_t* rhs, int32_t* out,
-                     int m_vec, int V, int K, int N, int preA, int preB, int mode)
+                     int m_vec, int V, int K, int N, int preA, int preB, int mode, int layout)
 {
     (void)K;
     const int mma_k = (preA == 4 || preB == 4) ? 32 : 16;
-    int plane_bits, planes;
-    if (preA == 4) { plane_bits = 4; planes = 1; }
-    else if (preA == 8) { plane_bits = preB == 4 ? 4 : 8; planes = preB == 4 ? 2 : 1; }
-    else { plane_bits = preB == 4 ? 4 : 8; planes = preB == 4 ? 4 : 2; }
-    const int plane_bytes = V * mma_k * plane_bits / 8;
-    const int chunk_bytes = plane_bytes * planes;
+    /* layout 0: the packer's (above).  layout 1: the layout the extension's
+     * quantized softmax writes (q_softmax_kernel.cu:133-176,258-269): chunks of
+     * 16 slots ([v][16] bytes for 8-bit, [v][low 16][high 16] for 16-bit) or
+     * of 32 slots for 4-bit ([v][32] nibbles); column indices unshuffled. */
+    const int softmax = layout == 1;
+    const int chunk = softmax ? (preA == 4 ? 32 : 16) : mma_k;
+    const int plane_bits = chunk == 32 ? 4 : 8;
+    const int planes = preA / plane_bits;
+    const int interleaved = softmax && preA == 16;
+    const int chunk_bytes = V * chunk * preA / 8;
+    const int plane_elems = interleaved ? chunk : V * chunk;
+    const int vstride = interleaved ? planes * chunk : chunk;
     const int b_tile = 32 / preB;
     const int ints_per_row = N / b_tile;
     const uint32_t mb = (1u << preB) - 1u;
@@ -192,19 +198,18 @@ void mco_spmm_device(const int32_t* row_offsets, const int32_t* col_indices,
     for (int i = 0; i < m_vec; ++i) {
         const int start = row_offsets[2 * i], end = row_offsets[2 * i + 1];
         for (int j = start; j < end; ++j) {
-            int slot = j;
             int stored = j;
-            if (mma_k == 32) {
+            if (mma_k == 32 && !softmax) {
                 int p = j % 8;  /* logical position p lives at shuffled slot */
                 stored = (j / 8) * 8 + (p % 2) * 4 + p / 2;
             }
             const int col = col_indices[stored];
-            const int chunk = slot / mma_k, jj = slot % mma_k;
-            const uint8_t* cbase = values + (size_t)chunk * chunk_bytes;
+            const int ci = j / chunk, jj = j % chunk;
+            const uint8_t* cbase = values + (size_t)ci * chunk_bytes;
             for (int v = 0; v < V; ++v) {
                 uint32_t raw = 0;
                 for (int p = 0; p < planes; ++p)
-                    raw |= lane_u(cbase + (size_t)p * plane_bytes, (int64_t)v * mma_k + jj, plane_bits) << (p * plane_bits);
+                    raw |= lane_u(cbase, (int64_t)p * plane_elems + (int64_t)v * vstride + jj, plane_bits) << (p * plane_bits);
                 int32_t a = (mode == MCO_SIGNED) ? sext(raw, planes * plane_bits) : (int32_t)raw;
                 const uint32_t* brow = (const uint32_t*)rhs + (size_t)col * ints_per_row;
                 uint32_t* crow = acc + (size_t)(i * V + v) * N;

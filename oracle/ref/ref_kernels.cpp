@@ -17,7 +17,7 @@
 
 extern "C" size_t mcref_alloc_size(const void* p);
 extern "C" void mco_spmm_device(const int32_t*, const int32_t*, const uint8_t*, const int32_t*, int32_t*, int, int,
-                                int, int, int, int, int);
+                                int, int, int, int, int, int);
 extern "C" void mco_sddmm_host(const int32_t*, const int32_t*, int32_t*, int, int, int, int, int, int,
                                const int32_t*, const int32_t*, int, int, int);
 
@@ -50,7 +50,7 @@ static int spmm_stub(int preA, int preB, int m_vec, int V, int n, int k, const i
     if (done == out) return 0;
     done = out;
     mco_spmm_device(ro, ci, reinterpret_cast<const uint8_t*>(values), rhs, out, m_vec, V, k, n, preA, preB,
-                    /*unsigned lanes*/ 1);
+                    /*unsigned lanes*/ 1, /*packer layout*/ 0);
     dump_meta("spmm", m_vec, V, n, k, preA, preB);
     dump("row_indices.bin", ri, mcref_alloc_size(ri));
     dump("row_offsets.bin", ro, mcref_alloc_size(ro));

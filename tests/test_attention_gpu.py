@@ -1,0 +1,151 @@
+"""The sparse-attention steps (sptrans mirror) and the attention module on the
+GPU, against the CPU oracle (oracle/attention.py, oracle/mc_oracle.c)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+import oracle.attention as oatt
+from magicube_gb300 import attention, formats, masks, synth
+from magicube_gb300.sptrans import deq_sddmm, deq_spmm, q_softmax, quantization
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("bits", [4, 8])
+@pytest.mark.parametrize("shape", [(2, 64, 64), (3, 40, 32)])
+def test_bquantization(cuda, bits, shape):
+    x = (torch.randn(shape, generator=torch.Generator().manual_seed(1)) * 3).half()
+    got = quantization.bquantization(x.to(cuda), bits, 36.0)
+    assert got.shape == (shape[0], shape[1], shape[2] * bits // 32)
+    ref = oatt.quantize(x.numpy(), bits, 36.0)
+    np.testing.assert_array_equal(got.cpu().numpy().view(np.uint8).ravel(), ref)
+
+
+def _mask(L, V, bits_rhs, seed):
+    mma_k = 16 if bits_rhs == 8 else 32
+    (cols, cols_sh, pairs, ri, n), m = masks.banded_random_mask(L, V, 32, 0.8, mma_k, seed=seed)
+    return m, cols, pairs, ri, n
+
+
+@pytest.mark.parametrize("bits", [4, 8])
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_bsddmm(cuda, bits, V):
+    L, d, B = 256, 64, 3
+    m, cols, pairs, ri, n = _mask(L, V, bits, seed=V + bits)
+    rng = np.random.default_rng(5)
+    lhs = rng.integers(0, 256, size=(B, L, d * bits // 8), dtype=np.uint8)
+    rhs = rng.integers(0, 256, size=(B, L, d * bits // 8), dtype=np.uint8)
+    fn = deq_sddmm.bsddmm_8b if bits == 8 else deq_sddmm.bsddmm_4b
+    scale = 36.0 * 36.0
+    got = fn(ri, pairs, cols, torch.from_numpy(lhs).view(torch.int32).to(cuda),
+             torch.from_numpy(rhs).view(torch.int32).to(cuda), V, bits, scale).cpu().numpy()
+    assert got.shape == (B, n * V)
+    hp, hc = pairs.cpu().numpy(), cols.cpu().numpy()
+    written = np.zeros(n * V, bool)
+    for i in range(m.m_vec):
+        written[hp[2 * i] * V:hp[2 * i + 1] * V] = True
+    for b in range(B):
+        acc = oracle.sddmm_host(lhs[b], rhs[b], hp, hc, m.m_vec, V, d, L, bits, bits, oracle.SIGNED,
+                                layout=oracle.OUT_VECMAJOR)
+        ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
+        np.testing.assert_array_equal(got[b][written].view(np.uint16), ref[written].view(np.uint16))
+
+
+def _decode_softmax(buf: np.ndarray, pairs, V, bits, n):
+    """Packed softmax-layout bytes -> signed ints per (slot, lane)."""
+    out = np.zeros((n, V), dtype=np.int64)
+    for s in range(n):
+        for v in range(V):
+            if bits == 8:
+                x = buf[(s // 16) * V * 16 + v * 16 + s % 16]
+                out[s, v] = x - 256 if x >= 128 else x
+            elif bits == 16:
+                o = (s // 16) * V * 32 + v * 32 + s % 16
+                x = int(buf[o]) | (int(buf[o + 16]) << 8)
+                out[s, v] = x - 65536 if x >= 32768 else x
+            else:
+                x = (buf[(s // 32) * V * 16 + v * 16 + (s % 32) // 2] >> (4 * (s % 2))) & 0xF
+                out[s, v] = x - 16 if x >= 8 else x
+    return out
+
+
+@pytest.mark.parametrize("bits,scale", [(8, 32.0), (8, 127.0), (16, 32767.0), (4, 7.0)])
+@pytest.mark.parametrize("V", [2, 8])
+def test_q_bcsr_softmax(cuda, bits, scale, V):
+    """Quantized softmax vs the fp32 restatement: every value within 1 of it,
+    and equal wherever p*scale is not within 1e-3 of an integer (the GPU's
+    __expf and summation order differ from numpy's in the last bits)."""
+    L, B = 256, 2
+    m, cols, pairs, ri, n = _mask(L, V, 8 if bits != 4 else 4, seed=11)
+    rng = np.random.default_rng(3)
+    scores = (rng.standard_normal((B, n * V)) * 20).astype(np.float16)
+    got = q_softmax.q_bcsr_softmax(ri, pairs, torch.from_numpy(scores).to(cuda), 0.125, scale, V, B, bits)
+    got = got.cpu().numpy().view(np.uint8)
+    hp, hr = pairs.cpu().numpy(), ri.cpu().numpy()
+    for b in range(B):
+        ref, exact = oatt.softmax_quant(scores[b], hp, hr, V, bits, 0.125, scale, got.shape[1])
+        g = _decode_softmax(got[b], hp, V, bits, n)
+        r = _decode_softmax(ref, hp, V, bits, n)
+        assert np.abs(g - r).max() <= 1
+        frac = np.abs(exact.reshape(n, V) - np.round(exact.reshape(n, V)))
+        safe = frac > 1e-3
+        np.testing.assert_array_equal(g[safe], r[safe])
+
+
+@pytest.mark.parametrize("pa,pb", [(4, 4), (8, 4), (8, 8), (16, 8)])
+@pytest.mark.parametrize("V", [2, 8])
+def test_bspmm(cuda, pa, pb, V):
+    L, d, B = 256, 64, 2
+    m, cols, pairs, ri, n = _mask(L, V, pb, seed=21)
+    hp = pairs.cpu().numpy()
+    rng = np.random.default_rng(9)
+    vals = [rng.integers(0, 256, size=m.nnz_vec * V * pa // 8, dtype=np.uint8) for _ in range(B)]
+    packed = [formats.pack_spmm_values(m, hp, n, v, pa, pb, layout=formats.VALUES_SOFTMAX) for v in vals]
+    rhs = rng.integers(0, 256, size=(B, L, d * pb // 8), dtype=np.uint8)
+    fn = {(4, 4): deq_spmm.bspmm_4b, (8, 4): deq_spmm.bspmm_8b4b, (8, 8): deq_spmm.bspmm_8b,
+          (16, 8): deq_spmm.bspmm_16b8b}[(pa, pb)]
+    scale = 36.0 * 32.0
+    vt = torch.from_numpy(np.stack(packed)).view(torch.int32).to(cuda)
+    got = fn(ri, pairs, cols, vt, torch.from_numpy(rhs).view(torch.int32).to(cuda), V, pa, pb, scale)
+    assert got.shape == (B, L, d)
+    for b in range(B):
+        acc = oracle.spmm_host(vals[b], rhs[b], m.row_offsets, m.col_indices, m.m_vec, V, L, d, pa, pb, oracle.SIGNED)
+        ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
+        np.testing.assert_array_equal(got[b].cpu().numpy().view(np.uint16), ref.view(np.uint16))
+
+
+@pytest.mark.parametrize("lhs_pre,rhs_pre", [(8, 8), (16, 8), (8, 4), (4, 4)])
+def test_sparse_attention_error_vs_fp64(cuda, lhs_pre, rhs_pre):
+    """The full quantized attention against the float64 oracle of the
+    unquantized computation.  With calibrated scales (activations scaled to
+    the integer range, probabilities to the full output range) the relative
+    error is bounded per precision pair; with the reference's fixed scales
+    (36, 32) it is only reported (probabilities below 1/32 truncate to 0)."""
+    torch.manual_seed(0)
+    L, bsz, E, H, V = 256, 2, 128, 2, 8
+    d = E // H
+    mha = attention.SpMultiheadAttention(E, H).to(cuda).half()
+    x = (torch.randn(L, bsz, E, device=cuda) * 0.5).half()
+    mma_k = 16 if rhs_pre == 8 else 32
+    (cols, _, pairs, ri, n), m = masks.banded_random_mask(L, V, 64, 0.8, mma_k, seed=4)
+    qmax = {8: 127.0, 4: 7.0}[rhs_pre]
+    with torch.no_grad():
+        q, k, v = torch.nn.functional.linear(x, mha.in_proj_weight, mha.in_proj_bias).chunk(3, dim=-1)
+        amax = max(float(t.abs().max()) for t in (q, k, v))
+        pmax = {16: 32767.0, 8: 127.0, 4: 7.0}[lhs_pre]
+        out, _ = mha(x, x, x, need_weights=False, row_indices=ri, row_offsets=pairs, column_indices=cols,
+                     vec_length=V, lhs_pre=lhs_pre, rhs_pre=rhs_pre, scale_qkv=qmax / amax, scale_sfmx=pmax)
+        # reference path: attention core in float64, same projections
+        heads = lambda t: t.contiguous().view(L, bsz * H, d).transpose(0, 1).double().cpu().numpy()  # noqa: E731
+        mk = oatt.dense_mask(pairs.cpu().numpy(), cols.cpu().numpy(), m.m_vec, V, L)
+        core = oatt.sparse_attention_fp64(heads(q), heads(k), heads(v), mk, d ** -0.5)
+        core = torch.from_numpy(core).transpose(0, 1).reshape(L, bsz, E)
+        ref = torch.nn.functional.linear(core, mha.out_proj.weight.double().cpu(), mha.out_proj.bias.double().cpu())
+    err = (out.double().cpu() - ref).norm() / ref.norm()
+    # Measured on GB300 for this seed: L16-R8 0.025, L8-R8 0.23, L8-R4 0.49,
+    # L4-R4 1.0 (truncated 4-bit probabilities of rows with ~50 nonzeros are
+    # all zero: the error of the reference's own quantization scheme).
+    bound = {(8, 8): 0.3, (16, 8): 0.05, (8, 4): 0.6, (4, 4): 1.0001}[(lhs_pre, rhs_pre)]
+    assert torch.isfinite(out).all()
+    assert err < bound, f"relative error {err:.4f} >= {bound}"

@@ -42,11 +42,13 @@ def test_pack_then_decode_equals_oracle(pa, pb, V):
     m = synth.lengths_mask([0, 1, 31, 32, 33, 100, 7], K, V, seed=pa + pb + V)
     vals = synth.random_bytes(m.nnz_vec * V * pa // 8, 1)
     rhs = synth.random_bytes(K * N * pb // 8, 2)
-    h = formats.prepare_spmm(m, vals, pa, pb)
-    for mode in (oracle.UNSIGNED, oracle.SIGNED):
-        a = oracle.spmm_host(vals, rhs, m.row_offsets, m.col_indices, m.m_vec, V, K, N, pa, pb, mode)
-        b = oracle.spmm_device(h.row_offsets, h.col_indices, h.values, rhs, m.m_vec, V, K, N, pa, pb, mode)
-        np.testing.assert_array_equal(a, b)
+    for layout in (formats.VALUES_PACKED, formats.VALUES_SOFTMAX):
+        h = formats.prepare_spmm(m, vals, pa, pb, layout=layout)
+        for mode in (oracle.UNSIGNED, oracle.SIGNED):
+            a = oracle.spmm_host(vals, rhs, m.row_offsets, m.col_indices, m.m_vec, V, K, N, pa, pb, mode)
+            b = oracle.spmm_device(h.row_offsets, h.col_indices, h.values, rhs, m.m_vec, V, K, N, pa, pb, mode,
+                                   layout)
+            np.testing.assert_array_equal(a, b)
 
 
 def test_empty_matrix_packs():

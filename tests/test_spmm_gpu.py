@@ -108,12 +108,15 @@ def test_spmm_batched_strided(cuda, pa, pb):
 
 
 @pytest.mark.parametrize("pa,pb", [(4, 4), (8, 4), (8, 8), (16, 8)])
-def test_spmm_half_output(cuda, pa, pb):
-    V, K, N, scale = 8, 256, 64, 36.0 * 32.0
+@pytest.mark.parametrize("V", [2, 4, 8])
+@pytest.mark.parametrize("variant", [_lib.KERNEL_PER_ROW, _lib.KERNEL_STREAM])
+def test_spmm_half_output(cuda, pa, pb, V, variant):
+    """Dequantised half output on the softmax value layout (the extension's bspmm)."""
+    K, N, scale = 256, 64, 36.0 * 32.0
     mask, vals, rhs = _case(pa, pb, V, K, N, RAGGED, seed=5)
-    h = formats.prepare_spmm(mask, vals, pa, pb)
+    h = formats.prepare_spmm(mask, vals, pa, pb, layout=formats.VALUES_SOFTMAX)
     d = ops.DeviceSpmmLhs.from_host(h, cuda)
-    out = ops.spmm(d, torch.from_numpy(rhs).to(cuda), N, signed=True, out_half=True, scale=scale)
+    out = ops.spmm(d, torch.from_numpy(rhs).to(cuda), N, signed=True, out_half=True, scale=scale, variant=variant)
     acc = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb, oracle.SIGNED)
     ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
     np.testing.assert_array_equal(out.cpu().numpy().view(np.uint16), ref.view(np.uint16))

@@ -362,6 +362,38 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
             "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"], "instances_per_step": B}
 
 
+def run_profile_case(args) -> None:
+    """A small case of one kernel for ncu captures: `--batch` instances of the
+    headline SDDMM (about 7.3 MB each) or of the SpMM L8-R8 configuration
+    (about 1.4 MB each), launched `--reps` times."""
+    import torch
+
+    from magicube_gb300 import formats, ops, synth
+    dev = torch.device("cuda:0")
+    if args.profile == "sddmm":
+        mask, hm, lhs_h, rhs_h = sddmm_workload(8, 8, args.batch)
+        dm = ops.DeviceSddmmMask.from_host(hm, dev)
+        lhs, rhs = torch.from_numpy(lhs_h).to(dev), torch.from_numpy(rhs_h).to(dev)
+        out = torch.empty((args.batch, hm.aligned_nnz * VEC), dtype=torch.int32, device=dev)
+        for _ in range(args.reps):
+            ops.sddmm(dm, lhs, rhs, HEAD_DIM, 8, 8, signed=True, out=out, batch=args.batch, mma_kind=args.mma)
+    else:
+        M = K = 1024
+        N = 256
+        mask = synth.uniform_mask(M // VEC, K, VEC, SPARSITY, seed=7)
+        vals = np.random.default_rng(8).integers(0, 256, size=mask.nnz_vec * VEC, dtype=np.uint8)
+        h = formats.prepare_spmm(mask, vals, 8, 8)
+        d = ops.DeviceSpmmLhs.from_host(h, dev)
+        d.values = d.values.repeat(args.batch)
+        rhs = torch.randint(0, 256, (args.batch, K * N), dtype=torch.uint8, device=dev)
+        out = torch.empty((args.batch, M, N), dtype=torch.int32, device=dev)
+        for _ in range(args.reps):
+            ops.spmm(d, rhs, N, signed=True, out=out, batch=args.batch, values_stride=h.values.size,
+                     mma_kind=args.mma)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": args.profile, "batch": args.batch, "reps": args.reps}))
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -370,6 +402,9 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=64, help="instances per step")
     ap.add_argument("--impl", choices=["magicube_gb300", "reference"], default="magicube_gb300")
     ap.add_argument("--headline-only", action="store_true")
+    ap.add_argument("--profile", choices=["sddmm", "spmm"], default=None,
+                    help="run only a small case of one kernel (for ncu captures)")
+    ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")
     ap.add_argument("--mma", choices=["int8", "f16"], default="int8",
                     help="tensor path (both are bit-exact; see include/magicube_gb300.h)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -377,7 +412,11 @@ def main() -> None:
     if args.warmup < 3:
         args.warmup = 3
     args.mma = 2 if args.mma == "f16" else 1
-    if args.impl == "reference":
+    if args.profile:
+        if args.batch == 64 and args.profile == "spmm":
+            args.batch = 128
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

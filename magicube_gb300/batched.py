@@ -1,0 +1,215 @@
+"""Batched sparse attention over uneven instances in one set of launches.
+
+Instances of different sequence lengths, each with its own vector-sparse
+mask, are laid out as one block-diagonal vector-sparse problem: their
+vector-rows are stacked, and each instance's column indices are offset by the
+instance's first token in the stacked Q / K / V.  Heads are the batch
+dimension.  One quantization, one SDDMM, one quantized softmax and one SpMM
+launch then cover every (instance, head) pair -- the kernels see a single
+large mask whose rows are processed longest first -- and the four launches
+can be captured in a CUDA graph and replayed.  Each instance's result is the
+same, bit for bit, as when it runs alone (the per-row arithmetic does not
+depend on the other rows).
+
+PerInstanceSparseAttention runs the same computation with separate launches
+per instance (the plain baseline).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib, autotune, formats
+from .formats import VectorSparse
+
+
+@dataclass
+class AttentionMaskDev:
+    m_vec: int
+    vec_length: int
+    seq_len: int
+    aligned_nnz: int
+    row_indices: torch.Tensor
+    row_offsets: torch.Tensor
+    col_indices: torch.Tensor
+
+
+def block_diagonal(masks: list[VectorSparse]) -> tuple[VectorSparse, np.ndarray]:
+    """Stack masks into one block-diagonal mask; returns it and the token
+    offset of every instance."""
+    V = masks[0].vec_length
+    if any(m.vec_length != V for m in masks):
+        raise ValueError("all instances must use the same vector length")
+    tok = np.zeros(len(masks) + 1, dtype=np.int64)
+    for i, m in enumerate(masks):
+        if m.ncols != m.m_vec * V:
+            raise ValueError("an attention mask must be seq_len x seq_len")
+        tok[i + 1] = tok[i] + m.ncols
+    ro = [np.zeros(1, dtype=np.int64)]
+    cols = []
+    base = 0
+    for i, m in enumerate(masks):
+        ro.append(m.row_offsets[1:].astype(np.int64) + base)
+        cols.append(m.col_indices.astype(np.int64) + tok[i])
+        base += m.nnz_vec
+    row_offsets = np.concatenate(ro).astype(np.int32)
+    col_indices = np.concatenate(cols).astype(np.int32) if cols else np.zeros(0, np.int32)
+    mega = VectorSparse(int(sum(m.m_vec for m in masks)), V, int(tok[-1]), row_offsets, col_indices)
+    return mega, tok
+
+
+def to_device(mask: VectorSparse, alignment: int, device) -> AttentionMaskDev:
+    pairs, n = formats.align_row_offsets(mask, alignment)
+    cols = formats.pad_column_indices(mask, pairs, n, shuffle8=False)
+    ri = formats.sorted_row_swizzle(mask)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)  # noqa: E731
+    return AttentionMaskDev(mask.m_vec, mask.vec_length, mask.ncols, n, t(ri), t(pairs),
+                            t(cols if cols.size else np.full(1, -1, np.int32)))
+
+
+class _AttentionCore:
+    """quantize -> SDDMM -> quantized softmax -> SpMM on one mask (heads batched)."""
+
+    def __init__(self, mask: AttentionMaskDev, heads: int, head_dim: int, lhs_bits: int, rhs_bits: int,
+                 scale_qkv: float, scale_sfmx: float, device, tune: bool):
+        if head_dim % 64:
+            raise ValueError("head_dim must be a multiple of 64")
+        self.m, self.H, self.d = mask, heads, head_dim
+        self.lb, self.rb = lhs_bits, rhs_bits
+        self.scale_qkv, self.scale_sfmx = scale_qkv, scale_sfmx
+        self.scaling = head_dim ** -0.5
+        L, V = mask.seq_len, mask.vec_length
+        self.q_words = L * head_dim * rhs_bits // 32
+        self.qkv_q = torch.empty((3, heads, self.q_words), dtype=torch.int32, device=device)
+        self.scores = torch.empty((heads, mask.aligned_nnz * V), dtype=torch.float16, device=device)
+        self.probs = torch.zeros((heads, mask.aligned_nnz * V * lhs_bits // 32), dtype=torch.int32, device=device)
+        self.out = torch.empty((heads, L, head_dim), dtype=torch.float16, device=device)
+        self.sddmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO, "row_split": 0}
+        self.spmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO}
+        self._tune = tune
+
+    # -- the four steps -----------------------------------------------------
+    def _quantize(self, qkv: torch.Tensor, stream) -> None:
+        _lib.check(_lib.lib().mcQuantize(qkv.data_ptr(), self.qkv_q.data_ptr(), qkv.numel(), self.rb,
+                                         float(self.scale_qkv), stream), "mcQuantize")
+
+    def _sddmm(self, cfg: dict, stream) -> None:
+        m = self.m
+        bytes_per_head = self.q_words * 4
+        d = _lib.McSddmmDesc(
+            m_vec=m.m_vec, vec_length=m.vec_length, n=m.seq_len, k=self.d, lhs_bits=self.rb, rhs_bits=self.rb,
+            is_signed=1, out_half=1, out_vecmajor=1, scale=float(self.scale_qkv ** 2), batch=self.H,
+            row_split=cfg.get("row_split", 0), row_indices=m.row_indices.data_ptr(),
+            row_offsets=m.row_offsets.data_ptr(), column_indices=m.col_indices.data_ptr(),
+            lhs=self.qkv_q[0].data_ptr(), lhs_stride=bytes_per_head, rhs=self.qkv_q[1].data_ptr(),
+            rhs_stride=bytes_per_head, out=self.scores.data_ptr(), out_stride=self.scores.shape[1],
+            mma_kind=cfg["mma_kind"], kernel_variant=cfg["variant"])
+        _lib.check(_lib.lib().mcSddmm(ctypes.byref(d), stream), "mcSddmm")
+
+    def _softmax(self, stream) -> None:
+        m = self.m
+        d = _lib.McSoftmaxDesc(
+            m_vec=m.m_vec, vec_length=m.vec_length, batch=self.H, bits=self.lb, scaling=float(self.scaling),
+            scale=float(self.scale_sfmx), row_indices=m.row_indices.data_ptr(), row_offsets=m.row_offsets.data_ptr(),
+            scores=self.scores.data_ptr(), scores_stride=self.scores.shape[1], out=self.probs.data_ptr(),
+            out_stride=self.probs.shape[1] * 4)
+        _lib.check(_lib.lib().mcQuantSoftmax(ctypes.byref(d), stream), "mcQuantSoftmax")
+
+    def _spmm(self, cfg: dict, stream) -> None:
+        m = self.m
+        d = _lib.McSpmmDesc(
+            m_vec=m.m_vec, vec_length=m.vec_length, n=self.d, k=m.seq_len, lhs_bits=self.lb, rhs_bits=self.rb,
+            is_signed=1, out_half=1, scale=float(self.scale_qkv * self.scale_sfmx), batch=self.H,
+            row_indices=m.row_indices.data_ptr(), row_offsets=m.row_offsets.data_ptr(),
+            column_indices=m.col_indices.data_ptr(), values=self.probs.data_ptr(),
+            values_stride=self.probs.shape[1] * 4, rhs=self.qkv_q[2].data_ptr(), rhs_stride=self.q_words * 4,
+            out=self.out.data_ptr(), out_stride=m.seq_len * self.d, mma_kind=cfg["mma_kind"],
+            kernel_variant=cfg["variant"], value_layout=_lib.VALUES_SOFTMAX)
+        _lib.check(_lib.lib().mcSpmm(ctypes.byref(d), stream), "mcSpmm")
+
+    def tune(self, qkv: torch.Tensor) -> None:
+        """Pick the SDDMM and SpMM configurations with the autotuner."""
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        m = self.m
+        avg = m.aligned_nnz / max(1, m.m_vec)
+        self._quantize(qkv, stream)
+        sig = autotune.signature("sddmm_attn", self.rb, self.rb, m.vec_length, self.d, m.m_vec, avg, self.H)
+        self.sddmm_cfg = autotune.tune(sig, autotune.sddmm_candidates(self.d), lambda c: self._sddmm(c, stream))
+        self._sddmm(self.sddmm_cfg, stream)
+        self._softmax(stream)
+        sig = autotune.signature("spmm_attn", self.lb, self.rb, m.vec_length, self.d, m.m_vec, avg, self.H)
+        self.spmm_cfg = autotune.tune(sig, autotune.spmm_candidates(), lambda c: self._spmm(c, stream))
+
+    def run(self, qkv: torch.Tensor) -> torch.Tensor:
+        """qkv: [3, H, L, d] half (contiguous) -> [H, L, d] half."""
+        if self._tune:
+            self.tune(qkv)
+            self._tune = False
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        self._quantize(qkv, stream)
+        self._sddmm(self.sddmm_cfg, stream)
+        self._softmax(stream)
+        self._spmm(self.spmm_cfg, stream)
+        return self.out
+
+
+class BatchedSparseAttention:
+    """Sparse attention of uneven instances (own length and mask each), all
+    heads and instances in one quantize / SDDMM / softmax / SpMM sequence."""
+
+    def __init__(self, masks: list[VectorSparse], heads: int, head_dim: int = 64, lhs_bits: int = 8,
+                 rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 32.0, device="cuda",
+                 tune: bool = True):
+        mega, self.token_offsets = block_diagonal(masks)
+        align = 16 if rhs_bits == 8 else 32
+        self.mask = to_device(mega, align, device)
+        self.core = _AttentionCore(self.mask, heads, head_dim, lhs_bits, rhs_bits, scale_qkv, scale_sfmx, device,
+                                   tune)
+        self.seq_lens = [m.ncols for m in masks]
+        self.total_tokens = int(self.token_offsets[-1])
+        self.qkv = torch.zeros((3, heads, self.total_tokens, head_dim), dtype=torch.float16, device=device)
+        self._graph = None
+
+    def __call__(self, qkv: torch.Tensor | None = None) -> torch.Tensor:
+        """qkv: [3, H, total_tokens, d] half (instances stacked along tokens);
+        None runs on the internal input buffer ``self.qkv``."""
+        return self.core.run(self.qkv if qkv is None else qkv.contiguous())
+
+    def capture(self) -> "BatchedSparseAttention":
+        """Capture the launch sequence (on ``self.qkv``) in a CUDA graph."""
+        self.core.run(self.qkv)  # tunes and warms up outside the capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.core.run(self.qkv)
+        torch.cuda.current_stream().wait_stream(s)
+        self._graph = g
+        return self
+
+    def replay(self) -> torch.Tensor:
+        self._graph.replay()
+        return self.core.out
+
+    def instance_output(self, i: int) -> torch.Tensor:
+        a, b = int(self.token_offsets[i]), int(self.token_offsets[i + 1])
+        return self.core.out[:, a:b]
+
+
+class PerInstanceSparseAttention:
+    """The plain baseline: the same steps launched separately per instance."""
+
+    def __init__(self, masks: list[VectorSparse], heads: int, head_dim: int = 64, lhs_bits: int = 8,
+                 rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 32.0, device="cuda"):
+        align = 16 if rhs_bits == 8 else 32
+        self.cores = [_AttentionCore(to_device(m, align, device), heads, head_dim, lhs_bits, rhs_bits, scale_qkv,
+                                     scale_sfmx, device, tune=False) for m in masks]
+        self.seq_lens = [m.ncols for m in masks]
+
+    def __call__(self, qkvs: list[torch.Tensor]) -> list[torch.Tensor]:
+        return [c.run(x) for c, x in zip(self.cores, qkvs)]

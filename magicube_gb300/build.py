@@ -22,6 +22,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libmagicube_gb300.so"
+CLI = PKG / "cli"
+BIN = PKG / "bin"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -70,8 +72,28 @@ def _compile(src: Path, verbose: bool) -> Path:
     return obj
 
 
+def _cuda_lib() -> str:
+    return str(Path(_nvcc()).resolve().parent.parent / "lib64")
+
+
+def build_cli() -> list[Path]:
+    """The command-line benchmark programs (magicube_gb300/bin), linked
+    against the library."""
+    BIN.mkdir(exist_ok=True)
+    outs = []
+    for src in sorted(CLI.glob("*.cpp")):
+        exe = BIN / src.stem
+        if not exe.exists() or any(p.stat().st_mtime > exe.stat().st_mtime for p in [src, LIB, *INCLUDE.glob("*.h")]):
+            _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", str(INCLUDE), "-I", _cuda_include(), str(src),
+                  "-o", str(exe), "-L", str(PKG), "-lmagicube_gb300", "-L", _cuda_lib(), "-lcudart",
+                  "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath," + _cuda_lib()])
+        outs.append(exe)
+    return outs
+
+
 def build(verbose: bool = False, jobs: int | None = None) -> Path:
-    """Compile and link the library; returns the path of the shared object."""
+    """Compile and link the library and the CLI programs; returns the path of
+    the shared object."""
     BUILD.mkdir(exist_ok=True)
     srcs = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 4))
@@ -81,6 +103,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         tmp = LIB.with_suffix(".so.tmp")
         _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)])
         os.replace(tmp, LIB)
+    build_cli()
     return LIB
 
 

@@ -1,0 +1,217 @@
+"""Continuous-batching server for the sparse encoder.
+
+Requests carry a sequence of their own length and (per encoder layer) their
+own vector-sparse attention mask.  On arrival a request's tokens and masks are
+copied to the device once and stay resident until it completes.  The
+scheduler admits queued requests into a new batch whenever an in-flight slot
+is free and the free HBM covers the batch's estimated working set; a batch
+is one block-diagonal forward pass over the admitted requests (the token
+tensors concatenated, the masks stacked into one mask per layer) launched on
+its own CUDA stream, so batches that are admitted while others still run
+overlap on the device.  Completion is observed through CUDA events, and each
+request's latency is (completion - arrival).
+
+serve_sequential is the baseline: one request at a time, in arrival order,
+each its own forward pass.
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import formats, synth
+from .batched import AttentionMaskDev
+from .formats import VectorSparse
+
+
+@dataclass
+class Request:
+    rid: int
+    seq_len: int
+    arrival: float                   # seconds after the start of the run
+    x: torch.Tensor                  # [seq_len, hidden] half (host until admitted)
+    masks: list[VectorSparse]        # one per encoder layer
+    out: torch.Tensor | None = None  # [seq_len, hidden] half
+    t_admit: float = float("nan")
+    t_done: float = float("nan")
+    dev: dict = field(default_factory=dict)
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+
+def make_requests(n: int, rate: float, hidden: int = 256, layers: int = 2, V: int = 8, sparsity: float = 0.95,
+                  median: int = 2048, clip: tuple[int, int] = (256, 8192), sigma: float = 0.5,
+                  seed: int = 0) -> list[Request]:
+    """Poisson arrivals at `rate` requests/s; lengths lognormal(median) clipped,
+    rounded to a multiple of 64; uniform random column vectors at `sparsity`."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=n) if rate > 0 else np.zeros(n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    lens = np.clip(np.exp(rng.normal(np.log(median), sigma, size=n)), clip[0], clip[1])
+    lens = (np.round(lens / 64) * 64).astype(int).clip(clip[0], clip[1])
+    reqs = []
+    for i in range(n):
+        L = int(lens[i])
+        x = (torch.randn(L, hidden, generator=torch.Generator().manual_seed(seed * 100003 + i)) * 0.5).half()
+        masks = [synth.uniform_mask(L // V, L, V, sparsity, seed=seed * 1000 + i * 10 + l) for l in range(layers)]
+        reqs.append(Request(i, L, float(arrivals[i]), x, masks))
+    return reqs
+
+
+def _upload(req: Request, alignment: int, device) -> None:
+    """Copy a request's tokens and aligned masks to the device (once)."""
+    if req.dev:
+        return
+    req.dev["x"] = req.x.to(device, non_blocking=True)
+    per_layer = []
+    for m in req.masks:
+        pairs, n = formats.align_row_offsets(m, alignment)
+        cols = formats.pad_column_indices(m, pairs, n, shuffle8=False)
+        ri = formats.sorted_row_swizzle(m)
+        per_layer.append((torch.from_numpy(pairs).to(device, non_blocking=True),
+                          torch.from_numpy(cols).to(device, non_blocking=True),
+                          torch.from_numpy(ri).to(device, non_blocking=True), m.m_vec, n))
+    req.dev["masks"] = per_layer
+
+
+def batch_masks(reqs: list[Request], layers: int, V: int) -> list[AttentionMaskDev]:
+    """One block-diagonal attention mask per layer over the batch (device ops)."""
+    out = []
+    for l in range(layers):
+        pairs, cols, ri = [], [], []
+        abase = tbase = mbase = 0
+        for r in reqs:
+            p, c, i, m_vec, n = r.dev["masks"][l]
+            pairs.append(p + abase)
+            cols.append(torch.where(c >= 0, c + tbase, c))
+            ri.append(i + mbase)
+            abase += n
+            tbase += r.seq_len
+            mbase += m_vec
+        if abase == 0:
+            cols = [torch.full((1,), -1, dtype=torch.int32, device=pairs[0].device)]
+        out.append(AttentionMaskDev(mbase, V, tbase, abase, torch.cat(ri), torch.cat(pairs), torch.cat(cols)))
+    return out
+
+
+def footprint_bytes(reqs: list[Request], hidden: int, heads: int, layers: int, V: int) -> int:
+    """Device working set of one batched forward pass (activations, scores,
+    quantized operands and per-layer masks), used for admission."""
+    T = sum(r.seq_len for r in reqs)
+    nnz = max(sum(m.nnz_vec for m in r.masks) for r in reqs) * len(reqs)
+    act = T * hidden * 2 * 14             # fp16 activations, qkv, ffn intermediates (4x hidden)
+    att = nnz * V * heads * (2 + 1 + 4)   # half scores, int8 probabilities, slack
+    return int(act + att + nnz * 8)
+
+
+class ContinuousBatchingServer:
+    def __init__(self, model, hidden: int = 256, heads: int = 4, V: int = 8, rhs_bits: int = 8,
+                 max_inflight: int = 3, max_batch_tokens: int = 65536, hbm_reserve: int = 2 << 30,
+                 device="cuda"):
+        self.model, self.hidden, self.heads, self.V = model, hidden, heads, V
+        self.layers = len(model.layers)
+        self.alignment = 16 if rhs_bits == 8 else 32
+        self.max_inflight, self.max_batch_tokens, self.hbm_reserve = max_inflight, max_batch_tokens, hbm_reserve
+        self.device = torch.device(device)
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
+        self.batches: list[list[int]] = []
+
+    def _fits(self, reqs: list[Request]) -> bool:
+        free, _ = torch.cuda.mem_get_info(self.device)
+        return footprint_bytes(reqs, self.hidden, self.heads, self.layers, self.V) + self.hbm_reserve <= free
+
+    def serve(self, requests: list[Request]) -> dict:
+        pending = deque(sorted(requests, key=lambda r: r.arrival))
+        queue: deque[Request] = deque()
+        inflight: list[tuple[torch.cuda.Event, list[Request], int]] = []
+        free_streams = list(range(self.max_inflight))
+        done = 0
+        t0 = time.perf_counter()
+        with torch.no_grad():
+            while done < len(requests):
+                now = time.perf_counter() - t0
+                while pending and pending[0].arrival <= now:
+                    r = pending.popleft()
+                    queue.append(r)
+                # completions
+                still = []
+                for ev, batch, si in inflight:
+                    if ev.query():
+                        tdone = time.perf_counter() - t0
+                        for r in batch:
+                            r.t_done = tdone
+                            r.dev.clear()
+                        done += len(batch)
+                        free_streams.append(si)
+                    else:
+                        still.append((ev, batch, si))
+                inflight = still
+                # admission of a new batch: as many queued requests as the
+                # token budget and the free HBM allow (the first one always,
+                # when nothing else is on the device)
+                if queue and free_streams:
+                    batch, tokens = [], 0
+                    while queue:
+                        r = queue[0]
+                        if batch and tokens + r.seq_len > self.max_batch_tokens:
+                            break
+                        if (batch or inflight) and not self._fits(batch + [r]):
+                            break
+                        batch.append(queue.popleft())
+                        tokens += r.seq_len
+                    if batch:
+                        si = free_streams.pop()
+                        s = self.streams[si]
+                        with torch.cuda.stream(s):
+                            for r in batch:
+                                _upload(r, self.alignment, self.device)
+                                r.t_admit = time.perf_counter() - t0
+                            masks = batch_masks(batch, self.layers, self.V)
+                            x = torch.cat([r.dev["x"] for r in batch], dim=0)
+                            y = self.model(x, masks)
+                            off = 0
+                            for r in batch:
+                                r.out = y[off:off + r.seq_len]
+                                off += r.seq_len
+                            ev = torch.cuda.Event()
+                            ev.record(s)
+                        inflight.append((ev, batch, si))
+                        self.batches.append([r.rid for r in batch])
+                        continue
+                if not inflight and not queue and pending:
+                    time.sleep(max(0.0, min(0.001, pending[0].arrival - (time.perf_counter() - t0))))
+        torch.cuda.synchronize()
+        return summarize(requests, time.perf_counter() - t0)
+
+
+def serve_sequential(model, requests: list[Request], V: int = 8, rhs_bits: int = 8, device="cuda") -> dict:
+    """Baseline: one request at a time in arrival order, each its own forward pass."""
+    alignment = 16 if rhs_bits == 8 else 32
+    layers = len(model.layers)
+    t0 = time.perf_counter()
+    with torch.no_grad():
+        for r in sorted(requests, key=lambda q: q.arrival):
+            now = time.perf_counter() - t0
+            if r.arrival > now:
+                time.sleep(r.arrival - now)
+            r.t_admit = time.perf_counter() - t0
+            _upload(r, alignment, device)
+            masks = batch_masks([r], layers, V)
+            r.out = model(r.dev["x"], masks)
+            torch.cuda.synchronize()
+            r.t_done = time.perf_counter() - t0
+            r.dev.clear()
+    return summarize(requests, time.perf_counter() - t0)
+
+
+def summarize(requests: list[Request], makespan: float) -> dict:
+    lat = np.array([r.latency for r in requests]) * 1e3
+    return {"requests": len(requests), "makespan_s": makespan, "req_per_s": len(requests) / makespan,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "tokens": int(sum(r.seq_len for r in requests))}

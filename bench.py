@@ -109,6 +109,19 @@ def sddmm_workload(pa: int, pb: int, batch: int, seed: int = 42):
     return mask, hm, lhs, rhs
 
 
+def measured_traffic_per_instance() -> float | None:
+    """DRAM bytes per SDDMM instance from the committed ncu summary of the
+    headline kernel (profiles/sddmm_k64_L8R8_4096x4096x64_V8.md)."""
+    p = ROOT / "profiles" / "sddmm_k64_L8R8_4096x4096x64_V8.md"
+    try:
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_instance:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def sddmm_bytes(hm, pa: int, pb: int, batch: int) -> tuple[float, float]:
     """(algorithmic bytes per launch, ops per launch) of a batched SDDMM."""
     nnz = hm.mask.nnz_vec
@@ -308,6 +321,7 @@ def run_gpu(args) -> None:
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
 
+    tpk = tensor_peaks(dev)
     if rank == 0:
         gbs = head["gbs"]
         line = {
@@ -320,8 +334,19 @@ def run_gpu(args) -> None:
                        "instances_per_step": B, "step_bytes": head["bytes"],
                        "l2": "inputs+outputs per step exceed 2x L2 (no flush)", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": gbs / peaks["hbm_gbs"], "traffic": None,
-                         "peak_source": peaks["source"]},
+                         "frac": gbs / peaks["hbm_gbs"],
+                         "traffic": (measured_traffic_per_instance() * B
+                                     if measured_traffic_per_instance() and args.mma == 1 else None),
+                         "traffic_source": "ncu capture of 32 instances scaled to the launch (see profiles/)",
+                         "algorithmic_bytes": head["bytes"], "peak_source": peaks["source"]},
+            # The int8 contraction runs on mma.sync (sm_103a has no tcgen05
+            # integer MMA); its measured peak bounds this kernel before HBM does.
+            "tensor_roofline": {"achieved": head["tops"], "peak": tpk["int8_mma_sync" if args.mma == 1 else
+                                                                      "f16_mma_sync"],
+                                "unit": "TOP/s", "frac": head["tops"] / tpk["int8_mma_sync" if args.mma == 1 else
+                                                                            "f16_mma_sync"],
+                                "peak_source": "measured mma.sync probe (mcProbeTensorPeak)",
+                                "probe_tops": tpk},
             "e2e": e2e,
             "gpu_launches": args.steps * launches_per_step,
             "clocks": head["clocks"],
@@ -360,6 +385,23 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
     byts = B * (h.values.size + K * N + M * N * 4) + h.aligned_nnz * 4 + mask.m_vec * 12
     return {"tops": opc * world / t / 1e12, "ms": t * 1e3, "gbs": byts / t / 1e9,
             "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"], "instances_per_step": B}
+
+
+def tensor_peaks(dev) -> dict:
+    """Measured mma.sync peaks (TOP/s) of the int8, int4 and f16 paths."""
+    import torch
+
+    from magicube_gb300 import _lib
+    sink = torch.empty(4 * 256 * 8 * torch.cuda.get_device_properties(dev).multi_processor_count,
+                       dtype=torch.uint8, device=dev)
+    out = {}
+    for kind, name in ((0, "int8_mma_sync"), (1, "int4_mma_sync"), (2, "f16_mma_sync")):
+        ms, ops = ctypes.c_float(), ctypes.c_double()
+        _lib.check(_lib.lib().mcProbeTensorPeak(kind, sink.data_ptr(), sink.numel(), 2048, ctypes.byref(ms),
+                                                ctypes.byref(ops), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                   "mcProbeTensorPeak")
+        out[name] = ops.value / (ms.value * 1e-3) / 1e12
+    return out
 
 
 def run_profile_case(args) -> None:

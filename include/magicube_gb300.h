@@ -171,6 +171,16 @@ typedef struct mcSoftmaxDesc {
 } mcSoftmaxDesc;
 int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
 
+/* ---- Diagnostics ---------------------------------------------------------------
+ * mcProbeTensorPeak: times one full-grid launch of back-to-back independent
+ * mma.sync of `kind` (0: m16n8k32 s8, 1: m16n8k64 s4, 2: m16n8k16 f16 with f32
+ * accumulators) and returns its duration and operation count (2 per MAC), the
+ * measured tensor peak its kernels are compared with.  sink: device buffer of
+ * at least 4 bytes x 256 threads x 8 CTAs x SMs that receives each thread's
+ * (meaningless) accumulator sum, so the MMAs are not optimised away. */
+int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, float* ms_out,
+                      double* ops_out, cudaStream_t stream);
+
 /* ---- Host-side format conversion (host pointers) ---------------------------
  * The reference's host packer (SpMM/SpMM/spmm_benchmark.cpp:177-377,
  * SDDMM/SDDMM/sddmm_benchmark.cpp:104-127) as library routines. */

@@ -65,6 +65,8 @@ _SIGNATURES = {
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
     "mcQuantize": (_c_int, [_c_vp, _c_vp, _c_ll, _c_int, _c_float, _c_vp]),
     "mcQuantSoftmax": (_c_int, [ctypes.POINTER(McSoftmaxDesc), _c_vp]),
+    "mcProbeTensorPeak": (_c_int, [_c_int, _c_vp, _c_ll, _c_int, ctypes.POINTER(ctypes.c_float),
+                                   ctypes.POINTER(ctypes.c_double), _c_vp]),
     "mcAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp]),
     "mcPadColumnIndices": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_vp]),
     "mcPackSpmmValues": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_int, _c_vp, _c_vp]),

@@ -320,6 +320,13 @@ def run_gpu(args) -> None:
                               (args.mma, 1, "per_row_kernel")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
+    attention = serving_res = None
+    if not args.headline_only and rank == 0:
+        torch.cuda.empty_cache()
+        attention = attention_suite(args, dev)
+        torch.cuda.empty_cache()
+        if args.serving_requests > 0:
+            serving_res = serving_suite(args, dev)
 
     tpk = tensor_peaks(dev)
     if rank == 0:
@@ -351,6 +358,8 @@ def run_gpu(args) -> None:
             "gpu_launches": args.steps * launches_per_step,
             "clocks": head["clocks"],
             "variants": variants,
+            "batched_attention": attention,
+            "serving": serving_res,
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
@@ -385,6 +394,92 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
     byts = B * (h.values.size + K * N + M * N * 4) + h.aligned_nnz * 4 + mask.m_vec * 12
     return {"tops": opc * world / t / 1e12, "ms": t * 1e3, "gbs": byts / t / 1e9,
             "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"], "instances_per_step": B}
+
+
+def attention_suite(args, dev) -> dict:
+    """Batched uneven sparse attention: 64 instances x 4 heads, head dim 64,
+    sequence lengths uniform in [512, 4096] (multiples of 64), each instance's
+    mask a 256-wide band plus random V=8 column vectors at total sparsity 0.9;
+    int8 Q/K/V, int8 probabilities.  All instances and heads in one
+    graph-captured launch sequence against the plain per-instance launches."""
+    import torch
+
+    import oracle.attention as oatt
+    from magicube_gb300 import batched, synth
+    rng = np.random.default_rng(11)
+    n_inst, H, d, V = 64, 4, 64, 8
+    lens = (rng.integers(512, 4097, size=n_inst) // 64 * 64).clip(512, 4096).tolist()
+    masks = [synth.band_random_mask(L, V, 256, 0.9, seed=100 + i) for i, L in enumerate(lens)]
+    total = int(sum(lens))
+    gen = torch.Generator().manual_seed(12)
+    qkv_host = (torch.randn(3, H, total, d, generator=gen) * 0.5).half()
+    amax = float(qkv_host.abs().max())
+    sq, ss = 127.0 / amax, 127.0
+    b = batched.BatchedSparseAttention(masks, H, d, 8, 8, scale_qkv=sq, scale_sfmx=ss, device=dev, tune=True)
+    b.qkv.copy_(qkv_host.to(dev))
+    b.capture()
+    stream = torch.cuda.current_stream()
+    ms_b = time_cuda(lambda: b.replay(), args.steps, args.warmup, stream)
+    t_b = sum(ms_b) / len(ms_b)
+    p = batched.PerInstanceSparseAttention(masks, H, d, 8, 8, scale_qkv=sq, scale_sfmx=ss, device=dev)
+    qkvs = [b.qkv[:, :, int(b.token_offsets[i]):int(b.token_offsets[i + 1])].contiguous() for i in range(n_inst)]
+    ms_p = time_cuda(lambda: p(qkvs), args.steps, args.warmup, stream)
+    t_p = sum(ms_p) / len(ms_p)
+    same = all(torch.equal(b.instance_output(i), c.out) for i, c in enumerate(p.cores))
+    nnz = sum(m.nnz_vec for m in masks)
+    ops = 4.0 * nnz * V * d * H
+    # accuracy: the two shortest instances against the float64 oracle
+    errs = []
+    for i in np.argsort(lens)[:2].tolist():
+        a, z = int(b.token_offsets[i]), int(b.token_offsets[i + 1])
+        q, k, v = (qkv_host[j, :, a:z].double().numpy() for j in range(3))
+        pairs, n = formats_align(masks[i], 16)
+        mk = oatt.dense_mask(pairs[0], pairs[1], masks[i].m_vec, V, lens[i])
+        ref = oatt.sparse_attention_fp64(q, k, v, mk, d ** -0.5)
+        got = b.instance_output(i).double().cpu().numpy()
+        errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+    return {"config": "64 instances x 4 heads, d=64, L ~ U[512,4096], band 256 + random V=8, sparsity 0.9, "
+                      "int8 Q/K/V, int8 probabilities",
+            "tokens": total, "nonzero_vectors": int(nnz), "batched_ms": t_b, "per_instance_ms": t_p,
+            "batched_req_per_s": n_inst / (t_b / 1e3), "per_instance_req_per_s": n_inst / (t_p / 1e3),
+            "speedup": t_p / t_b, "batched_tops": ops / (t_b / 1e3) / 1e12,
+            "launches": {"batched": 4, "per_instance": 4 * n_inst, "batched_is_cuda_graph": True},
+            "results_identical": bool(same), "scales": {"qkv": sq, "softmax": ss},
+            "rel_error_vs_fp64_two_shortest": errs, "autotuned": {"sddmm": b.core.sddmm_cfg, "spmm": b.core.spmm_cfg}}
+
+
+def formats_align(mask, alignment):
+    from magicube_gb300 import formats
+    pairs, n = formats.align_row_offsets(mask, alignment)
+    cols = formats.pad_column_indices(mask, pairs, n, False)
+    return (pairs, cols), n
+
+
+def serving_suite(args, dev) -> dict:
+    """Continuous batching of a 2-layer sparse encoder (hidden 256, 4 x 64
+    heads, FFN 1024, random-init weights), int8 vector-sparse attention at
+    sparsity 0.95; Poisson arrivals at each rate of `--serving-rates`, lengths
+    lognormal (median 2048, clipped to [256, 8192]); against serving the same
+    requests one at a time."""
+    import torch
+
+    from magicube_gb300 import model, serving
+    torch.manual_seed(0)
+    enc = model.SparseEncoder(2, 256, 4, 1024).to(dev).half().eval()
+    warm = serving.make_requests(4, 0.0, seed=99)
+    serving.ContinuousBatchingServer(enc, device=dev).serve(warm)
+    serving.serve_sequential(enc, serving.make_requests(2, 0.0, seed=98), device=dev)
+    out = []
+    for rate in args.serving_rates:
+        reqs = serving.make_requests(args.serving_requests, rate, seed=5)
+        srv = serving.ContinuousBatchingServer(enc, max_inflight=3, device=dev)
+        cb = srv.serve(reqs)
+        seq = serving.serve_sequential(enc, serving.make_requests(args.serving_requests, rate, seed=5), device=dev)
+        out.append({"arrival_rate": rate, "continuous": cb, "sequential": seq,
+                    "mean_batch": float(np.mean([len(b) for b in srv.batches])),
+                    "req_per_s_ratio": cb["req_per_s"] / seq["req_per_s"]})
+    return {"config": "2-layer sparse encoder, hidden 256, 4x64 heads, FFN 1024, sparsity 0.95, "
+                      "lengths lognormal(median 2048) in [256, 8192]", "runs": out}
 
 
 def tensor_peaks(dev) -> dict:
@@ -447,6 +542,9 @@ def main() -> None:
     ap.add_argument("--profile", choices=["sddmm", "spmm"], default=None,
                     help="run only a small case of one kernel (for ncu captures)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")
+    ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")], default=[200.0, 2000.0],
+                    help="Poisson arrival rates (requests/s) of the serving runs")
+    ap.add_argument("--serving-requests", type=int, default=48, help="requests per serving run (0 skips it)")
     ap.add_argument("--mma", choices=["int8", "f16"], default="int8",
                     help="tensor path (both are bit-exact; see include/magicube_gb300.h)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

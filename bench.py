@@ -426,10 +426,29 @@ def attention_suite(args, dev) -> dict:
     ms_p = time_cuda(lambda: p(qkvs), args.steps, args.warmup, stream)
     t_p = sum(ms_p) / len(ms_p)
     same = all(torch.equal(b.instance_output(i), c.out) for i, c in enumerate(p.cores))
+    ref_out = b.core.out.clone()
+    del p, qkvs
+    torch.cuda.empty_cache()
+    # the fused kernel: quantize + one launch for everything, fixed and row-max requantization
+    fused = {}
+    for mode in ("fixed", "rowmax"):
+        f = batched.BatchedSparseAttention(masks, H, d, 8, 8, scale_qkv=sq, scale_sfmx=ss, device=dev, fused=True,
+                                           requant=mode)
+        f.qkv.copy_(b.qkv)
+        f.capture()
+        ms_f = time_cuda(lambda: f.replay(), args.steps, args.warmup, stream)
+        t_f = sum(ms_f) / len(ms_f)
+        fused[mode] = {"ms": t_f, "req_per_s": n_inst / (t_f / 1e3), "speedup_vs_per_instance": t_p / t_f,
+                       "launches": 2, "status": int(f.core.status.item())}
+        if mode == "fixed":
+            fused[mode]["identical_to_separate_steps"] = bool(torch.equal(f.core.out, ref_out))
+        else:
+            fused_rowmax = f
+        del f
     nnz = sum(m.nnz_vec for m in masks)
     ops = 4.0 * nnz * V * d * H
     # accuracy: the two shortest instances against the float64 oracle
-    errs = []
+    errs, errs_rowmax = [], []
     for i in np.argsort(lens)[:2].tolist():
         a, z = int(b.token_offsets[i]), int(b.token_offsets[i + 1])
         q, k, v = (qkv_host[j, :, a:z].double().numpy() for j in range(3))
@@ -438,6 +457,8 @@ def attention_suite(args, dev) -> dict:
         ref = oatt.sparse_attention_fp64(q, k, v, mk, d ** -0.5)
         got = b.instance_output(i).double().cpu().numpy()
         errs.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
+        got = fused_rowmax.instance_output(i).double().cpu().numpy()
+        errs_rowmax.append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
     return {"config": "64 instances x 4 heads, d=64, L ~ U[512,4096], band 256 + random V=8, sparsity 0.9, "
                       "int8 Q/K/V, int8 probabilities",
             "tokens": total, "nonzero_vectors": int(nnz), "batched_ms": t_b, "per_instance_ms": t_p,
@@ -445,7 +466,9 @@ def attention_suite(args, dev) -> dict:
             "speedup": t_p / t_b, "batched_tops": ops / (t_b / 1e3) / 1e12,
             "launches": {"batched": 4, "per_instance": 4 * n_inst, "batched_is_cuda_graph": True},
             "results_identical": bool(same), "scales": {"qkv": sq, "softmax": ss},
-            "rel_error_vs_fp64_two_shortest": errs, "autotuned": {"sddmm": b.core.sddmm_cfg, "spmm": b.core.spmm_cfg}}
+            "fused": fused,
+            "rel_error_vs_fp64_two_shortest": {"fixed_scale": errs, "rowmax_requant": errs_rowmax},
+            "autotuned": {"sddmm": b.core.sddmm_cfg, "spmm": b.core.spmm_cfg}}
 
 
 def formats_align(mask, alignment):
@@ -507,6 +530,19 @@ def run_profile_case(args) -> None:
 
     from magicube_gb300 import formats, ops, synth
     dev = torch.device("cuda:0")
+    if args.profile == "attention":
+        from magicube_gb300 import batched, synth
+        rng = np.random.default_rng(11)
+        lens = (rng.integers(512, 4097, size=args.batch) // 64 * 64).clip(512, 4096).tolist()
+        masks = [synth.band_random_mask(L, VEC, 256, 0.9, seed=100 + i) for i, L in enumerate(lens)]
+        f = batched.BatchedSparseAttention(masks, 4, 64, 8, 8, scale_qkv=40.0, scale_sfmx=127.0, device=dev,
+                                           fused=True, requant=args.requant)
+        f.qkv.copy_((torch.randn(f.qkv.shape, generator=torch.Generator().manual_seed(12)) * 0.5).half())
+        for _ in range(args.reps):
+            f()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "attention", "instances": args.batch, "reps": args.reps}))
+        return
     if args.profile == "sddmm":
         mask, hm, lhs_h, rhs_h = sddmm_workload(8, 8, args.batch)
         dm = ops.DeviceSddmmMask.from_host(hm, dev)
@@ -539,7 +575,9 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=64, help="instances per step")
     ap.add_argument("--impl", choices=["magicube_gb300", "reference"], default="magicube_gb300")
     ap.add_argument("--headline-only", action="store_true")
-    ap.add_argument("--profile", choices=["sddmm", "spmm"], default=None,
+    ap.add_argument("--requant", choices=["fixed", "rowmax"], default="rowmax",
+                    help="requantization of the --profile attention case")
+    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention"], default=None,
                     help="run only a small case of one kernel (for ncu captures)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")
     ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")], default=[200.0, 2000.0],

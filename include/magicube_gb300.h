@@ -181,6 +181,38 @@ int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
 int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, float* ms_out,
                       double* ops_out, cudaStream_t stream);
 
+/* mcSparseAttention: the quantized sparse attention of every vector-row and
+ * head in one persistent kernel (SDDMM, softmax + requantization, SpMM with
+ * scores and probabilities kept on chip).  q, k, v: int8 [heads][tokens][64]
+ * (mcQuantize output), out: half [heads][tokens][64]; the mask in the
+ * attention layout (rows aligned to 16, columns unshuffled).
+ *   scores  s = half(acc / score_scale) * scaling           (as mcSddmm + softmax)
+ *   MC_REQUANT_FIXED:  q = trunc(clamp(exp(s - max) / sum * prob_scale)),
+ *                      out = half(acc / out_scale) -- bit-identical to
+ *                      mcSddmm + mcQuantSoftmax + mcSpmm with the same scales;
+ *   MC_REQUANT_ROWMAX: q = round(127 * exp(s - max)),
+ *                      out = half(acc / (127 * sum * out_scale)).
+ * max_row_nnz must be at least every row's nonzero count (at most 4096); a
+ * longer row is skipped and *status (if given) set to 1. */
+enum { MC_REQUANT_FIXED = 0, MC_REQUANT_ROWMAX = 1 };
+typedef struct mcAttnDesc {
+    int m_vec, vec_length, heads, head_dim, max_row_nnz;
+    int lhs_bits, rhs_bits;     /* probabilities, Q/K/V: 8, 8 */
+    int requant;
+    float score_scale, scaling, prob_scale, out_scale;
+    const int* row_indices;
+    const int* row_offsets;
+    const int* column_indices;
+    const void* q;
+    const void* k;
+    const void* v;
+    long long head_stride;      /* bytes between heads of q, k, v */
+    void* out;
+    long long out_head_stride;  /* halves between heads of out */
+    int* status;                /* optional device int */
+} mcAttnDesc;
+int mcSparseAttention(const mcAttnDesc* desc, cudaStream_t stream);
+
 /* ---- Host-side format conversion (host pointers) ---------------------------
  * The reference's host packer (SpMM/SpMM/spmm_benchmark.cpp:177-377,
  * SDDMM/SDDMM/sddmm_benchmark.cpp:104-127) as library routines. */

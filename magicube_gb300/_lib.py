@@ -51,6 +51,18 @@ class McSoftmaxDesc(ctypes.Structure):
     ]
 
 
+class McAttnDesc(ctypes.Structure):
+    _fields_ = [
+        ("m_vec", _c_int), ("vec_length", _c_int), ("heads", _c_int), ("head_dim", _c_int),
+        ("max_row_nnz", _c_int), ("lhs_bits", _c_int), ("rhs_bits", _c_int), ("requant", _c_int),
+        ("score_scale", _c_float), ("scaling", _c_float), ("prob_scale", _c_float), ("out_scale", _c_float),
+        ("row_indices", _c_vp), ("row_offsets", _c_vp), ("column_indices", _c_vp),
+        ("q", _c_vp), ("k", _c_vp), ("v", _c_vp), ("head_stride", _c_ll),
+        ("out", _c_vp), ("out_head_stride", _c_ll), ("status", _c_vp),
+    ]
+
+
+REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
 MMA_DEFAULT, MMA_INT8, MMA_F16 = 0, 1, 2
 KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM = 0, 1, 2
 VALUES_PACKED, VALUES_SOFTMAX = 0, 1
@@ -65,6 +77,7 @@ _SIGNATURES = {
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
     "mcQuantize": (_c_int, [_c_vp, _c_vp, _c_ll, _c_int, _c_float, _c_vp]),
     "mcQuantSoftmax": (_c_int, [ctypes.POINTER(McSoftmaxDesc), _c_vp]),
+    "mcSparseAttention": (_c_int, [ctypes.POINTER(McAttnDesc), _c_vp]),
     "mcProbeTensorPeak": (_c_int, [_c_int, _c_vp, _c_ll, _c_int, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_double), _c_vp]),
     "mcAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp]),

@@ -11,6 +11,10 @@ can be captured in a CUDA graph and replayed.  Each instance's result is the
 same, bit for bit, as when it runs alone (the per-row arithmetic does not
 depend on the other rows).
 
+With ``fused=True`` the attention of every instance and head is instead one
+launch of the fused kernel (mcSparseAttention) after one quantization launch;
+scores and probabilities then never reach device memory.
+
 PerInstanceSparseAttention runs the same computation with separate launches
 per instance (the plain baseline).
 """
@@ -35,6 +39,7 @@ class AttentionMaskDev:
     row_indices: torch.Tensor
     row_offsets: torch.Tensor
     col_indices: torch.Tensor
+    max_row_nnz: int = 0
 
 
 def block_diagonal(masks: list[VectorSparse]) -> tuple[VectorSparse, np.ndarray]:
@@ -66,15 +71,27 @@ def to_device(mask: VectorSparse, alignment: int, device) -> AttentionMaskDev:
     cols = formats.pad_column_indices(mask, pairs, n, shuffle8=False)
     ri = formats.sorted_row_swizzle(mask)
     t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)  # noqa: E731
+    lens = mask.row_lengths()
     return AttentionMaskDev(mask.m_vec, mask.vec_length, mask.ncols, n, t(ri), t(pairs),
-                            t(cols if cols.size else np.full(1, -1, np.int32)))
+                            t(cols if cols.size else np.full(1, -1, np.int32)), int(lens.max()) if lens.size else 0)
 
 
 class _AttentionCore:
-    """quantize -> SDDMM -> quantized softmax -> SpMM on one mask (heads batched)."""
+    """quantize -> SDDMM -> quantized softmax -> SpMM on one mask (heads
+    batched), or quantize -> the fused attention kernel (`fused`; requant
+    "fixed" reproduces the separate steps bit for bit, "rowmax" requantizes the
+    probabilities relative to each row's maximum)."""
 
     def __init__(self, mask: AttentionMaskDev, heads: int, head_dim: int, lhs_bits: int, rhs_bits: int,
-                 scale_qkv: float, scale_sfmx: float, device, tune: bool):
+                 scale_qkv: float, scale_sfmx: float, device, tune: bool, fused: bool = False,
+                 requant: str = "fixed"):
+        self.fused = fused
+        self.requant = _lib.REQUANT_ROWMAX if requant == "rowmax" else _lib.REQUANT_FIXED
+        if fused and (lhs_bits, rhs_bits, head_dim) != (8, 8, 64):
+            raise ValueError("the fused attention kernel computes L8-R8 with head_dim 64")
+        if not fused and requant != "fixed":
+            raise ValueError("row-max requantization needs the fused kernel")
+        self.status = torch.zeros(1, dtype=torch.int32, device=device)
         if head_dim % 64:
             raise ValueError("head_dim must be a multiple of 64")
         self.m, self.H, self.d = mask, heads, head_dim
@@ -84,8 +101,11 @@ class _AttentionCore:
         L, V = mask.seq_len, mask.vec_length
         self.q_words = L * head_dim * rhs_bits // 32
         self.qkv_q = torch.empty((3, heads, self.q_words), dtype=torch.int32, device=device)
-        self.scores = torch.empty((heads, mask.aligned_nnz * V), dtype=torch.float16, device=device)
-        self.probs = torch.zeros((heads, mask.aligned_nnz * V * lhs_bits // 32), dtype=torch.int32, device=device)
+        # scores and probabilities only exist in memory on the unfused path
+        self.scores = None if fused else torch.empty((heads, mask.aligned_nnz * V), dtype=torch.float16,
+                                                     device=device)
+        self.probs = None if fused else torch.zeros((heads, mask.aligned_nnz * V * lhs_bits // 32),
+                                                    dtype=torch.int32, device=device)
         self.out = torch.empty((heads, L, head_dim), dtype=torch.float16, device=device)
         self.sddmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO, "row_split": 0}
         self.spmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO}
@@ -143,12 +163,30 @@ class _AttentionCore:
         sig = autotune.signature("spmm_attn", self.lb, self.rb, m.vec_length, self.d, m.m_vec, avg, self.H)
         self.spmm_cfg = autotune.tune(sig, autotune.spmm_candidates(), lambda c: self._spmm(c, stream))
 
+    def _fused(self, stream) -> None:
+        m = self.m
+        d = _lib.McAttnDesc(
+            m_vec=m.m_vec, vec_length=m.vec_length, heads=self.H, head_dim=self.d, max_row_nnz=m.max_row_nnz,
+            lhs_bits=self.lb, rhs_bits=self.rb, requant=self.requant, score_scale=float(self.scale_qkv ** 2),
+            scaling=float(self.scaling), prob_scale=float(self.scale_sfmx),
+            out_scale=float(self.scale_qkv if self.requant == _lib.REQUANT_ROWMAX
+                            else self.scale_qkv * self.scale_sfmx),
+            row_indices=m.row_indices.data_ptr(), row_offsets=m.row_offsets.data_ptr(),
+            column_indices=m.col_indices.data_ptr(), q=self.qkv_q[0].data_ptr(), k=self.qkv_q[1].data_ptr(),
+            v=self.qkv_q[2].data_ptr(), head_stride=self.q_words * 4, out=self.out.data_ptr(),
+            out_head_stride=m.seq_len * self.d, status=self.status.data_ptr())
+        _lib.check(_lib.lib().mcSparseAttention(ctypes.byref(d), stream), "mcSparseAttention")
+
     def run(self, qkv: torch.Tensor) -> torch.Tensor:
         """qkv: [3, H, L, d] half (contiguous) -> [H, L, d] half."""
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        if self.fused:
+            self._quantize(qkv, stream)
+            self._fused(stream)
+            return self.out
         if self._tune:
             self.tune(qkv)
             self._tune = False
-        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         self._quantize(qkv, stream)
         self._sddmm(self.sddmm_cfg, stream)
         self._softmax(stream)
@@ -162,12 +200,12 @@ class BatchedSparseAttention:
 
     def __init__(self, masks: list[VectorSparse], heads: int, head_dim: int = 64, lhs_bits: int = 8,
                  rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 32.0, device="cuda",
-                 tune: bool = True):
+                 tune: bool = True, fused: bool = False, requant: str = "fixed"):
         mega, self.token_offsets = block_diagonal(masks)
         align = 16 if rhs_bits == 8 else 32
         self.mask = to_device(mega, align, device)
         self.core = _AttentionCore(self.mask, heads, head_dim, lhs_bits, rhs_bits, scale_qkv, scale_sfmx, device,
-                                   tune)
+                                   tune, fused=fused, requant=requant)
         self.seq_lens = [m.ncols for m in masks]
         self.total_tokens = int(self.token_offsets[-1])
         self.qkv = torch.zeros((3, heads, self.total_tokens, head_dim), dtype=torch.float16, device=device)

@@ -1,0 +1,350 @@
+// attn_fused.cu -- the quantized sparse attention in one persistent kernel.
+//
+// One work item = one vector-row (V query rows sharing a column pattern) of
+// one head.  A CTA of 4 warps runs, per item, with everything in shared
+// memory between the steps:
+//   1. SDDMM: scores of the row's nonzero vectors, 16 per warp tile
+//      (mma.m16n8k32 s8, K rows gathered with 128-bit loads straight into the
+//      A fragment, Q rows in registers), dequantised exactly as the separate
+//      SDDMM does (half(acc / scale_qkv^2)) and multiplied by the softmax
+//      scaling, kept as f32 [v][slot] (MC_REQUANT_ROWMAX scales the int32
+//      accumulator straight to f32 instead, skipping the half rounding);
+//   2. softmax per vector lane: max, sum of exp, requantization to int8
+//      [v][slot] -- warp w owns lanes 2w, 2w+1 and visits slots in the same
+//      per-thread order and reduction tree as the separate softmax kernel,
+//      so with MC_REQUANT_FIXED every probability equals its output bit for
+//      bit; MC_REQUANT_ROWMAX instead stores q = round(127 exp(s - max)) and
+//      dequantises the output by 127 * sum * scale_qkv per lane (probabilities
+//      keep 7 bits relative to the row maximum instead of an absolute scale);
+//   3. SpMM: P (int8, from shared memory) times the gathered V rows, split
+//      over the slots: warp w takes 32-slot steps w, w+4, ..., stages their V
+//      rows through its own 2-deep cp.async ring, transposes them with
+//      ldmatrix.m16n16.x2.trans.b8 and multiplies all 64 output columns; the
+//      four warps' int32 partial sums are added through shared memory.
+// Scores and probabilities never leave the SM: per item the kernel reads the
+// Q rows, the gathered K and V rows (L2-resident per head) and writes V x 64
+// half outputs.  Heads vary fastest between consecutive items.  Needs
+// head_dim == 64 and rows of at most 4096 nonzero vectors (shared memory).
+#include <cfloat>
+#include <cstdint>
+
+#include "mc_host.h"
+#include "mc_ptx.cuh"
+
+namespace mc {
+
+struct AttnParams {
+    int m_vec, heads, items, nnzp;
+    const int* row_indices;
+    const int* row_offsets;
+    const int* col_indices;
+    const uint8_t* q;
+    const uint8_t* k;
+    const uint8_t* v;
+    long long head_stride;      // bytes between heads of q, k, v
+    __half* out;
+    long long out_head_stride;  // halves between heads of out
+    float score_scale;          // scores = half(acc / score_scale)
+    float scaling;              // softmax input scaling
+    float prob_scale;           // fixed requantization scale
+    float out_scale;            // output divisor (fixed) or its per-lane factor (row-max)
+    int* status;                // optional: set to 1 when a row exceeds nnzp
+};
+
+__device__ __forceinline__ void ldsm_x2_trans_b8_a(uint32_t (&r)[4], const void* p)
+{
+    asm volatile("ldmatrix.sync.aligned.m16n16.x2.trans.shared.b8 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_u32(p)));
+}
+
+template <int V, bool ROWMAX>
+__global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams p)
+{
+    constexpr int STAGES = 2;   // per-warp V-row ring depth
+    constexpr int ROW = 64;     // bytes of one int8 row of d = 64
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int SP = p.nnzp + 4;    // f32 score row stride (bank offset 4 words per lane)
+    const int PP = p.nnzp + 16;   // int8 probability row stride
+    // S (scores) and, after the softmax, the cross-warp reduction buffer
+    float* S = reinterpret_cast<float*>(smem);
+    int* RED = reinterpret_cast<int*>(smem);
+    const size_t s_bytes = ((size_t)V * SP * 4 > 8192 ? (size_t)V * SP * 4 : 8192);
+    uint8_t* P = smem + s_bytes;
+    int* C = reinterpret_cast<int*>(P + (size_t)V * PP);
+    float* DEN = reinterpret_cast<float*>(C + p.nnzp);
+    float* MAXW = DEN + 8;  // [4 warps][8 lanes] partial row maxima of the scores
+    uint8_t* rings = reinterpret_cast<uint8_t*>(
+        (reinterpret_cast<uintptr_t>(MAXW + 32) + 127) & ~static_cast<uintptr_t>(127));
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int g = lane >> 2, t = lane & 3;
+    uint8_t* ring = rings + warp * STAGES * 32 * ROW;  // this warp's private V-row ring
+
+#pragma unroll 1
+    for (int item = blockIdx.x; item < p.items; item += gridDim.x) {
+        const int h = item % p.heads;
+        const int row = __ldg(p.row_indices + item / p.heads);
+        const int start = __ldg(p.row_offsets + 2 * row);
+        const int nnz = __ldg(p.row_offsets + 2 * row + 1) - start;
+        if (nnz > p.nnzp) {  // the caller's max_row_nnz is too small: leave the row, report it
+            if (tid == 0 && p.status) atomicExch(p.status, 1);
+            continue;
+        }
+        const uint8_t* qh = p.q + (long long)h * p.head_stride;
+        const uint8_t* kh = p.k + (long long)h * p.head_stride;
+        const uint8_t* vh = p.v + (long long)h * p.head_stride;
+
+        __syncthreads();  // the previous item is done with S/RED, C, P, DEN and MAXW
+        for (int j = tid; j < nnz; j += 128) C[j] = __ldg(p.col_indices + start + j);
+        int4 qf = make_int4(0, 0, 0, 0);
+        if (g < V) qf = ldg_nc_v4(qh + (long long)(row * V + g) * ROW + 16 * t);
+        __syncthreads();
+
+        // The V rows of this warp's first two SpMM steps are requested now and
+        // land while the scores and the softmax are computed.
+        const int nround = (nnz + 31) & ~31;
+        const int steps = nround >> 5;
+        auto issue = [&](int s, int slot) {
+            if (s < steps) {
+                const int j = s * 32 + lane;
+                if (j < nnz) {
+                    const uint8_t* src = vh + (long long)C[j] * ROW;
+                    uint8_t* dst = ring + slot * 32 * ROW + lane * ROW;
+                    const int sw = (lane >> 1) & 3;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) cp_async16(dst + ((c ^ sw) << 4), src + c * 16);
+                }
+            }
+            cp_async_commit();
+        };
+        issue(warp, 0);
+        issue(warp + 4, 1);
+
+        // ---- 1. scores: warp w takes tiles w, w+4, ...; two tiles in flight ----
+        const int ntiles = (nnz + 15) >> 4;
+        const float sfac = p.scaling / p.score_scale;  // row-max mode: no half rounding
+        float mxl[2] = {-FLT_MAX, -FLT_MAX};           // running max of lanes 2t, 2t+1
+        auto store_scores = [&](int tile, const int (&acc)[4]) {
+            if (2 * t >= V) return;
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const int j = tile * 16 + g + 8 * hh;
+                if (j >= nnz) continue;
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int a = acc[2 * hh + e];
+                    const float x = ROWMAX ? __int2float_rn(a) * sfac
+                                           : __half2float(deq_half(a, p.score_scale)) * p.scaling;
+                    S[(2 * t + e) * SP + j] = x;
+                    mxl[e] = fmaxf(mxl[e], x);
+                }
+            }
+        };
+#pragma unroll 1
+        for (int tile = warp; tile < ntiles; tile += 8) {
+            int4 r[2][2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int j0 = (tile + 4 * u) * 16 + g, j1 = j0 + 8;
+                r[u][0] = j0 < nnz ? ldg_nc_v4(kh + (long long)C[j0] * ROW + 16 * t) : make_int4(0, 0, 0, 0);
+                r[u][1] = j1 < nnz ? ldg_nc_v4(kh + (long long)C[j1] * ROW + 16 * t) : make_int4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (tile + 4 * u >= ntiles) break;
+                int acc[4] = {0, 0, 0, 0};
+                mma_k32<true, true>(acc, r[u][0].x, r[u][1].x, r[u][0].y, r[u][1].y, qf.x, qf.y);
+                mma_k32<true, true>(acc, r[u][0].z, r[u][1].z, r[u][0].w, r[u][1].w, qf.z, qf.w);
+                store_scores(tile + 4 * u, acc);
+            }
+        }
+        // lanes with the same t hold the same vector lanes: reduce over g
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+#pragma unroll
+            for (int o = 4; o < 32; o <<= 1) mxl[e] = fmaxf(mxl[e], __shfl_xor_sync(0xffffffffu, mxl[e], o));
+        }
+        if (g == 0 && 2 * t < V) {
+            MAXW[warp * 8 + 2 * t] = mxl[0];
+            MAXW[warp * 8 + 2 * t + 1] = mxl[1];
+        }
+        __syncthreads();
+
+        // ---- 2. softmax + requantization (warp w: lanes 2w, 2w+1) ------------
+        // The maximum is exact in any order; the sum keeps the per-thread order
+        // and reduction tree of the separate softmax kernel.
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int v = 2 * warp + e;
+            if (v >= V) break;
+            float* sv = S + v * SP;
+            const float mx = fmaxf(fmaxf(MAXW[v], MAXW[8 + v]), fmaxf(MAXW[16 + v], MAXW[24 + v]));
+            uint8_t* pv = P + v * PP;
+            float sum = 0.f;
+            if constexpr (ROWMAX) {
+                for (int j = lane; j < nround; j += 32) {
+                    int qv = 0;
+                    if (j < nnz) {
+                        const float ex = __expf(sv[j] - mx);
+                        sum += ex;
+                        qv = __float2int_rn(127.f * ex);
+                    }
+                    pv[j] = (uint8_t)qv;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            } else {
+                for (int j = lane; j < nnz; j += 32) {
+                    const float ex = __expf(sv[j] - mx);
+                    sum += ex;
+                    sv[j] = ex;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                for (int j = lane; j < nround; j += 32) {
+                    int qv = 0;
+                    if (j < nnz) {
+                        float f = sv[j] / sum * p.prob_scale;
+                        f = fminf(fmaxf(f, -128.f), 127.f);
+                        qv = (int)f;
+                    }
+                    pv[j] = (uint8_t)qv;
+                }
+            }
+            if (lane == 0) DEN[v] = ROWMAX ? 127.f * sum * p.out_scale : p.out_scale;
+        }
+        __syncthreads();
+
+        // ---- 3. out = P x V rows: warp w takes steps w, w+4, ... (k-split) ------
+        // Each lane stages one gathered V row (four 16-byte copies) of the step
+        // into the warp's private ring; the warp then multiplies all 64 output
+        // columns (four MMAs sharing the P fragment).  No CTA barrier inside.
+        int acc[4][4] = {};
+        int slot = 0;
+#pragma unroll 1
+        for (int s = warp; s < steps; s += 4) {
+            // step s sits in `slot` (requested two steps earlier, or at item start)
+            cp_async_wait<1>();
+            __syncwarp();
+            const uint8_t* st = ring + slot * 32 * ROW;
+            uint32_t b0 = 0, b1 = 0;
+            if (g < V) {
+                b0 = lds32(P + g * PP + s * 32 + 4 * t);
+                b1 = lds32(P + g * PP + s * 32 + 16 + 4 * t);
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) {
+                uint32_t a[4];
+                ldsm_x2_trans_b8_a(a, st + lane * ROW + ((m ^ ((lane >> 1) & 3)) << 4));
+                mma_k32<true, true>(acc[m], a[0], a[1], a[2], a[3], b0, b1);
+            }
+            __syncwarp();  // every lane is done with this slot before it is refilled
+            issue(s + 8, slot);
+            slot ^= 1;
+        }
+        cp_async_wait<0>();
+        // cross-warp sum of the partial products (exact integer adds)
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) RED[(warp * 16 + m * 4 + e) * 32 + lane] = acc[m][e];
+        __syncthreads();
+        int tot[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            uint32_t x = 0;
+#pragma unroll
+            for (int w = 0; w < 4; ++w) x += (uint32_t)RED[(w * 16 + warp * 4 + e) * 32 + lane];
+            tot[e] = (int)x;
+        }
+        // tot: column n = 16 warp + g (+8 for tot[2], tot[3]), lane v = 2t (+1 for odd)
+        if (2 * t < V) {
+            __half* o = p.out + (long long)h * p.out_head_stride + (long long)(row * V + 2 * t) * 64 + 16 * warp + g;
+            const float d0 = DEN[2 * t], d1 = DEN[2 * t + 1];
+            o[0] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[0]), d0));
+            o[64] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[1]), d1));
+            o[8] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[2]), d0));
+            o[72] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[3]), d1));
+        }
+    }
+}
+
+inline size_t attn_smem_bytes(int V, int nnzp)
+{
+    size_t sb = (size_t)V * (nnzp + 4) * 4;
+    if (sb < 8192) sb = 8192;  // doubles as the 4 x 16 x 32-int reduction buffer
+    const size_t s = sb + (size_t)V * (nnzp + 16) + (size_t)nnzp * 4 + 8 * 4 + 32 * 4;
+    return (s + 127) / 128 * 128 + 128 + 4 * 2 * 32 * 64;  // + four private 2-stage rings
+}
+
+template <int V, bool ROWMAX>
+int attention_launch(const AttnParams& p, size_t smem, cudaStream_t s)
+{
+    auto kern = sparse_attention_kernel<V, ROWMAX>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return (int)cudaGetLastError();
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long grid = (long long)per_sm * sms;
+    if (grid > p.items) grid = p.items;
+    kern<<<(unsigned)(grid < 1 ? 1 : grid), 128, smem, s>>>(p);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace mc
+
+extern "C" int mcSparseAttention(const mcAttnDesc* d, cudaStream_t stream)
+{
+    mc::clear_error();
+    if (!d) return mc::fail(1, "mcSparseAttention: null descriptor");
+    if (!(d->vec_length == 2 || d->vec_length == 4 || d->vec_length == 8))
+        return mc::fail(1, "mcSparseAttention: vec_length must be 2, 4 or 8");
+    if (d->head_dim != 64) return mc::fail(1, "mcSparseAttention: head_dim must be 64");
+    if (d->lhs_bits != 8 || d->rhs_bits != 8)
+        return mc::fail(1, "mcSparseAttention: the fused kernel computes L8-R8 (int8 probabilities, int8 Q/K/V)");
+    if (d->requant != MC_REQUANT_FIXED && d->requant != MC_REQUANT_ROWMAX)
+        return mc::fail(1, "mcSparseAttention: invalid requant mode");
+    if (d->m_vec < 0 || d->heads < 1 || d->max_row_nnz < 0 || d->max_row_nnz > 4096)
+        return mc::fail(1, "mcSparseAttention: bad m_vec / heads / max_row_nnz (at most 4096 nonzero vectors per row)");
+    if ((long long)d->m_vec * d->heads > 0x7fffffffLL) return mc::fail(1, "mcSparseAttention: too many items");
+    if (d->m_vec == 0) return 0;
+    if (!d->row_indices || !d->row_offsets || !d->column_indices || !d->q || !d->k || !d->v || !d->out)
+        return mc::fail(1, "mcSparseAttention: null pointer");
+    auto al = [](const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; };
+    if (!al(d->q) || !al(d->k) || !al(d->v) || d->head_stride % 16 || !al(d->out) || d->out_head_stride % 8)
+        return mc::fail(1, "mcSparseAttention: q, k, v, out must be 16-byte aligned with 16-byte strides");
+    mc::AttnParams p;
+    p.m_vec = d->m_vec;
+    p.heads = d->heads;
+    p.items = d->m_vec * d->heads;
+    p.nnzp = (d->max_row_nnz + 31) & ~31;
+    if (p.nnzp == 0) p.nnzp = 32;
+    p.row_indices = d->row_indices;
+    p.row_offsets = d->row_offsets;
+    p.col_indices = d->column_indices;
+    p.q = static_cast<const uint8_t*>(d->q);
+    p.k = static_cast<const uint8_t*>(d->k);
+    p.v = static_cast<const uint8_t*>(d->v);
+    p.head_stride = d->head_stride;
+    p.out = static_cast<__half*>(d->out);
+    p.out_head_stride = d->out_head_stride;
+    p.score_scale = d->score_scale;
+    p.scaling = d->scaling;
+    p.prob_scale = d->prob_scale;
+    p.out_scale = d->out_scale;
+    p.status = d->status;
+    if (!(p.score_scale != 0.f) || !(p.out_scale != 0.f))
+        return mc::fail(1, "mcSparseAttention: score_scale and out_scale must be nonzero");
+    const size_t smem = mc::attn_smem_bytes(d->vec_length, p.nnzp);
+    const bool rowmax = d->requant == MC_REQUANT_ROWMAX;
+    switch (d->vec_length) {
+        case 2: return rowmax ? mc::attention_launch<2, true>(p, smem, stream) : mc::attention_launch<2, false>(p, smem, stream);
+        case 4: return rowmax ? mc::attention_launch<4, true>(p, smem, stream) : mc::attention_launch<4, false>(p, smem, stream);
+        default: return rowmax ? mc::attention_launch<8, true>(p, smem, stream) : mc::attention_launch<8, false>(p, smem, stream);
+    }
+}

@@ -69,3 +69,61 @@ def test_server_results_same_alone_and_mixed(cuda):
         ref = a.out.float().cpu()
         assert torch.isfinite(ref).all()
         assert (m - ref).abs().max() <= 2e-2 * ref.abs().max()
+
+
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_fused_fixed_equals_separate_steps(cuda, V):
+    """The fused kernel with fixed requantization reproduces the separate
+    SDDMM -> softmax -> SpMM launches bit for bit."""
+    lens = [64, 512, 128, 1024, 192]
+    masks = [synth.band_random_mask(L, V, 64, 0.8, seed=30 + i) for i, L in enumerate(lens)]
+    H, d = 2, 64
+    qkv = (torch.randn(3, H, sum(lens), d, generator=torch.Generator().manual_seed(3)) * 0.5).half().to(cuda)
+    sep = batched.BatchedSparseAttention(masks, H, d, scale_qkv=60.0, scale_sfmx=100.0, device=cuda, tune=False)
+    fus = batched.BatchedSparseAttention(masks, H, d, scale_qkv=60.0, scale_sfmx=100.0, device=cuda, fused=True)
+    a = sep(qkv).clone()
+    b = fus(qkv).clone()
+    torch.cuda.synchronize()
+    assert int(fus.core.status.item()) == 0
+    assert torch.equal(a, b)
+
+
+def test_fused_rowmax_error_vs_fp64(cuda):
+    """Row-max requantization keeps 7 bits relative to each row's largest
+    probability: the output error against the float64 unquantized attention
+    is far below the fixed-scale scheme's."""
+    import oracle.attention as oatt
+    from magicube_gb300 import formats
+    lens = [256, 512]
+    masks = [synth.band_random_mask(L, 8, 128, 0.8, seed=40 + i) for i, L in enumerate(lens)]
+    H, d = 2, 64
+    qkv_h = (torch.randn(3, H, sum(lens), d, generator=torch.Generator().manual_seed(4)) * 0.5).half()
+    sq = 127.0 / float(qkv_h.abs().max())
+    fus = batched.BatchedSparseAttention(masks, H, d, scale_qkv=sq, scale_sfmx=127.0, device=cuda, fused=True,
+                                         requant="rowmax")
+    fus(qkv_h.to(cuda))
+    torch.cuda.synchronize()
+    for i, m in enumerate(masks):
+        a, z = int(fus.token_offsets[i]), int(fus.token_offsets[i + 1])
+        pairs, n = formats.align_row_offsets(m, 16)
+        cols = formats.pad_column_indices(m, pairs, n, False)
+        mk = oatt.dense_mask(pairs, cols, m.m_vec, 8, lens[i])
+        q, k, v = (qkv_h[j, :, a:z].double().numpy() for j in range(3))
+        ref = oatt.sparse_attention_fp64(q, k, v, mk, d ** -0.5)
+        got = fus.instance_output(i).double().cpu().numpy()
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err < 0.05, err
+
+
+def test_fused_reports_rows_longer_than_declared(cuda):
+    """A max_row_nnz smaller than a row's length must not touch memory out of
+    bounds: the kernel skips that row and sets the status word."""
+    masks = [synth.band_random_mask(512, 8, 64, 0.8, seed=50)]
+    fus = batched.BatchedSparseAttention(masks, 1, 64, scale_qkv=60.0, scale_sfmx=100.0, device=cuda, fused=True)
+    fus.mask.max_row_nnz = 32  # deliberately too small
+    fus.core.m.max_row_nnz = 32
+    fus.core.out.fill_(7.0)
+    fus((torch.randn(3, 1, 512, 64) * 0.5).half().to(cuda))
+    torch.cuda.synchronize()
+    assert int(fus.core.status.item()) == 1
+    assert torch.all(fus.core.out == 7.0)  # every row exceeds 32 nonzero vectors: nothing written

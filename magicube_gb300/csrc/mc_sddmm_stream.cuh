@@ -7,11 +7,14 @@
 //  * k == 64 is one 64-element block: the V rows of A are loaded once per
 //    vector-row and every tile is two mma.m16n8k32 (per byte-plane pair) with
 //    no inner k loop.
-//  * Each warp keeps two tiles of 16 nonzeros in flight: the gathered B rows
-//    of both tiles are requested before either is multiplied, and the column
-//    indices of the warp's next pair of tiles are fetched while the current
-//    pair is multiplied and stored.
+//  * Each warp keeps U tiles of 16 nonzeros in flight: the gathered B rows of
+//    all U are requested before any is multiplied, and the column indices of
+//    the warp's next U tiles are fetched while the current ones are
+//    multiplied and stored.
 //  * Per-row pointers are formed once; per-tile offsets are 32-bit.
+// U = 2 is the measured optimum on GB300 for the 4096x4096x64 V=8 L8-R8 case
+// (114 TOP/s; U = 3: 108, U = 4: 97): more tiles in flight cost registers
+// (56 -> 78 per thread) and with them resident CTAs.
 // The kernel is latency/issue bound rather than HBM bound on GB300 (the
 // sm_103a int8 tensor path is the slow legacy mma.sync), so instruction count
 // per tile is what sets its speed.
@@ -20,7 +23,7 @@
 
 namespace mc {
 
-template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool F16>
+template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool F16, int U = 2>
 __global__ void __launch_bounds__(WARPS * 32)
 sddmm_k64_kernel(const SddmmParams p)
 {
@@ -63,15 +66,15 @@ sddmm_k64_kernel(const SddmmParams p)
         cc[1] = j0 + 8 < nnz ? __ldg(cols + j0 + 8) : -1;
     };
 
-    int c[2][2];
-    load_cols(ti, c[0]);
-    load_cols(ti + stride, c[1]);
+    int c[U][2];
+#pragma unroll
+    for (int u = 0; u < U; ++u) load_cols(ti + u * stride, c[u]);
 
 #pragma unroll 1
-    for (; ti < ntiles; ti += 2 * stride) {
-        uint32_t r[2][2][2][4];  // [tile][row half][byte plane][word]
+    for (; ti < ntiles; ti += U * stride) {
+        uint32_t r[U][2][2][4];  // [tile][row half][byte plane][word]
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int u = 0; u < U; ++u)
 #pragma unroll
             for (int hf = 0; hf < 2; ++hf) {
 #pragma unroll
@@ -80,12 +83,12 @@ sddmm_k64_kernel(const SddmmParams p)
                     for (int e = 0; e < 4; ++e) r[u][hf][q][e] = 0u;
                 if (c[u][hf] >= 0) load_kfrag<PREB, SIGNED>(rhs + (unsigned)c[u][hf] * RHS_ROW, 0, t, r[u][hf]);
             }
-        int cn[2][2];
-        load_cols(ti + 2 * stride, cn[0]);
-        load_cols(ti + 3 * stride, cn[1]);
+        int cn[U][2];
+#pragma unroll
+        for (int u = 0; u < U; ++u) load_cols(ti + (U + u) * stride, cn[u]);
 
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
+        for (int u = 0; u < U; ++u) {
             const int tile = ti + u * stride;
             if (tile >= ntiles) break;
             int d[4];
@@ -171,7 +174,7 @@ sddmm_k64_kernel(const SddmmParams p)
             }
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u) { c[u][0] = cn[u][0]; c[u][1] = cn[u][1]; }
+        for (int u = 0; u < U; ++u) { c[u][0] = cn[u][0]; c[u][1] = cn[u][1]; }
     }
 }
 

@@ -320,8 +320,10 @@ def run_gpu(args) -> None:
                               (args.mma, 1, "per_row_kernel")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
-    attention = serving_res = None
+    attention = serving_res = packer = None
     if not args.headline_only and rank == 0:
+        torch.cuda.empty_cache()
+        packer = packer_suite(args, dev, peaks)
         torch.cuda.empty_cache()
         attention = attention_suite(args, dev)
         torch.cuda.empty_cache()
@@ -360,6 +362,7 @@ def run_gpu(args) -> None:
             "variants": variants,
             "batched_attention": attention,
             "serving": serving_res,
+            "device_packer": packer,
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
@@ -471,6 +474,44 @@ def attention_suite(args, dev) -> dict:
             "autotuned": {"sddmm": b.core.sddmm_cfg, "spmm": b.core.spmm_cfg}}
 
 
+def packer_suite(args, dev, peaks) -> dict:
+    """The vector-sparse packer on the GPU (mcDevice*: aligned pairs, padded
+    columns, packed values, longest-first row order) against the library's
+    host packer, on one SpMM L8-R8 operand: 16,384 vector-rows (M = 131,072),
+    K = 4096, V = 8, row lengths ~ Normal(0.1 K, 0.3 mu), random int8 values.
+    Device packing runs without a host round trip (upper-bound buffers)."""
+    import torch
+
+    from magicube_gb300 import device_format as dfm
+    from magicube_gb300 import formats, synth
+    m = synth.normal_mask(16384, 4096, VEC, 0.9, seed=21)
+    vals = synth.random_bytes(m.nnz_vec * VEC, 22)
+    t0 = time.perf_counter()
+    h = formats.prepare_spmm(m, vals, 8, 8)
+    host_s = time.perf_counter() - t0
+    ro, ci = torch.from_numpy(m.row_offsets).to(dev), torch.from_numpy(m.col_indices).to(dev)
+    dv = torch.from_numpy(vals).to(dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        dfm.prepare_spmm(ro, ci, dv, VEC, m.ncols, 8, 8, sync=False)
+
+    ms = time_cuda(step, 10, 3, stream)
+    t = sum(ms) / len(ms)
+    d = dfm.prepare_spmm(ro, ci, dv, VEC, m.ncols, 8, 8)
+    same = (np.array_equal(d.values.cpu().numpy(), h.values) and np.array_equal(d.col_indices.cpu().numpy(),
+                                                                                 h.col_indices))
+    mv, nnz, al = m.m_vec, m.nnz_vec, h.aligned_nnz
+    nbytes = (4 * (mv + 1) + 4 * nnz + nnz * VEC) + (8 * mv + 4 * al + al * VEC + 4 * mv)
+    gbs = nbytes / (t / 1e3) / 1e9
+    return {"workload": "SpMM L8-R8 operand: 16384 vector-rows x 4096, V=8, sparsity 0.9 (normal row lengths), "
+                        "packed value layout, sorted rows",
+            "nnz_vec": int(nnz), "aligned_nnz": int(al), "algorithmic_bytes": int(nbytes),
+            "device_ms": t, "device_gbs": gbs, "hbm_frac": gbs / peaks["hbm_gbs"],
+            "host_ms": host_s * 1e3, "speedup_vs_host_packer": host_s * 1e3 / t,
+            "identical_to_host_packer": bool(same)}
+
+
 def formats_align(mask, alignment):
     from magicube_gb300 import formats
     pairs, n = formats.align_row_offsets(mask, alignment)
@@ -543,6 +584,18 @@ def run_profile_case(args) -> None:
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "attention", "instances": args.batch, "reps": args.reps}))
         return
+    if args.profile == "packer":
+        from magicube_gb300 import device_format as dfm
+        from magicube_gb300 import synth
+        m = synth.normal_mask(16384, 4096, VEC, 0.9, seed=21)
+        vals = synth.random_bytes(m.nnz_vec * VEC, 22)
+        ro, ci = torch.from_numpy(m.row_offsets).to(dev), torch.from_numpy(m.col_indices).to(dev)
+        dv = torch.from_numpy(vals).to(dev)
+        for _ in range(args.reps):
+            dfm.prepare_spmm(ro, ci, dv, VEC, m.ncols, 8, 8, sync=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "packer", "reps": args.reps}))
+        return
     if args.profile == "sddmm":
         mask, hm, lhs_h, rhs_h = sddmm_workload(8, 8, args.batch)
         dm = ops.DeviceSddmmMask.from_host(hm, dev)
@@ -577,7 +630,7 @@ def main() -> None:
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--requant", choices=["fixed", "rowmax"], default="rowmax",
                     help="requantization of the --profile attention case")
-    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention"], default=None,
+    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention", "packer"], default=None,
                     help="run only a small case of one kernel (for ncu captures)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")
     ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")], default=[200.0, 2000.0],

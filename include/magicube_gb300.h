@@ -6,7 +6,10 @@
  * cudaErrorInvalidValue (1) for rejected arguments (mcGetLastErrorString()
  * says why), or the CUDA error of the launch.  All pointers passed to compute
  * entry points are device pointers unless stated otherwise; buffers are owned
- * by the caller.  Nothing here allocates device memory.
+ * by the caller.  Nothing here allocates device memory except the
+ * device-side format conversion entry points, which take their scratch from
+ * the stream-ordered allocator (cudaMallocAsync / cudaFreeAsync on the
+ * caller's stream).
  *
  * Storage format (identical to the reference's): a sparse M x K matrix is
  * stored as m_vec = M / V vector-rows of column vectors of V = 2, 4 or 8
@@ -238,6 +241,62 @@ int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int rhs_bits, co
 /* Vector-row processing order: longest first (bm_test_utils.h:222-237), or identity. */
 int mcSortedRowSwizzle(int m_vec, const int* row_offsets, int* row_indices);
 int mcIdentityRowSwizzle(int m_vec, int* row_indices);
+
+/* ---- Device-side format conversion (device pointers, stream-ordered) -------
+ * The host packer above run on the GPU (the reference has it only as serial
+ * host code: spmm_benchmark.cpp:177-377, bm_test_utils.h:222-237).  Outputs
+ * are byte-identical to the host routines.  The aligned slot count stays in
+ * device memory, so a caller that sizes its buffers by the upper bound
+ * nnz_vec + m_vec * (alignment - 1) packs without a host round trip. */
+
+/* Aligned pairs (8-byte aligned device array of 2*m_vec ints) and the aligned
+ * slot count (*aligned_nnz, a device int; -1 when the offsets are not
+ * monotone or the count overflows int).  Scratch of 8 * ceil(m_vec / 4096) +
+ * 256 bytes comes from the stream-ordered allocator and is released on the
+ * stream. */
+int mcDeviceAlignRowOffsets(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs,
+                            int* aligned_nnz, cudaStream_t stream);
+/* Column indices into the aligned slots, -1 padded, 8-shuffled if shuffle8
+ * (col_indices and, below, values may be NULL when no row has nonzeros).
+ * Vector-row i fills the slots from its start to the next row's start (the
+ * first row from slot 0, the last up to *aligned_nnz); capacity = elements of
+ * out_cols.  A row whose slots are inconsistent (overlap, past capacity, not
+ * multiples of 8 when shuffling) is skipped and *status (optional device
+ * int) set to 1. */
+int mcDevicePadColumnIndices(int m_vec, const int* row_offsets, const int* col_indices,
+                             const int* aligned_pairs, const int* aligned_nnz, int shuffle8, int* out_cols,
+                             long long capacity, int* status, cudaStream_t stream);
+/* Values into the SpMM device layout (as mcPackSpmmValuesEx); out 4-byte
+ * aligned, capacity_bytes its size.  Row slots must be whole value chunks. */
+int mcDevicePackSpmmValues(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
+                           const int* aligned_pairs, const int* aligned_nnz, const void* values, void* out,
+                           long long capacity_bytes, int value_layout, int* status, cudaStream_t stream);
+/* Longest-first vector-row order; rows of equal length in ascending index
+ * order (a stable sort).  Scratch from the stream-ordered allocator. */
+int mcDeviceSortedRowSwizzle(int m_vec, const int* row_offsets, int* row_indices, cudaStream_t stream);
+
+/* All of the above in one call (fused: one align scan, one per-row pass
+ * writing columns and values, one row sort).  lhs_bits = 0 converts a mask
+ * without values (SDDMM; alignment must then be given).  alignment = 0 with
+ * values: the SpMM alignment of the pair (16, or 32 with a 4-bit operand). */
+typedef struct mcDevicePackDesc {
+    int m_vec, vec_length;
+    int lhs_bits, rhs_bits;       /* the SpMM pair, or lhs_bits = 0 */
+    int alignment;
+    int shuffle8;                 /* 8-shuffle the columns (packed layout with a 4-bit operand) */
+    int value_layout;             /* MC_VALUES_PACKED / MC_VALUES_SOFTMAX */
+    int sort_rows;                /* 1: longest-first row_indices; 0: row_indices untouched */
+    const int* row_offsets;       /* m_vec + 1 */
+    const int* col_indices;
+    const void* values;           /* nnz_vec * V * lhs_bits / 8 bytes */
+    int* aligned_pairs;           /* 2 * m_vec, 8-byte aligned */
+    int* aligned_nnz;             /* one device int */
+    int* out_cols;       long long cols_capacity;         /* elements */
+    void* out_values;    long long values_capacity_bytes; /* 4-byte aligned */
+    int* row_indices;             /* m_vec */
+    int* status;                  /* optional device int, set to 1 on inconsistent rows */
+} mcDevicePackDesc;
+int mcDevicePack(const mcDevicePackDesc* desc, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -62,6 +62,17 @@ class McAttnDesc(ctypes.Structure):
     ]
 
 
+class McDevicePackDesc(ctypes.Structure):
+    _fields_ = [
+        ("m_vec", _c_int), ("vec_length", _c_int), ("lhs_bits", _c_int), ("rhs_bits", _c_int),
+        ("alignment", _c_int), ("shuffle8", _c_int), ("value_layout", _c_int), ("sort_rows", _c_int),
+        ("row_offsets", _c_vp), ("col_indices", _c_vp), ("values", _c_vp),
+        ("aligned_pairs", _c_vp), ("aligned_nnz", _c_vp),
+        ("out_cols", _c_vp), ("cols_capacity", _c_ll), ("out_values", _c_vp), ("values_capacity_bytes", _c_ll),
+        ("row_indices", _c_vp), ("status", _c_vp),
+    ]
+
+
 REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
 MMA_DEFAULT, MMA_INT8, MMA_F16 = 0, 1, 2
 KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM = 0, 1, 2
@@ -86,6 +97,12 @@ _SIGNATURES = {
     "mcPackSpmmValuesEx": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_int]),
     "mcSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp]),
     "mcIdentityRowSwizzle": (_c_int, [_c_int, _c_vp]),
+    "mcDeviceAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "mcDevicePadColumnIndices": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_ll, _c_vp, _c_vp]),
+    "mcDevicePackSpmmValues": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_ll,
+                                        _c_int, _c_vp, _c_vp]),
+    "mcDeviceSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp]),
+    "mcDevicePack": (_c_int, [ctypes.POINTER(McDevicePackDesc), _c_vp]),
 }
 for _p in ("4b", "8b4b", "16b4b", "8b", "16b8b"):
     _SIGNATURES[f"mcWmmaSpmm_{_p}"] = (_c_int, [_c_int, _c_int, _c_int, _c_int] + [_c_vp] * 6)

@@ -10,6 +10,20 @@ namespace mc {
 int default_mma_kind();
 inline int resolve_mma_kind(int k) { return k == MC_MMA_DEFAULT ? default_mma_kind() : k; }
 
+// Number of SMs of the current device (cached per device).
+inline int sm_count()
+{
+    static int cache[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cache[dev] = n;
+    }
+    return cache[dev];
+}
+
 // Records `msg` as the calling thread's last argument error and returns `code`.
 int fail(int code, const char* msg);
 // Clears the calling thread's last argument error.

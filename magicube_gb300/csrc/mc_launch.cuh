@@ -10,20 +10,6 @@
 
 namespace mc {
 
-// Number of SMs of the current device (cached per device).
-inline int sm_count()
-{
-    static int cache[64] = {};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
-    if (!cache[dev]) {
-        int n = 0;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
-        cache[dev] = n;
-    }
-    return cache[dev];
-}
-
 // Persistent grid: resident CTAs of `kernel` over all SMs, capped by the work.
 template <typename K>
 inline int persistent_ctas(K kernel, int threads, long long work_ctas)

@@ -256,6 +256,12 @@ int mcIdentityRowSwizzle(int m_vec, int* row_indices);
  * stream. */
 int mcDeviceAlignRowOffsets(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs,
                             int* aligned_nnz, cudaStream_t stream);
+/* mcDeviceAlignRowOffsets without any allocation (no counterpart in the
+ * reference): the scratch is a 128 KB file-scope device array, so at most
+ * 16,744,448 vector-rows (larger m_vec is rejected with status 1).  Calls that
+ * overlap on the device (concurrent streams) share that scratch and race. */
+int mcDeviceAlignRowOffsetsNoAlloc(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs,
+                                   int* aligned_nnz, cudaStream_t stream);
 /* Column indices into the aligned slots, -1 padded, 8-shuffled if shuffle8
  * (col_indices and, below, values may be NULL when no row has nonzeros).
  * Vector-row i fills the slots from its start to the next row's start (the

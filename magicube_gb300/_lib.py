@@ -98,6 +98,7 @@ _SIGNATURES = {
     "mcSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp]),
     "mcIdentityRowSwizzle": (_c_int, [_c_int, _c_vp]),
     "mcDeviceAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "mcDeviceAlignRowOffsetsNoAlloc": (_c_int, [_c_int, _c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
     "mcDevicePadColumnIndices": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_int, _c_vp, _c_ll, _c_vp, _c_vp]),
     "mcDevicePackSpmmValues": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_ll,
                                         _c_int, _c_vp, _c_vp]),

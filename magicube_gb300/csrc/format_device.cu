@@ -24,6 +24,7 @@
 
 #include <climits>
 #include <cstdint>
+#include <mutex>
 #include <type_traits>
 
 #include "mc_host.h"
@@ -529,7 +530,50 @@ static int key_bits(long long bound)
 
 static size_t round256(size_t b) { return (b + 255) / 256 * 256; }
 
+// Scratch of mcDeviceAlignRowOffsetsNoAlloc: a file-scope device array, so
+// the call allocates nothing.  Calls that overlap on the device (concurrent
+// streams) share it and race.
+constexpr long long kStaticAlignScratchBytes = 128 * 1024;
+static __device__ __align__(256) unsigned char g_align_scratch[kStaticAlignScratchBytes];
+
+// Device address of g_align_scratch on the current device, looked up once per
+// device.
+static int static_align_scratch(void** out)
+{
+    static std::mutex mu;
+    static void* addr[64] = {};
+    int dev = 0;
+    int rc = (int)cudaGetDevice(&dev);
+    if (rc) return rc;
+    if (dev < 0 || dev >= 64) return fail(1, "mcDeviceAlignRowOffsetsNoAlloc: device index out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        rc = (int)cudaGetSymbolAddress(&p, g_align_scratch);
+        if (rc) return rc;
+        addr[dev] = p;
+    }
+    *out = addr[dev];
+    return 0;
+}
+
 }  // namespace mc
+
+extern "C" int mcDeviceAlignRowOffsetsNoAlloc(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs,
+                                              int* aligned_nnz, cudaStream_t stream)
+{
+    mc::clear_error();
+    if (int rc = mc::check_align_args(m_vec, row_offsets, alignment, aligned_pairs, aligned_nnz)) return rc;
+    if (mc::align_scratch_bytes(m_vec) > mc::kStaticAlignScratchBytes)
+        return mc::fail(1, "mcDeviceAlignRowOffsetsNoAlloc: m_vec exceeds the static scratch (at most 16,744,448 "
+                           "vector-rows)");
+    void* scratch = nullptr;
+    if (int rc = mc::static_align_scratch(&scratch)) return rc;
+    // device_align_launch clears the flag word that must start at zero; the
+    // tile sums are written before they are read.
+    return mc::device_align_launch(m_vec, row_offsets, alignment, aligned_pairs, aligned_nnz, scratch, nullptr,
+                                   nullptr, stream);
+}
 
 extern "C" int mcDeviceAlignRowOffsets(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs,
                                        int* aligned_nnz, cudaStream_t stream)

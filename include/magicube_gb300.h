@@ -87,7 +87,7 @@ int mcSetDefaultMmaKind(int kind);
  * MC_KERNEL_STREAM:  the pipelined kernels: SpMM -- persistent CTAs that
  *                    stream many vector-rows through one cp.async ring (needs
  *                    16-byte aligned values); SDDMM -- the k == 64 kernel with
- *                    two tiles in flight per warp (needs k == 64).
+ *                    a warp per 16-nonzero tile at full occupancy (needs k == 64).
  * MC_KERNEL_AUTO:    the pipelined kernel where it applies, else per-row. */
 enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2 };
 

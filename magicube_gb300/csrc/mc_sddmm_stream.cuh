@@ -10,11 +10,14 @@
 //  * Each warp keeps U tiles of 16 nonzeros in flight: the gathered B rows of
 //    all U are requested before any is multiplied, and the column indices of
 //    the warp's next U tiles are fetched while the current ones are
-//    multiplied and stored.
+//    multiplied and stored.  Latency is hidden by resident warps rather than
+//    by depth within a warp (see U below).
 //  * Per-row pointers are formed once; per-tile offsets are 32-bit.
-// U = 2 is the measured optimum on GB300 for the 4096x4096x64 V=8 L8-R8 case
-// (114 TOP/s; U = 3: 108, U = 4: 97): more tiles in flight cost registers
-// (56 -> 78 per thread) and with them resident CTAs.
+// U = 1 is the measured optimum on GB300 for the 4096x4096x64 V=8 L8-R8 case:
+// 32 registers per thread, 16 resident CTAs (64 warps) per SM, 124 TOP/s.
+// More tiles in flight per warp cost registers and with them resident warps
+// (U = 2: 56 registers, 114 TOP/s; U = 3: 108; U = 4: 78 registers, 97; U = 2
+// capped at 48 registers spills: 101).
 // The kernel is latency/issue bound rather than HBM bound on GB300 (the
 // sm_103a int8 tensor path is the slow legacy mma.sync), so instruction count
 // per tile is what sets its speed.
@@ -23,7 +26,7 @@
 
 namespace mc {
 
-template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool F16, int U = 2>
+template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool F16, int U = 1>
 __global__ void __launch_bounds__(WARPS * 32)
 sddmm_k64_kernel(const SddmmParams p)
 {

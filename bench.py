@@ -320,10 +320,12 @@ def run_gpu(args) -> None:
                               (args.mma, 1, "per_row_kernel")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
-    attention = serving_res = packer = None
+    attention = serving_res = packer = projection = None
     if not args.headline_only and rank == 0:
         torch.cuda.empty_cache()
         packer = packer_suite(args, dev, peaks)
+        torch.cuda.empty_cache()
+        projection = projection_suite(args, dev, peaks)
         torch.cuda.empty_cache()
         attention = attention_suite(args, dev)
         torch.cuda.empty_cache()
@@ -363,6 +365,7 @@ def run_gpu(args) -> None:
             "batched_attention": attention,
             "serving": serving_res,
             "device_packer": packer,
+            "qkv_projection": projection,
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
@@ -512,6 +515,44 @@ def packer_suite(args, dev, peaks) -> dict:
             "identical_to_host_packer": bool(same)}
 
 
+def projection_suite(args, dev, peaks) -> dict:
+    """The attention's input projection (hidden 256 -> Q, K, V of 4 heads x 64)
+    over the batched-attention token count (160,640 tokens): the fused tcgen05
+    projection + quantization (mcQkvProjectQuantize) against the unfused path
+    (cuBLAS fp16 F.linear, permute to [3, H, T, d], mcQuantize)."""
+    import torch
+    import torch.nn.functional as F
+
+    from magicube_gb300 import _lib
+    from magicube_gb300.projection import qkv_project_quantize
+    T, E, H, bits, scale = 160640, 256, 4, 8, 40.0
+    g = torch.Generator().manual_seed(31)
+    x = (torch.randn(T, E, generator=g) * 0.5).half().to(dev)
+    w = (torch.randn(3 * E, E, generator=g) / 16).half().to(dev)
+    b = (torch.randn(3 * E, generator=g) * 0.1).half().to(dev)
+    out = torch.empty((3, H, T * (E // H) * bits // 32), dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+
+    def fused():
+        qkv_project_quantize(x, w, b, H, bits, scale, out=out)
+
+    def unfused():
+        qkv = F.linear(x, w, b).view(T, 3, H, E // H).permute(1, 2, 0, 3).contiguous()
+        _lib.check(_lib.lib().mcQuantize(qkv.data_ptr(), out.data_ptr(), qkv.numel(), bits, scale, sh), "mcQuantize")
+
+    ms_f = statistics.median(time_cuda(fused, 20, 5, stream))
+    ms_u = statistics.median(time_cuda(unfused, 20, 5, stream))
+    nbytes = 2 * T * E + 2 * 3 * E * E + 2 * 3 * E + 3 * T * E * bits // 8
+    flops = 2.0 * T * E * 3 * E
+    gbs = nbytes / (ms_f / 1e3) / 1e9
+    return {"workload": "x [160640, 256] half @ W [768, 256]^T + b -> int8 Q, K, V [3][4][160640][64]",
+            "fused_ms": ms_f, "unfused_ms": ms_u, "speedup": ms_u / ms_f,
+            "algorithmic_bytes": int(nbytes), "fused_gbs": gbs, "hbm_frac": gbs / peaks["hbm_gbs"],
+            "fused_tflops": flops / (ms_f / 1e3) / 1e12,
+            "launches": {"fused": 1, "unfused": "F.linear + permute copy + mcQuantize"}}
+
+
 def formats_align(mask, alignment):
     from magicube_gb300 import formats
     pairs, n = formats.align_row_offsets(mask, alignment)
@@ -584,6 +625,18 @@ def run_profile_case(args) -> None:
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "attention", "instances": args.batch, "reps": args.reps}))
         return
+    if args.profile == "projection":
+        from magicube_gb300.projection import qkv_project_quantize
+        T, E, H = 131072, 256, 4  # x 64 MB + out 96 MB: more than the 129 MB L2
+        g = torch.Generator().manual_seed(31)
+        x = (torch.randn(T, E, generator=g) * 0.5).half().to(dev)
+        w = (torch.randn(3 * E, E, generator=g) / 16).half().to(dev)
+        b = (torch.randn(3 * E, generator=g) * 0.1).half().to(dev)
+        for _ in range(args.reps):
+            qkv_project_quantize(x, w, b, H, 8, 40.0)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "projection", "tokens": T, "reps": args.reps}))
+        return
     if args.profile == "packer":
         from magicube_gb300 import device_format as dfm
         from magicube_gb300 import synth
@@ -630,7 +683,7 @@ def main() -> None:
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--requant", choices=["fixed", "rowmax"], default="rowmax",
                     help="requantization of the --profile attention case")
-    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention", "packer"], default=None,
+    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention", "packer", "projection"], default=None,
                     help="run only a small case of one kernel (for ncu captures)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")
     ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")], default=[200.0, 2000.0],

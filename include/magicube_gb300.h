@@ -216,6 +216,31 @@ typedef struct mcAttnDesc {
 } mcAttnDesc;
 int mcSparseAttention(const mcAttnDesc* desc, cudaStream_t stream);
 
+/* ---- Input projection with fused quantization ------------------------------
+ * out[which][h][t][c] = trunc(clamp(float(half(x[t] . W[n] + b[n])) * scale))
+ * for n = which*hidden + h*head_dim + c (which = q, k, v): the reference's
+ * fp16 F.linear + permute + bquantization (spattention.py:189-191,
+ * quantization_kernel.cu:173-213) in one tcgen05 (5th-generation tensor core)
+ * kernel.  x: [tokens][hidden] half, weight: [3*hidden][hidden] half (the
+ * nn.Linear layout), bias: [3*hidden] half or NULL, all 16-byte aligned; out:
+ * [3][heads][tokens][head_dim] packed int8 (bits 8) or int4 (bits 4, two per
+ * byte, low nibble first).  Needs 64 <= hidden <= 256, hidden % 64 == 0,
+ * head_dim % 64 == 0, heads * head_dim == hidden.  The f32 accumulation order
+ * differs from cuBLAS's, so an element whose half rounding or truncation sits
+ * on a boundary can differ by one step from the unfused path.  *status
+ * (optional) is set to 1 if an internal wait timed out. */
+typedef struct mcQkvProjDesc {
+    int tokens, hidden, heads, head_dim;
+    int bits;
+    float scale;
+    const void* x;
+    const void* weight;
+    const void* bias;
+    void* out;
+    int* status;
+} mcQkvProjDesc;
+int mcQkvProjectQuantize(const mcQkvProjDesc* desc, cudaStream_t stream);
+
 /* ---- Host-side format conversion (host pointers) ---------------------------
  * The reference's host packer (SpMM/SpMM/spmm_benchmark.cpp:177-377,
  * SDDMM/SDDMM/sddmm_benchmark.cpp:104-127) as library routines. */

@@ -62,6 +62,13 @@ class McAttnDesc(ctypes.Structure):
     ]
 
 
+class McQkvProjDesc(ctypes.Structure):
+    _fields_ = [
+        ("tokens", _c_int), ("hidden", _c_int), ("heads", _c_int), ("head_dim", _c_int), ("bits", _c_int),
+        ("scale", _c_float), ("x", _c_vp), ("weight", _c_vp), ("bias", _c_vp), ("out", _c_vp), ("status", _c_vp),
+    ]
+
+
 class McDevicePackDesc(ctypes.Structure):
     _fields_ = [
         ("m_vec", _c_int), ("vec_length", _c_int), ("lhs_bits", _c_int), ("rhs_bits", _c_int),
@@ -104,6 +111,7 @@ _SIGNATURES = {
                                         _c_int, _c_vp, _c_vp]),
     "mcDeviceSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp]),
     "mcDevicePack": (_c_int, [ctypes.POINTER(McDevicePackDesc), _c_vp]),
+    "mcQkvProjectQuantize": (_c_int, [ctypes.POINTER(McQkvProjDesc), _c_vp]),
 }
 for _p in ("4b", "8b4b", "16b4b", "8b", "16b8b"):
     _SIGNATURES[f"mcWmmaSpmm_{_p}"] = (_c_int, [_c_int, _c_int, _c_int, _c_int] + [_c_vp] * 6)

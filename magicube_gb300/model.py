@@ -18,6 +18,7 @@ import torch.nn.functional as F
 
 from . import _lib
 from .batched import AttentionMaskDev
+from .projection import qkv_project_quantize
 
 
 def attention_core(qkv: torch.Tensor, mask: AttentionMaskDev, head_dim: int, lhs_bits: int, rhs_bits: int,
@@ -26,13 +27,25 @@ def attention_core(qkv: torch.Tensor, mask: AttentionMaskDev, head_dim: int, lhs
     """qkv: [3, H, T, d] half contiguous -> [H, T, d] half: quantize, SDDMM,
     quantized softmax, SpMM on the current stream."""
     _, H, T, d = qkv.shape
-    dev = qkv.device
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    q_words = T * d * rhs_bits // 32
+    qkv_q = torch.empty((3, H, q_words), dtype=torch.int32, device=qkv.device)
+    _lib.check(_lib.lib().mcQuantize(qkv.data_ptr(), qkv_q.data_ptr(), qkv.numel(), rhs_bits, float(scale_qkv),
+                                     stream), "mcQuantize")
+    return attention_core_quantized(qkv_q, T, mask, head_dim, lhs_bits, rhs_bits, scale_qkv, scale_sfmx,
+                                    sddmm_cfg, spmm_cfg)
+
+
+def attention_core_quantized(qkv_q: torch.Tensor, T: int, mask: AttentionMaskDev, head_dim: int, lhs_bits: int,
+                             rhs_bits: int, scale_qkv: float, scale_sfmx: float, sddmm_cfg: dict | None = None,
+                             spmm_cfg: dict | None = None) -> torch.Tensor:
+    """qkv_q: [3, H, T*d*rhs_bits/32] int32 (quantized Q, K, V) -> [H, T, d]
+    half: SDDMM, quantized softmax, SpMM on the current stream."""
+    H, d = qkv_q.shape[1], head_dim
+    dev = qkv_q.device
     V = mask.vec_length
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     q_words = T * d * rhs_bits // 32
-    qkv_q = torch.empty((3, H, q_words), dtype=torch.int32, device=dev)
-    _lib.check(_lib.lib().mcQuantize(qkv.data_ptr(), qkv_q.data_ptr(), qkv.numel(), rhs_bits, float(scale_qkv),
-                                     stream), "mcQuantize")
     scores = torch.empty((H, mask.aligned_nnz * V), dtype=torch.float16, device=dev)
     sc = sddmm_cfg or {}
     sd = _lib.McSddmmDesc(
@@ -81,15 +94,24 @@ class SparseEncoderLayer(nn.Module):
         self.linear2 = nn.Linear(ffn, hidden)
         self.sddmm_cfg: dict | None = None
         self.spmm_cfg: dict | None = None
+        # The fused projection + quantization kernel (tcgen05) where its shape
+        # constraints hold; otherwise F.linear, permute and mcQuantize.
+        self.fused_projection = hidden % 64 == 0 and 64 <= hidden <= 256 and self.head_dim % 64 == 0
 
     def forward(self, x: torch.Tensor, mask: AttentionMaskDev) -> torch.Tensor:
         """x: [T, hidden] half (sequences back to back) -> [T, hidden]."""
         T = x.shape[0]
         h = self.ln1(x)
-        qkv = F.linear(h, self.in_proj.weight, self.in_proj.bias)              # [T, 3E]
-        qkv = qkv.view(T, 3, self.heads, self.head_dim).permute(1, 2, 0, 3).contiguous()  # [3, H, T, d]
-        att = attention_core(qkv, mask, self.head_dim, self.lhs_bits, self.rhs_bits, self.scale_qkv,
-                             self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg)  # [H, T, d]
+        if self.fused_projection and h.dtype == torch.float16:
+            qkv_q = qkv_project_quantize(h, self.in_proj.weight, self.in_proj.bias, self.heads, self.rhs_bits,
+                                         self.scale_qkv)
+            att = attention_core_quantized(qkv_q, T, mask, self.head_dim, self.lhs_bits, self.rhs_bits,
+                                           self.scale_qkv, self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg)
+        else:
+            qkv = F.linear(h, self.in_proj.weight, self.in_proj.bias)              # [T, 3E]
+            qkv = qkv.view(T, 3, self.heads, self.head_dim).permute(1, 2, 0, 3).contiguous()  # [3, H, T, d]
+            att = attention_core(qkv, mask, self.head_dim, self.lhs_bits, self.rhs_bits, self.scale_qkv,
+                                 self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg)  # [H, T, d]
         att = att.permute(1, 0, 2).reshape(T, self.hidden)
         out = F.linear(att, self.out_proj.weight, self.out_proj.bias) + x
         out = self.ln2(out)

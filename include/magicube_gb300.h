@@ -34,24 +34,35 @@ const char* mcVersion(void);
 
 /* ---- Reference-compatible SpMM entry points --------------------------------
  * Same arguments, layouts and unsigned-lane semantics as the reference's
- * spmm::wmmaSpmm_<P> (SpMM/SpMM/include/wmma_spmm.cuh:14-75), launched on the
+ * spmm::wmmaSpmm_<P> (SpMM/SpMM/include/wmma_spmm.cuh:15-78), launched on the
  * legacy default stream.  output_matrix is M x N int32 row-major.
  * Requires n % 64 == 0.  values is the packer's device layout. */
 int mcWmmaSpmm_4b(int m_vec, int vec_length, int n, int k, const int* row_indices,
                   const int* row_offsets, const int* column_indices, const int* values,
-                  const int* rhs_matrix, int* output_matrix);    /* wmma_spmm.cuh:14 */
+                  const int* rhs_matrix, int* output_matrix);    /* wmma_spmm.cuh:15 */
 int mcWmmaSpmm_8b4b(int m_vec, int vec_length, int n, int k, const int* row_indices,
                     const int* row_offsets, const int* column_indices, const int* values,
-                    const int* rhs_matrix, int* output_matrix);  /* wmma_spmm.cuh:22 */
+                    const int* rhs_matrix, int* output_matrix);  /* wmma_spmm.cuh:23 */
 int mcWmmaSpmm_16b4b(int m_vec, int vec_length, int n, int k, const int* row_indices,
                      const int* row_offsets, const int* column_indices, const int* values,
-                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:38 */
+                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:39 */
 int mcWmmaSpmm_8b(int m_vec, int vec_length, int n, int k, const int* row_indices,
                   const int* row_offsets, const int* column_indices, const int* values,
-                  const int* rhs_matrix, int* output_matrix);    /* wmma_spmm.cuh:46 */
+                  const int* rhs_matrix, int* output_matrix);    /* wmma_spmm.cuh:47 */
 int mcWmmaSpmm_16b8b(int m_vec, int vec_length, int n, int k, const int* row_indices,
                      const int* row_offsets, const int* column_indices, const int* values,
-                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:62 */
+                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:63 */
+/* 12-bit values in the reference's 12-bit layouts (the 16-bit ones with the
+ * top 4 bits clear) and 16-bit x 16-bit. */
+int mcWmmaSpmm_12b4b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                     const int* row_offsets, const int* column_indices, const int* values,
+                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:31 */
+int mcWmmaSpmm_12b8b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                     const int* row_offsets, const int* column_indices, const int* values,
+                     const int* rhs_matrix, int* output_matrix); /* wmma_spmm.cuh:55 */
+int mcWmmaSpmm_16b(int m_vec, int vec_length, int n, int k, const int* row_indices,
+                   const int* row_offsets, const int* column_indices, const int* values,
+                   const int* rhs_matrix, int* output_matrix);   /* wmma_spmm.cuh:71 */
 
 /* ---- Reference-compatible SDDMM entry points -------------------------------
  * Same arguments, layouts and unsigned-lane semantics as the reference's
@@ -114,7 +125,8 @@ enum { MC_VALUES_PACKED = 0, MC_VALUES_SOFTMAX = 1 };
  * GPU kernels do.  out_half = 1 writes half(float(acc) / scale). */
 typedef struct mcSpmmDesc {
     int m_vec, vec_length, n, k;
-    int lhs_bits, rhs_bits;     /* (4,4) (8,4) (16,4) (8,8) (16,8) */
+    int lhs_bits, rhs_bits;     /* (4,4) (8,4) (12,4) (16,4) (8,8) (12,8) (16,8) (16,16);
+                                   12-bit: unsigned lanes, int32 output */
     int is_signed;
     int out_half;
     float scale;
@@ -254,9 +266,10 @@ int mcAlignRowOffsets(int m_vec, const int* row_offsets, int alignment, int* ali
 int mcPadColumnIndices(int m_vec, const int* row_offsets, const int* col_indices,
                        const int* aligned_pairs, int aligned_nnz, int shuffle8, int* out_cols);
 /* Pack original per-vector values (V lanes of lhs_bits, lane v at bit
- * v*lhs_bits) into the SpMM device value layout for the (lhs_bits, rhs_bits)
- * pair: chunk transpose and bit-plane decomposition (spmm_benchmark.cpp:224-377).
- * out holds aligned_nnz*V*lhs_bits/8 bytes. */
+ * v*lhs_bits; 12-bit values in 16-bit lanes) into the SpMM device value layout
+ * for the (lhs_bits, rhs_bits) pair: chunk transpose and bit-plane
+ * decomposition (spmm_benchmark.cpp:224-377).  out holds
+ * aligned_nnz*V*lhs_bits/8 bytes (16 bits per lane for 12-bit values). */
 int mcPackSpmmValues(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
                      const int* aligned_pairs, int aligned_nnz, const void* values, void* out);
 /* Same, for either value layout (MC_VALUES_PACKED or MC_VALUES_SOFTMAX). */

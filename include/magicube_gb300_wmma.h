@@ -2,12 +2,11 @@
  * magicube_gb300_wmma.h -- the reference's C++ kernel API as provided by
  * libmagicube_gb300.so (C++ linkage, namespaces spmm and sddmm).
  *
- * The declarations are the reference's own (SpMM/SpMM/include/wmma_spmm.cuh:14-75,
+ * The declarations are the reference's own (SpMM/SpMM/include/wmma_spmm.cuh:15-78,
  * SDDMM/SDDMM/include/wmma_sddmm.cuh), so a program that includes the
  * reference's headers links against this library unchanged.  Semantics:
  * unsigned lanes, legacy default stream, the reference's device layouts (see
- * magicube_gb300.h).  wmmaSpmm_12b4b, wmmaSpmm_12b8b and wmmaSpmm_16b return
- * cudaErrorNotSupported.
+ * magicube_gb300.h), every precision variant included.
  */
 #ifndef MAGICUBE_GB300_WMMA_H
 #define MAGICUBE_GB300_WMMA_H

@@ -113,7 +113,7 @@ _SIGNATURES = {
     "mcDevicePack": (_c_int, [ctypes.POINTER(McDevicePackDesc), _c_vp]),
     "mcQkvProjectQuantize": (_c_int, [ctypes.POINTER(McQkvProjDesc), _c_vp]),
 }
-for _p in ("4b", "8b4b", "16b4b", "8b", "16b8b"):
+for _p in ("4b", "8b4b", "12b4b", "16b4b", "8b", "12b8b", "16b8b", "16b"):
     _SIGNATURES[f"mcWmmaSpmm_{_p}"] = (_c_int, [_c_int, _c_int, _c_int, _c_int] + [_c_vp] * 6)
 for _p in ("4b", "8b", "16b"):
     _SIGNATURES[f"mcWmmaSddmm_{_p}"] = (_c_int, [_c_int, _c_int, _c_int] + [_c_vp] * 6 + [_c_int])

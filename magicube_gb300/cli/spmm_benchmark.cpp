@@ -10,7 +10,8 @@
 //   N       columns of B and C;  V  vector length (2, 4, 8)
 //   kernel  0 (the library's kernels; other values are rejected)
 //   sort    1: process vector-rows longest first;  func 1: verify on the host
-//   sparse  1;  preA / preB  lhs / rhs bits: 4-4, 8-4, 16-4, 8-8, 16-8
+//   sparse  1;  preA / preB  lhs / rhs bits: 4-4, 8-4, 12-4, 16-4, 8-8, 12-8,
+//           16-8, 16-16 (12-bit values in 16-bit containers)
 //
 // Data are generated as the reference does (bm_test_utils.h:130-164: a
 // default-seeded std::default_random_engine, copied into every call, and
@@ -86,14 +87,14 @@ bool read_smtx(const std::string& path, Smtx& s)
 }
 
 // Container type of one vector's values and the number of containers per
-// vector, as the reference dispatches them (spmm_benchmark.cpp:805-831).
-void container(int preA, int preB, int V, int& bytes, int& scale)
+// vector, as the reference dispatches them (spmm_benchmark.cpp:805-831);
+// `lane` is the bits per stored lane (16 for 12-bit values).
+void container(int lane, int preB, int V, int& bytes, int& scale)
 {
     scale = 1;
-    const int bits = V * preA;
-    if (preA == 16 && V == 8) { bytes = 8; scale = 2; }
-    else bytes = bits / 8;
-    (void)preB;
+    if (lane == 16 && preB == 16) { bytes = 2; scale = V; }
+    else if (lane == 16 && V == 8) { bytes = 8; scale = 2; }
+    else bytes = V * lane / 8;
 }
 
 template <typename T>
@@ -107,19 +108,20 @@ std::vector<uint8_t> gen_values(long long nvec, int V, int preA, int scale, std:
     return out;
 }
 
-// Host C = A * B over the original layout with unsigned lanes.
+// Host C = A * B over the original layout with unsigned lanes (lane: bits
+// per stored lane; preA: significant bits of a value).
 void host_spmm(const std::vector<uint8_t>& vals, const std::vector<int>& B, std::vector<int>& C, const Smtx& s, int V,
-               int N, int preA, int preB)
+               int N, int lane, int preA, int preB)
 {
     C.assign((size_t)s.m_vec * V * N, 0);
     const int per = 32 / preB, ipr = N / per;
-    const uint32_t mb = (1u << preB) - 1u;
+    const uint32_t mb = preB == 32 ? 0xFFFFFFFFu : (1u << preB) - 1u;
     for (int i = 0; i < s.m_vec; ++i)
         for (int j = s.offsets[i]; j < s.offsets[i + 1]; ++j)
             for (int v = 0; v < V; ++v) {
-                const long long bit = ((long long)j * V + v) * preA;
+                const long long bit = ((long long)j * V + v) * lane;
                 uint32_t a = 0;
-                for (int b = 0; b < (preA + 7) / 8 + 1 && bit / 8 + b < (long long)vals.size(); ++b)
+                for (int b = 0; b < (lane + 7) / 8 + 1 && bit / 8 + b < (long long)vals.size(); ++b)
                     a |= (uint32_t)vals[(size_t)(bit / 8 + b)] << (8 * b);
                 a = (a >> (bit % 8)) & ((1u << preA) - 1u);
                 uint32_t* crow = reinterpret_cast<uint32_t*>(C.data()) + (size_t)(i * V + v) * N;
@@ -149,9 +151,12 @@ int main(int argc, char** argv)
     int (*fn)(int, int, int, int, const int*, const int*, const int*, const int*, const int*, int*) = nullptr;
     if (preA == 4 && preB == 4) fn = mcWmmaSpmm_4b;
     else if (preA == 8 && preB == 4) fn = mcWmmaSpmm_8b4b;
+    else if (preA == 12 && preB == 4) fn = mcWmmaSpmm_12b4b;
     else if (preA == 16 && preB == 4) fn = mcWmmaSpmm_16b4b;
     else if (preA == 8 && preB == 8) fn = mcWmmaSpmm_8b;
+    else if (preA == 12 && preB == 8) fn = mcWmmaSpmm_12b8b;
     else if (preA == 16 && preB == 8) fn = mcWmmaSpmm_16b8b;
+    else if (preA == 16 && preB == 16) fn = mcWmmaSpmm_16b;
     if (!fn || !(V == 2 || V == 4 || V == 8)) {
         std::printf("Unsupported precision and vec_length!\n");
         return 1;
@@ -163,18 +168,19 @@ int main(int argc, char** argv)
     }
     const int K = s.ncols, M = s.m_vec * V;
     const int mma_k = (preA == 4 || preB == 4) ? 32 : 16;
-    std::printf("preA %d, preA_cut %d, preB %d, vec_length %d \n", preA, preA, preB, V);
+    const int lane = preA == 12 ? 16 : preA;  // bits per stored value lane
+    std::printf("preA %d, preA_cut %d, preB %d, vec_length %d \n", lane, preA, preB, V);
     std::printf("m_vec %d, dimN %d, nonzeros_vec %d, dimk %d, mma_k_dim %d \n", s.m_vec, N, s.nnz, K, mma_k);
 
     std::default_random_engine generator;
     int bytes = 0, scale = 1;
-    container(preA, preB, V, bytes, scale);
+    container(lane, preB, V, bytes, scale);
     std::vector<uint8_t> vals;
     switch (bytes) {
-        case 1: vals = gen_values<char>(s.nnz, V, preA, scale, generator); break;
-        case 2: vals = gen_values<short>(s.nnz, V, preA, scale, generator); break;
-        case 4: vals = gen_values<int>(s.nnz, V, preA, scale, generator); break;
-        default: vals = gen_values<long long>(s.nnz, V, preA, scale, generator); break;
+        case 1: vals = gen_values<char>(s.nnz, V, lane, scale, generator); break;
+        case 2: vals = gen_values<short>(s.nnz, V, lane, scale, generator); break;
+        case 4: vals = gen_values<int>(s.nnz, V, lane, scale, generator); break;
+        default: vals = gen_values<long long>(s.nnz, V, lane, scale, generator); break;
     }
     std::vector<int> B((size_t)K * N * preB / 32);
     make_dense<int>((long long)B.size(), B.data(), generator);
@@ -183,7 +189,7 @@ int main(int argc, char** argv)
     const int aligned = mcAlignRowOffsets(s.m_vec, s.offsets.data(), mma_k, pairs.data());
     std::printf(" nonzero_vec: %d aligned_ nonzero_vec: %d\n", s.nnz, aligned);
     std::vector<int> cols(aligned > 0 ? aligned : 1);
-    std::vector<uint8_t> packed((size_t)aligned * V * preA / 8 + 16);
+    std::vector<uint8_t> packed((size_t)aligned * V * lane / 8 + 16);
     if (aligned < 0 || mcPadColumnIndices(s.m_vec, s.offsets.data(), s.cols.data(), pairs.data(), aligned,
                                           mma_k == 32, cols.data()) ||
         mcPackSpmmValues(s.m_vec, V, preA, preB, s.offsets.data(), pairs.data(), aligned, vals.data(),
@@ -237,7 +243,7 @@ int main(int argc, char** argv)
         std::printf("performance TOP/s: %g\n", gops / (avg_ms / 1000.0) / 1000.0);
         std::vector<int> got((size_t)M * N), ref;
         CHECK_CUDA(cudaMemcpy(got.data(), d_C, sizeof(int) * got.size(), cudaMemcpyDeviceToHost));
-        host_spmm(vals, B, ref, s, V, N, preA, preB);
+        host_spmm(vals, B, ref, s, V, N, lane, preA, preB);
         long long errors = 0;
         for (size_t i = 0; i < got.size(); ++i) errors += got[i] != ref[i];
         if (errors) std::printf("SPMM does not agree with SEQUENTIAL! %lld errors!\n", errors);

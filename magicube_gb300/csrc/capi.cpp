@@ -29,12 +29,16 @@ static int check_spmm(const mcSpmmDesc& d)
     if (!(d.vec_length == 2 || d.vec_length == 4 || d.vec_length == 8))
         return fail(1, "mcSpmm: vec_length must be 2, 4 or 8");
     const bool pair_ok = (d.lhs_bits == 4 && d.rhs_bits == 4) || (d.lhs_bits == 8 && d.rhs_bits == 4) ||
-                         (d.lhs_bits == 16 && d.rhs_bits == 4) || (d.lhs_bits == 8 && d.rhs_bits == 8) ||
-                         (d.lhs_bits == 16 && d.rhs_bits == 8);
+                         (d.lhs_bits == 12 && d.rhs_bits == 4) || (d.lhs_bits == 16 && d.rhs_bits == 4) ||
+                         (d.lhs_bits == 8 && d.rhs_bits == 8) || (d.lhs_bits == 12 && d.rhs_bits == 8) ||
+                         (d.lhs_bits == 16 && d.rhs_bits == 8) || (d.lhs_bits == 16 && d.rhs_bits == 16);
     if (!pair_ok) {
         std::snprintf(buf, sizeof buf, "mcSpmm: unsupported precision pair L%d-R%d", d.lhs_bits, d.rhs_bits);
         return fail(1, buf);
     }
+    if (d.lhs_bits == 12 && (d.is_signed || d.out_half))
+        return fail(1, "mcSpmm: 12-bit values are unsigned lanes with int32 output (the reference's 12-bit "
+                       "kernels); signed 12-bit data runs as lhs_bits = 16 with sign-extended values");
     if (d.n % 64) return fail(1, "mcSpmm: n must be a multiple of 64");
     if (d.n / 64 > 65535) return fail(1, "mcSpmm: n too large");
     if (d.batch < 1 || d.batch > 65535) return fail(1, "mcSpmm: batch must be in [1, 65535]");
@@ -108,11 +112,19 @@ int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream)
     const mcSpmmDesc& d = *desc;
     if (int rc = mc::check_spmm(d)) return rc;
     if (d.m_vec == 0) return 0;
+    if (d.lhs_bits == 12) {
+        // 12-bit values use the 16-bit layouts with the top 4 bits clear
+        // (spmm_benchmark.cpp:288-358): the 16-bit kernels compute them.
+        mcSpmmDesc e = d;
+        e.lhs_bits = 16;
+        return d.rhs_bits == 4 ? mc::spmm_launch_16_4(e, stream) : mc::spmm_launch_16_8(e, stream);
+    }
     if (d.rhs_bits == 4) {
         if (d.lhs_bits == 4) return mc::spmm_launch_4_4(d, stream);
         if (d.lhs_bits == 8) return mc::spmm_launch_8_4(d, stream);
         return mc::spmm_launch_16_4(d, stream);
     }
+    if (d.rhs_bits == 16) return mc::spmm_launch_16_16(d, stream);
     if (d.lhs_bits == 8) return mc::spmm_launch_8_8(d, stream);
     return mc::spmm_launch_16_8(d, stream);
 }
@@ -158,6 +170,15 @@ int mcWmmaSpmm_8b(int m_vec, int vec_length, int n, int k, const int* ri, const 
 int mcWmmaSpmm_16b8b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
                      const int* values, const int* rhs, int* out)
 { return legacy_spmm(16, 8, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+int mcWmmaSpmm_12b4b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                     const int* values, const int* rhs, int* out)
+{ return legacy_spmm(12, 4, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+int mcWmmaSpmm_12b8b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                     const int* values, const int* rhs, int* out)
+{ return legacy_spmm(12, 8, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
+int mcWmmaSpmm_16b(int m_vec, int vec_length, int n, int k, const int* ri, const int* ro, const int* ci,
+                   const int* values, const int* rhs, int* out)
+{ return legacy_spmm(16, 16, m_vec, vec_length, n, k, ri, ro, ci, values, rhs, out); }
 
 static int legacy_sddmm(int bits, int m_vec, int k, int n, const int* row_indices, const int* row_offsets,
                         const int* column_indices, const int* lhs, const int* rhs, int* out, int vec_length)

@@ -1,13 +1,13 @@
 // compat.cpp -- the reference's C++ kernel API, implemented by this library.
 //
-// Defines spmm::wmmaSpmm_* (SpMM/SpMM/include/wmma_spmm.cuh:14-75) and
+// Defines spmm::wmmaSpmm_* (SpMM/SpMM/include/wmma_spmm.cuh:15-78) and
 // sddmm::wmmaSddmm_* (SDDMM/SDDMM/src/wmma_sddmm.cu:394,439,488) with the
 // reference's exact signatures, so code written against the reference (its
 // benchmark programs included) links against libmagicube_gb300.so in place
 // of the reference's wmma_spmm.cu / wmma_sddmm.cu, unchanged.  Each function
 // forwards to the matching C entry point (unsigned lanes, legacy default
-// stream, the reference's device layouts).  The 12-bit and 16-bit x 16-bit
-// SpMM variants return cudaErrorNotSupported.
+// stream, the reference's device layouts), the 12-bit and 16-bit x 16-bit
+// SpMM variants included.
 #include <cuda_runtime_api.h>
 
 #include "../../include/magicube_gb300_wmma.h"
@@ -29,20 +29,10 @@ MC_SPMM_FWD(wmmaSpmm_8b4b, mcWmmaSpmm_8b4b)
 MC_SPMM_FWD(wmmaSpmm_16b4b, mcWmmaSpmm_16b4b)
 MC_SPMM_FWD(wmmaSpmm_8b, mcWmmaSpmm_8b)
 MC_SPMM_FWD(wmmaSpmm_16b8b, mcWmmaSpmm_16b8b)
+MC_SPMM_FWD(wmmaSpmm_12b4b, mcWmmaSpmm_12b4b)
+MC_SPMM_FWD(wmmaSpmm_12b8b, mcWmmaSpmm_12b8b)
+MC_SPMM_FWD(wmmaSpmm_16b, mcWmmaSpmm_16b)
 #undef MC_SPMM_FWD
-
-#define MC_SPMM_UNSUPPORTED(NAME)                                                                  \
-    cudaError_t NAME(int, int, int, int, const int* __restrict__, const int* __restrict__,          \
-                     const int* __restrict__, const int* __restrict__, const int* __restrict__,     \
-                     int* __restrict__)                                                             \
-    {                                                                                               \
-        mc::fail(1, #NAME ": not provided by libmagicube_gb300");                                  \
-        return cudaErrorNotSupported;                                                               \
-    }
-MC_SPMM_UNSUPPORTED(wmmaSpmm_12b4b)
-MC_SPMM_UNSUPPORTED(wmmaSpmm_12b8b)
-MC_SPMM_UNSUPPORTED(wmmaSpmm_16b)
-#undef MC_SPMM_UNSUPPORTED
 
 }  // namespace spmm
 

@@ -40,8 +40,9 @@ inline void or_bits(uint8_t* p, long long lane, int bits, uint32_t v)
 bool valid_pair(int lhs_bits, int rhs_bits)
 {
     return (lhs_bits == 4 && rhs_bits == 4) || (lhs_bits == 8 && rhs_bits == 4) ||
-           (lhs_bits == 16 && rhs_bits == 4) || (lhs_bits == 8 && rhs_bits == 8) ||
-           (lhs_bits == 16 && rhs_bits == 8);
+           (lhs_bits == 12 && rhs_bits == 4) || (lhs_bits == 16 && rhs_bits == 4) ||
+           (lhs_bits == 8 && rhs_bits == 8) || (lhs_bits == 12 && rhs_bits == 8) ||
+           (lhs_bits == 16 && rhs_bits == 8) || (lhs_bits == 16 && rhs_bits == 16);
 }
 
 }  // namespace
@@ -99,8 +100,13 @@ extern "C" int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int r
     const int V = vec_length;
     if (m_vec < 0 || !(V == 2 || V == 4 || V == 8) || !valid_pair(lhs_bits, rhs_bits) || !row_offsets ||
         !aligned_pairs || !out || aligned_nnz < 0 ||
-        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX))
+        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX) ||
+        (lhs_bits == 12 && value_layout != MC_VALUES_PACKED))
         return mc::fail(1, "mcPackSpmmValues: invalid arguments");
+    // 12-bit values sit in 16-bit containers and use the 16-bit layouts with
+    // the top 4 bits cleared (spmm_benchmark.cpp:288-358).
+    const uint32_t vmask = lhs_bits == 12 ? 0xFFFu : 0xFFFFFFFFu;
+    if (lhs_bits == 12) lhs_bits = 16;
     const int mma_k = (lhs_bits == 4 || rhs_bits == 4) ? 32 : 16;
     if (aligned_nnz % mma_k) return mc::fail(1, "mcPackSpmmValues: aligned_nnz not a multiple of the chunk size");
     // Chunk of `chunk` slots holding `planes` planes of `plane_bits`; element
@@ -125,7 +131,7 @@ extern "C" int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int r
             uint8_t* cbase = dst + (slot / chunk) * chunk_bytes;
             const int jj = (int)(slot % chunk);
             for (int v = 0; v < V; ++v) {
-                const uint32_t x = get_bits(src, (long long)j * V + v, lhs_bits);
+                const uint32_t x = get_bits(src, (long long)j * V + v, lhs_bits) & vmask;
                 for (int pl = 0; pl < planes; ++pl)
                     or_bits(cbase, pl * plane_elems + v * vstride + jj, plane_bits, (x >> (pl * plane_bits)) & pmask);
             }

@@ -250,7 +250,7 @@ struct ValueLayout {
 // Output word w (counted from the row's first chunk c0) of a row's values.
 template <int V, int LHS, int CHUNK, bool INTERLEAVED>
 __device__ __forceinline__ uint32_t value_word(const RowSpan& r, const uint8_t* __restrict__ src, long long c0,
-                                               long long w, long long nw)
+                                               long long w, long long nw, uint32_t vmask)
 {
     using L = ValueLayout<V, LHS, CHUNK, INTERLEAVED>;
     constexpr uint32_t PMASK = (1u << L::PLANE) - 1u;
@@ -273,7 +273,7 @@ __device__ __forceinline__ uint32_t value_word(const RowSpan& r, const uint8_t* 
             }
             const long long jr = c * CHUNK + jj - r.start;
             if (jr >= 0 && jr < r.len) {
-                const uint32_t x = lane_bits<LHS>(src, (r.src + jr) * V + v);
+                const uint32_t x = lane_bits<LHS>(src, (r.src + jr) * V + v) & vmask;
                 word |= ((x >> (pl * L::PLANE)) & PMASK) << (e * L::PLANE);
             }
         }
@@ -331,7 +331,7 @@ __device__ __forceinline__ void pack_row_values_8b16(const RowSpan& r, const uin
 // FAST: the 8-bit 16-slot path (values V-byte aligned).
 template <int V, int LHS, int CHUNK, bool INTERLEAVED, bool FAST>
 __device__ __forceinline__ void pack_row_values(const RowSpan& r, const uint8_t* __restrict__ src,
-                                                uint8_t* __restrict__ out, int lane)
+                                                uint8_t* __restrict__ out, int lane, uint32_t vmask)
 {
     using L = ValueLayout<V, LHS, CHUNK, INTERLEAVED>;
     if constexpr (FAST && LHS == 8 && CHUNK == 16 && !INTERLEAVED) {
@@ -343,7 +343,8 @@ __device__ __forceinline__ void pack_row_values(const RowSpan& r, const uint8_t*
     for (long long w0 = lane; w0 < nw; w0 += 32 * kUnroll) {
         uint32_t word[kUnroll];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) word[u] = value_word<V, LHS, CHUNK, INTERLEAVED>(r, src, c0, w0 + 32 * u, nw);
+        for (int u = 0; u < kUnroll; ++u)
+            word[u] = value_word<V, LHS, CHUNK, INTERLEAVED>(r, src, c0, w0 + 32 * u, nw, vmask);
 #pragma unroll
         for (int u = 0; u < kUnroll; ++u) {
             const long long w = w0 + 32 * u;
@@ -361,7 +362,7 @@ __global__ void __launch_bounds__(256)
 fill_rows_kernel(int m_vec, const int* __restrict__ ro, const int* __restrict__ pairs,
                  const int* __restrict__ total, int unit, long long cap, const int* __restrict__ cols,
                  int shuffle8, int* __restrict__ cols_out, const uint8_t* __restrict__ src,
-                 uint8_t* __restrict__ vals_out, int* status)
+                 uint8_t* __restrict__ vals_out, uint32_t vmask, int* status)
 {
     const int rows = m_vec > 0 ? m_vec : 1;
     const int lane = threadIdx.x & 31;
@@ -373,7 +374,7 @@ fill_rows_kernel(int m_vec, const int* __restrict__ ro, const int* __restrict__ 
             continue;
         }
         if (cols_out) pad_row_columns(r, cols, shuffle8 != 0, cols_out, lane);
-        if constexpr (VALUES) pack_row_values<V, LHS, CHUNK, INTERLEAVED, FAST>(r, src, vals_out, lane);
+        if constexpr (VALUES) pack_row_values<V, LHS, CHUNK, INTERLEAVED, FAST>(r, src, vals_out, lane, vmask);
     }
 }
 
@@ -408,6 +409,7 @@ struct FillArgs {
     uint8_t* vals_out;
     long long vals_cap_bytes;
     int* status;
+    uint32_t vmask;  // applied to every source value (12-bit values: 0xFFF)
 };
 
 template <int V, int LHS, int CHUNK, bool IL>
@@ -421,13 +423,13 @@ int fill_launch(const FillArgs& a, cudaStream_t s)
         if (reinterpret_cast<uintptr_t>(a.src) % V == 0) {
             fill_rows_kernel<V, LHS, CHUNK, IL, true, true><<<grid, 256, 0, s>>>(
                 a.m_vec, a.ro, a.pairs, a.total, CHUNK, cap, a.cols, a.shuffle8, a.cols_out, a.src, a.vals_out,
-                a.status);
+                a.vmask, a.status);
             return (int)cudaGetLastError();
         }
     }
     fill_rows_kernel<V, LHS, CHUNK, IL, true><<<grid, 256, 0, s>>>(a.m_vec, a.ro, a.pairs, a.total, CHUNK, cap,
                                                                    a.cols, a.shuffle8, a.cols_out, a.src, a.vals_out,
-                                                                   a.status);
+                                                                   a.vmask, a.status);
     return (int)cudaGetLastError();
 }
 
@@ -449,13 +451,18 @@ int fill_v(int lhs_bits, int rhs_bits, int layout, const FillArgs& a, cudaStream
     return fill_launch<V, 16, 16, false>(a, s);
 }
 
-int fill(int vec_length, int lhs_bits, int rhs_bits, int layout, const FillArgs& a, cudaStream_t s)
+int fill(int vec_length, int lhs_bits, int rhs_bits, int layout, const FillArgs& a_in, cudaStream_t s)
 {
+    // 12-bit values: 16-bit containers in the 16-bit layouts, top 4 bits
+    // cleared (spmm_benchmark.cpp:288-358).
+    FillArgs a = a_in;
+    a.vmask = lhs_bits == 12 ? 0xFFFu : 0xFFFFFFFFu;
+    if (lhs_bits == 12) lhs_bits = 16;
     if (lhs_bits == 0) {
         const int grid = grid_for_warps(a.m_vec > 0 ? a.m_vec : 1);
         fill_rows_kernel<2, 8, 16, false, false><<<grid, 256, 0, s>>>(
             a.m_vec, a.ro, a.pairs, a.total, a.shuffle8 ? 8 : 1, a.cols_cap, a.cols, a.shuffle8, a.cols_out,
-            nullptr, nullptr, a.status);
+            nullptr, nullptr, 0xFFFFFFFFu, a.status);
         return (int)cudaGetLastError();
     }
     switch (vec_length) {
@@ -468,8 +475,9 @@ int fill(int vec_length, int lhs_bits, int rhs_bits, int layout, const FillArgs&
 bool valid_pair(int lhs_bits, int rhs_bits)
 {
     return (lhs_bits == 4 && rhs_bits == 4) || (lhs_bits == 8 && rhs_bits == 4) ||
-           (lhs_bits == 16 && rhs_bits == 4) || (lhs_bits == 8 && rhs_bits == 8) ||
-           (lhs_bits == 16 && rhs_bits == 8);
+           (lhs_bits == 12 && rhs_bits == 4) || (lhs_bits == 16 && rhs_bits == 4) ||
+           (lhs_bits == 8 && rhs_bits == 8) || (lhs_bits == 12 && rhs_bits == 8) ||
+           (lhs_bits == 16 && rhs_bits == 8) || (lhs_bits == 16 && rhs_bits == 16);
 }
 
 }  // namespace
@@ -597,7 +605,7 @@ extern "C" int mcDevicePadColumnIndices(int m_vec, const int* row_offsets, const
     if (m_vec < 0 || !row_offsets || !aligned_nnz || !out_cols || capacity < 0 || (m_vec > 0 && !aligned_pairs))
         return mc::fail(1, "mcDevicePadColumnIndices: invalid arguments");
     mc::FillArgs a{m_vec, row_offsets, aligned_pairs, aligned_nnz, col_indices, shuffle8 ? 1 : 0, out_cols,
-                   capacity, nullptr, nullptr, 0, status};
+                   capacity, nullptr, nullptr, 0, status, 0xFFFFFFFFu};
     return mc::fill(0, 0, 0, MC_VALUES_PACKED, a, stream);
 }
 
@@ -609,11 +617,13 @@ extern "C" int mcDevicePackSpmmValues(int m_vec, int vec_length, int lhs_bits, i
     mc::clear_error();
     if (m_vec < 0 || !(vec_length == 2 || vec_length == 4 || vec_length == 8) || !mc::valid_pair(lhs_bits, rhs_bits) ||
         !row_offsets || !aligned_nnz || !out || capacity_bytes < 0 ||
-        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX) || (m_vec > 0 && !aligned_pairs))
+        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX) || (m_vec > 0 && !aligned_pairs) ||
+        (lhs_bits == 12 && value_layout != MC_VALUES_PACKED))
         return mc::fail(1, "mcDevicePackSpmmValues: invalid arguments");
     if (reinterpret_cast<uintptr_t>(out) % 4) return mc::fail(1, "mcDevicePackSpmmValues: out must be 4-byte aligned");
     mc::FillArgs a{m_vec, row_offsets, aligned_pairs, aligned_nnz, nullptr, 0, nullptr, 0,
-                   static_cast<const uint8_t*>(values), static_cast<uint8_t*>(out), capacity_bytes, status};
+                   static_cast<const uint8_t*>(values), static_cast<uint8_t*>(out), capacity_bytes, status,
+                   0xFFFFFFFFu};
     return mc::fill(vec_length, lhs_bits, rhs_bits, value_layout, a, stream);
 }
 
@@ -659,6 +669,8 @@ extern "C" int mcDevicePack(const mcDevicePackDesc* d, cudaStream_t stream)
             (d->value_layout != MC_VALUES_PACKED && d->value_layout != MC_VALUES_SOFTMAX) || !d->out_values ||
             d->values_capacity_bytes < 0 || reinterpret_cast<uintptr_t>(d->out_values) % 4)
             return mc::fail(1, "mcDevicePack: invalid value arguments (pair, vec_length, layout, 4-byte aligned out)");
+        if (d->lhs_bits == 12 && d->value_layout != MC_VALUES_PACKED)
+            return mc::fail(1, "mcDevicePack: 12-bit values use the packed layout");
         const int chunk = (d->value_layout == MC_VALUES_SOFTMAX) ? (d->lhs_bits == 4 ? 32 : 16)
                                                                    : ((d->lhs_bits == 4 || d->rhs_bits == 4) ? 32 : 16);
         if (alignment == 0) alignment = (d->lhs_bits == 4 || d->rhs_bits == 4) ? 32 : 16;
@@ -685,7 +697,7 @@ extern "C" int mcDevicePack(const mcDevicePackDesc* d, cudaStream_t stream)
     if (!rc) {
         mc::FillArgs a{m, d->row_offsets, d->aligned_pairs, d->aligned_nnz, d->col_indices, d->shuffle8 ? 1 : 0,
                        d->out_cols, d->cols_capacity, static_cast<const uint8_t*>(d->values),
-                       static_cast<uint8_t*>(d->out_values), d->values_capacity_bytes, d->status};
+                       static_cast<uint8_t*>(d->out_values), d->values_capacity_bytes, d->status, 0xFFFFFFFFu};
         rc = mc::fill(d->vec_length, values ? d->lhs_bits : 0, d->rhs_bits, d->value_layout, a, stream);
     }
     if (!rc && arr)

@@ -35,6 +35,7 @@ int spmm_launch_8_4(const mcSpmmDesc& d, cudaStream_t s);
 int spmm_launch_16_4(const mcSpmmDesc& d, cudaStream_t s);
 int spmm_launch_8_8(const mcSpmmDesc& d, cudaStream_t s);
 int spmm_launch_16_8(const mcSpmmDesc& d, cudaStream_t s);
+int spmm_launch_16_16(const mcSpmmDesc& d, cudaStream_t s);
 int sddmm_launch_4_4(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_launch_8_8(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_launch_16_8(const mcSddmmDesc& d, cudaStream_t s);

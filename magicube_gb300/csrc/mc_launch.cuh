@@ -46,27 +46,41 @@ template <int V, int PA, int PB, bool S, bool H>
 int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
     constexpr bool E = H;
-    const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
-    const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
-    if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
-        return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");
-    if (d.kernel_variant != MC_KERNEL_PER_ROW && stream_ok) {
-        if (d.n % 128 == 0)
-            return f16 ? spmm_launch_stream<V, PA, PB, S, H, 4, true, E>(d, p, s)
-                       : spmm_launch_stream<V, PA, PB, S, H, 4, false, E>(d, p, s);
-        return f16 ? spmm_launch_stream<V, PA, PB, S, H, 2, true, E>(d, p, s)
-                   : spmm_launch_stream<V, PA, PB, S, H, 2, false, E>(d, p, s);
-    }
-    if (d.n % 128 == 0) {
-        dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 128), (unsigned)d.batch);
-        if (f16) spmm_kernel<V, PA, PB, S, 4, H, true, E><<<grid, 128, 0, s>>>(p);
-        else spmm_kernel<V, PA, PB, S, 4, H, false, E><<<grid, 128, 0, s>>>(p);
+    if constexpr (PB == 16) {
+        // 16-bit B: the per-row kernel on the int8 path (the f16 path gives the
+        // same integers; it is not built for four byte-plane products).
+        if (d.kernel_variant == MC_KERNEL_STREAM) return fail(1, "mcSpmm: 16-bit B runs on the per-row kernel");
+        if (d.n % 128 == 0) {
+            dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 128), (unsigned)d.batch);
+            spmm_kernel<V, PA, PB, S, 4, H, false, E><<<grid, 128, 0, s>>>(p);
+        } else {
+            dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 64), (unsigned)d.batch);
+            spmm_kernel<V, PA, PB, S, 2, H, false, E><<<grid, 64, 0, s>>>(p);
+        }
+        return (int)cudaGetLastError();
     } else {
-        dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 64), (unsigned)d.batch);
-        if (f16) spmm_kernel<V, PA, PB, S, 2, H, true, E><<<grid, 64, 0, s>>>(p);
-        else spmm_kernel<V, PA, PB, S, 2, H, false, E><<<grid, 64, 0, s>>>(p);
+        const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
+        const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
+        if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
+            return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");
+        if (d.kernel_variant != MC_KERNEL_PER_ROW && stream_ok) {
+            if (d.n % 128 == 0)
+                return f16 ? spmm_launch_stream<V, PA, PB, S, H, 4, true, E>(d, p, s)
+                           : spmm_launch_stream<V, PA, PB, S, H, 4, false, E>(d, p, s);
+            return f16 ? spmm_launch_stream<V, PA, PB, S, H, 2, true, E>(d, p, s)
+                       : spmm_launch_stream<V, PA, PB, S, H, 2, false, E>(d, p, s);
+        }
+        if (d.n % 128 == 0) {
+            dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 128), (unsigned)d.batch);
+            if (f16) spmm_kernel<V, PA, PB, S, 4, H, true, E><<<grid, 128, 0, s>>>(p);
+            else spmm_kernel<V, PA, PB, S, 4, H, false, E><<<grid, 128, 0, s>>>(p);
+        } else {
+            dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 64), (unsigned)d.batch);
+            if (f16) spmm_kernel<V, PA, PB, S, 2, H, true, E><<<grid, 64, 0, s>>>(p);
+            else spmm_kernel<V, PA, PB, S, 2, H, false, E><<<grid, 64, 0, s>>>(p);
+        }
+        return (int)cudaGetLastError();
     }
-    return (int)cudaGetLastError();
 }
 
 template <int PA, int PB>

@@ -154,6 +154,12 @@ __device__ __forceinline__ uint32_t lds32(const void* p)
     asm volatile("ld.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)));
     return v;
 }
+__device__ __forceinline__ uint2 lds64(const void* p)
+{
+    uint2 v;
+    asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(smem_u32(p)));
+    return v;
+}
 __device__ __forceinline__ uint32_t lds16(const void* p)
 {
     unsigned short v;

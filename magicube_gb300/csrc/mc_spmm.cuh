@@ -20,7 +20,10 @@
 //    fragment (4-bit B rows are unpacked to bytes on the way).
 //  * 16-bit lhs values run as two byte planes (u8 low, s8/u8 high) recombined
 //    by an exact shift-add; 4-bit planes are merged/unpacked to int8 in
-//    registers (sm_103a's fast integer MMA path is the 8-bit one).
+//    registers (sm_103a's fast integer MMA path is the 8-bit one).  16-bit B
+//    rows (the reference's wmmaSpmm_16b) are split into low and high byte
+//    planes in registers as well: four byte-plane products per step,
+//    recombined with shifts of 0, 8, 8 and 16 bits.
 //  * Accumulation wraps modulo 2^32 (no .satfinite): results equal the CPU
 //    oracle bit for bit for every input.
 #pragma once
@@ -71,16 +74,21 @@ __device__ __forceinline__ int vword16(int g, int t, int bp)
     else return bp * V * 16 + g * 16 + 4 * t;
 }
 
-// Shared-memory geometry of one staged gathered-row slice.
+// Shared-memory geometry of one staged gathered-row slice.  16-bit B: row
+// slices of 64 bytes per warp; the 64-bit reads of a half-warp (4 rows x 32
+// bytes) land in 8 distinct 16-byte bank groups through the XOR of the chunk
+// index with bits 2-3 of the row.
 template <int PREB, int WARPS>
 struct RhsSmem {
     static constexpr int RB = WARPS * 32 * PREB / 8;  // packed bytes per row slice
     static constexpr int CH = RB / 16;                // 16-byte chunks per row slice
-    static constexpr int STRIDE = (PREB == 8) ? (CH == 8 ? 128 : 80) : (CH == 4 ? 64 : 48);
+    static constexpr int STRIDE = (PREB == 16) ? RB : (PREB == 8) ? (CH == 8 ? 128 : 80) : (CH == 4 ? 64 : 48);
     static constexpr int STAGE_BYTES = 32 * STRIDE;
     __device__ __forceinline__ static int swz(int r, int c)
     {
-        if constexpr (PREB == 8) {
+        if constexpr (PREB == 16) {
+            return c ^ (((r >> 2) & 3) << 1);
+        } else if constexpr (PREB == 8) {
             if constexpr (CH == 8) return c ^ (((r >> 2) & 3) << 1);
             else return c ^ (((r >> 3) & 1) << 1);
         } else {
@@ -115,6 +123,8 @@ spmm_kernel(const SpmmParams p)
     constexpr int THREADS = WARPS * 32;
     constexpr int CHUNKS_PER_THREAD = (32 * S::CH) / THREADS;  // 2 for 8-bit B, 1 for 4-bit B
     constexpr int BP = L::BYTE_PLANES;
+    constexpr int BB = PREB == 16 ? 2 : 1;  // byte planes of B
+    static_assert(!(F16 && PREB == 16), "16-bit B runs on the int8 tensor path");
     constexpr int PLANE_BYTES = V * L::VCHUNK * L::PLANE_BITS / 8;
     constexpr int CHUNK_BYTES = PLANE_BYTES * L::PLANES;
 
@@ -202,14 +212,20 @@ spmm_kernel(const SpmmParams p)
         }
     };
 
-    int acc[BP][2][4];
+    int acc[BP * BB][2][4];   // [bp * BB + bb]: values byte plane bp x B byte plane bb
     float facc[BP][2][4];
+#pragma unroll
+    for (int k = 0; k < BP * BB; ++k)
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[k][m][e] = 0;
 #pragma unroll
     for (int bp = 0; bp < BP; ++bp)
 #pragma unroll
         for (int m = 0; m < 2; ++m)
 #pragma unroll
-            for (int e = 0; e < 4; ++e) { acc[bp][m][e] = 0; facc[bp][m][e] = 0.f; }
+            for (int e = 0; e < 4; ++e) facc[bp][m][e] = 0.f;
 
     // Pipeline prologue: column indices run one stage ahead of the copies.
     int cnext[CHUNKS_PER_THREAD];
@@ -242,6 +258,44 @@ spmm_kernel(const SpmmParams p)
         load_vals(s + 1, vnext);
 
         const uint8_t* st = rhs_s + (s % STAGES) * S::STAGE_BYTES;
+        if constexpr (PREB == 16) {
+            // Columns ncol..ncol+3 of rows 16h+4t+i: 8 bytes, split into the
+            // low and high bytes of the four 16-bit lanes, then byte-transposed.
+            uint32_t tb[2][2][4];  // [B byte plane][h][i]
+            const int byte = 2 * ncol;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int r = 16 * h + 4 * t + i;
+                    const uint2 w = lds64(st + r * S::STRIDE + S::swz(r, byte >> 4) * 16 + (byte & 15));
+                    tb[0][h][i] = prmt(w.x, w.y, 0x6420);
+                    tb[1][h][i] = prmt(w.x, w.y, 0x7531);
+                }
+                transpose4x4(tb[0][h]);
+                transpose4x4(tb[1][h]);
+            }
+#pragma unroll
+            for (int bp = 0; bp < BP; ++bp) {
+                const bool top = (bp == BP - 1);
+#pragma unroll
+                for (int bb = 0; bb < 2; ++bb) {
+                    int (&a)[2][4] = acc[bp * 2 + bb];
+                    const uint32_t (&T)[2][4] = tb[bb];
+#define MC_MMA16(AS, VS)                                                                                  \
+    mma_k32<AS, VS>(a[0], T[0][0], T[0][1], T[1][0], T[1][1], vcur[bp][0], vcur[bp][1]);                 \
+    mma_k32<AS, VS>(a[1], T[0][2], T[0][3], T[1][2], T[1][3], vcur[bp][0], vcur[bp][1]);
+                    // Only the high byte plane of each operand is signed.
+                    if (SIGNED && bb == 1 && top) { MC_MMA16(true, true) }
+                    else if (SIGNED && bb == 1) { MC_MMA16(true, false) }
+                    else if (SIGNED && top) { MC_MMA16(false, true) }
+                    else { MC_MMA16(false, false) }
+#undef MC_MMA16
+                }
+            }
+#pragma unroll
+            for (int bp = 0; bp < BP; ++bp) { vcur[bp][0] = vnext[bp][0]; vcur[bp][1] = vnext[bp][1]; }
+        } else {
         uint32_t tr[2][4];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -318,23 +372,27 @@ spmm_kernel(const SpmmParams p)
         }
 #pragma unroll
         for (int bp = 0; bp < BP; ++bp) { vcur[bp][0] = vnext[bp][0]; vcur[bp][1] = vnext[bp][1]; }
+        }  // PREB != 16
     }
     cp_async_wait<0>();
 
     // Epilogue.  acc[.][m][e]: column ncol + 2m + (e >> 1), vector lane 2t + (e & 1).
+    // Byte-plane products recombine as sum acc[bp][bb] << 8 (bp + bb), mod 2^32.
     int res[2][4];
 #pragma unroll
     for (int e2 = 0; e2 < 2; ++e2) {
         // vector lane v = 2t + e2, columns ncol .. ncol+3
-        int c4[4] = {acc[0][0][e2], acc[0][0][2 + e2], acc[0][1][e2], acc[0][1][2 + e2]};
-        if constexpr (BP == 2) {
-            int h4[4] = {acc[1][0][e2], acc[1][0][2 + e2], acc[1][1][e2], acc[1][1][2 + e2]};
+        uint32_t c4[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                c4[q] = (int)((uint32_t)c4[q] + ((uint32_t)h4[q] << 8));
+        for (int k = 0; k < BP * BB; ++k) {
+            const int sh = 8 * (k / BB + k % BB);
+            const uint32_t h4[4] = {(uint32_t)acc[k][0][e2], (uint32_t)acc[k][0][2 + e2], (uint32_t)acc[k][1][e2],
+                                    (uint32_t)acc[k][1][2 + e2]};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) c4[q] += h4[q] << sh;
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) res[e2][q] = c4[q];
+        for (int q = 0; q < 4; ++q) res[e2][q] = (int)c4[q];
     }
 #pragma unroll
     for (int e2 = 0; e2 < 2; ++e2) {

@@ -22,7 +22,7 @@ import ctypes
 import torch
 
 from . import _lib
-from .formats import VALUES_PACKED, VALUES_SOFTMAX, spmm_chunk
+from .formats import VALUES_PACKED, VALUES_SOFTMAX, lane_bits, spmm_chunk
 from .ops import DeviceSddmmMask, DeviceSpmmLhs
 
 
@@ -71,7 +71,7 @@ def pack_spmm_values(row_offsets: torch.Tensor, pairs: torch.Tensor, aligned_nnz
     if values.dtype != torch.uint8 or not values.is_cuda:
         raise TypeError("values must be a uint8 CUDA tensor")
     v = values.contiguous()
-    nbytes = capacity_slots * vec_length * lhs_bits // 8
+    nbytes = capacity_slots * vec_length * lane_bits(lhs_bits) // 8
     out = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=ro.device)
     _lib.check(_lib.lib().mcDevicePackSpmmValues(ro.numel() - 1, vec_length, lhs_bits, rhs_bits, ro.data_ptr(),
                                                  _ptr(pairs), aligned_nnz.data_ptr(), _ptr(v), out.data_ptr(), nbytes,
@@ -111,7 +111,7 @@ def _pack(ro: torch.Tensor, ci: torch.Tensor, values: torch.Tensor | None, vec_l
     n = torch.empty(1, dtype=torch.int32, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     cols = torch.empty(max(bound, 1), dtype=torch.int32, device=dev)
-    nbytes = bound * vec_length * lhs_bits // 8
+    nbytes = bound * vec_length * lane_bits(lhs_bits) // 8
     vals = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=dev) if lhs_bits else None
     ri = (torch.empty(max(m_vec, 1), dtype=torch.int32, device=dev) if sort_rows
           else torch.arange(max(m_vec, 1), dtype=torch.int32, device=dev))
@@ -141,7 +141,7 @@ def prepare_spmm(row_offsets: torch.Tensor, col_indices: torch.Tensor, values: t
                                              chunk == 32 and layout == VALUES_PACKED, layout, sort_rows, bound)
     aligned = _finish(n, status, sync, bound)
     if sync:
-        cols, vals = cols[:aligned], vals[:aligned * vec_length * lhs_bits // 8]
+        cols, vals = cols[:aligned], vals[:aligned * vec_length * lane_bits(lhs_bits) // 8]
     if cols.numel() == 0:
         cols = torch.full((1,), -1, dtype=torch.int32, device=ro.device)
     if vals.numel() == 0:

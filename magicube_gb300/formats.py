@@ -49,6 +49,12 @@ def spmm_chunk(lhs_bits: int, rhs_bits: int) -> int:
     return 32 if (lhs_bits == 4 or rhs_bits == 4) else 16
 
 
+def lane_bits(lhs_bits: int) -> int:
+    """Bits per stored value lane: 12-bit values live in 16-bit lanes (the
+    reference's 12-bit containers, SpMM/SpMM/spmm_benchmark.cpp:810-822)."""
+    return 16 if lhs_bits == 12 else lhs_bits
+
+
 def align_row_offsets(mask: VectorSparse, alignment: int) -> tuple[np.ndarray, int]:
     ro = np.ascontiguousarray(mask.row_offsets, dtype=np.int32)
     pairs = np.zeros(2 * mask.m_vec, dtype=np.int32)
@@ -73,10 +79,11 @@ VALUES_PACKED, VALUES_SOFTMAX = 0, 1
 
 def pack_spmm_values(mask: VectorSparse, pairs: np.ndarray, aligned_nnz: int, values: np.ndarray,
                      lhs_bits: int, rhs_bits: int, layout: int = VALUES_PACKED) -> np.ndarray:
-    """values: uint8 array of nnz_vec * V * lhs_bits / 8 bytes (lane v at bit v*lhs_bits)."""
+    """values: uint8 array of nnz_vec * V * lane_bits(lhs_bits) / 8 bytes (lane v
+    at bit v * lane_bits(lhs_bits))."""
     ro = np.ascontiguousarray(mask.row_offsets, dtype=np.int32)
     v = np.ascontiguousarray(values, dtype=np.uint8)
-    nbytes = aligned_nnz * mask.vec_length * lhs_bits // 8
+    nbytes = aligned_nnz * mask.vec_length * lane_bits(lhs_bits) // 8
     out = np.empty(max(nbytes, 4), dtype=np.uint8)
     _lib.check(_lib.lib().mcPackSpmmValuesEx(mask.m_vec, mask.vec_length, lhs_bits, rhs_bits, _ptr(ro),
                                              _ptr(pairs), aligned_nnz, _ptr(v) if v.size else None, _ptr(out), layout),

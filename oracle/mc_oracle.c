@@ -90,7 +90,13 @@ void mco_spmm_host(const uint8_t* values, const int32_t* rhs, int32_t* out,
             for (int av = 0; av < V; ++av) {
                 const int row = i * V + av;
                 uint32_t raw = lane_u(vec, av, preA) & cut_mask;
-                int32_t a = (mode == MCO_SIGNED) ? sext(raw, preA_cut) : (int32_t)raw;
+                /* MCO_LITERAL, L16-R16: the reference keeps those values in
+                 * `short` containers (spmm_benchmark.cpp:829-831), where
+                 * maskA and maskA_cut are (short)0xFFFF == -1 (:77-79), so
+                 * the lane is used sign-extended (:96). */
+                int32_t a = (mode == MCO_SIGNED || (mode == MCO_LITERAL && preA == 16 && preB == 16))
+                                ? sext(raw, preA_cut)
+                                : (int32_t)raw;
                 const uint32_t* brow = (const uint32_t*)rhs + (size_t)col * ints_per_row;
                 uint32_t* crow = acc + (size_t)row * N;
                 for (int n = 0; n < ints_per_row; ++n) {

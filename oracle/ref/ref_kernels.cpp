@@ -93,9 +93,11 @@ STUB(wmmaSpmm_8b4b, 8, 4)
 STUB(wmmaSpmm_16b4b, 16, 4)
 STUB(wmmaSpmm_8b, 8, 8)
 STUB(wmmaSpmm_16b8b, 16, 8)
-STUB(wmmaSpmm_12b4b, 0, 0)
-STUB(wmmaSpmm_12b8b, 0, 0)
-STUB(wmmaSpmm_16b, 0, 0)
+// The 12-bit variants receive the 16-bit layouts with the top 4 bits clear
+// (spmm_benchmark.cpp:288-358): decoded as 16-bit values.
+STUB(wmmaSpmm_12b4b, 16, 4)
+STUB(wmmaSpmm_12b8b, 16, 8)
+STUB(wmmaSpmm_16b, 16, 16)
 #undef STUB
 }  // namespace spmm
 #endif

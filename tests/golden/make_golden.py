@@ -38,7 +38,8 @@ sys.path.insert(0, str(ROOT))
 
 from magicube_gb300 import smtx, synth  # noqa: E402
 
-SPMM_CASES = [(pa, pb, V) for (pa, pb) in [(4, 4), (8, 4), (16, 4), (8, 8), (16, 8)] for V in (2, 4, 8)]
+SPMM_PAIRS = [(4, 4), (8, 4), (16, 4), (8, 8), (16, 8), (12, 4), (12, 8), (16, 16)]
+SPMM_CASES = [(pa, pb, V) for (pa, pb) in SPMM_PAIRS for V in (2, 4, 8)]
 SDDMM_CASES = [(b, V) for b in (4, 8, 16) for V in (2, 4, 8)]
 # (TypeA bytes, scaleA) per (preA, preB, V): the dispatch table of the
 # reference's main (SpMM/SpMM/spmm_benchmark.cpp:805-831).
@@ -46,7 +47,15 @@ TYPEA = {(4, 4, 8): (4, 1), (4, 4, 4): (2, 1), (4, 4, 2): (1, 1),
          (8, 4, 8): (8, 1), (8, 4, 4): (4, 1), (8, 4, 2): (2, 1),
          (16, 4, 8): (8, 2), (16, 4, 4): (8, 1), (16, 4, 2): (4, 1),
          (8, 8, 8): (8, 1), (8, 8, 4): (4, 1), (8, 8, 2): (2, 1),
-         (16, 8, 8): (8, 2), (16, 8, 4): (8, 1), (16, 8, 2): (4, 1)}
+         (16, 8, 8): (8, 2), (16, 8, 4): (8, 1), (16, 8, 2): (4, 1),
+         (12, 4, 8): (8, 2), (12, 4, 4): (8, 1), (12, 4, 2): (4, 1),
+         (12, 8, 8): (8, 2), (12, 8, 4): (8, 1), (12, 8, 2): (4, 1),
+         (16, 16, 8): (2, 8), (16, 16, 4): (2, 4), (16, 16, 2): (2, 2)}
+
+
+def lane_bits(pa: int) -> int:
+    """Bits per stored lane: the reference keeps 12-bit values in 16-bit containers."""
+    return 16 if pa == 12 else pa
 
 
 def _read(d: Path, name: str, dtype) -> np.ndarray:
@@ -110,14 +119,15 @@ def routine_spmm(lib: ctypes.CDLL, pa: int, pb: int, V: int, seed: int) -> dict:
     K, N = 64, 64
     mask = synth.lengths_mask([0, 3, 17, 40, 64, 9], K, V, seed=seed)
     tb, scaleA = TYPEA[(pa, pb, V)]
-    vals = synth.random_bytes(mask.nnz_vec * V * pa // 8, seed + 1)
+    lb = lane_bits(pa)
+    vals = synth.random_bytes(mask.nnz_vec * V * lb // 8, seed + 1)
     rhs = synth.random_bytes(K * N * pb // 8, seed + 2)
     C = np.zeros(mask.rows * N, dtype=np.int32)
     buf = np.ascontiguousarray(vals.copy())
     rb = np.ascontiguousarray(rhs.copy())
     ro = np.ascontiguousarray(mask.row_offsets.copy())
     ci = np.ascontiguousarray(mask.col_indices.copy())
-    lib.mcref_compute_ref_integers(tb, buf.ctypes.data, rb.ctypes.data, C.ctypes.data, mask.rows, K, N, pa, pa, pb, V,
+    lib.mcref_compute_ref_integers(tb, buf.ctypes.data, rb.ctypes.data, C.ctypes.data, mask.rows, K, N, lb, pa, pb, V,
                                    ro.ctypes.data, ci.ctypes.data if ci.size else None, mask.m_vec, scaleA)
     return {"m_vec": mask.m_vec, "V": V, "K": K, "N": N, "preA": pa, "preB": pb,
             "row_offsets": mask.row_offsets, "col_indices": mask.col_indices, "values": vals, "rhs": rhs, "out": C}

@@ -21,9 +21,11 @@ def names(prefix: str) -> list[str]:
 def unpack_spmm_values(dev: np.ndarray, pairs: np.ndarray, csr_offsets: np.ndarray, V: int, pa: int,
                        pb: int) -> np.ndarray:
     """Invert the SpMM device value layout back to per-vector packed values
-    (V lanes of pa bits each, lane v at bit v*pa)."""
+    (V lanes of pa bits each, lane v at bit v*pa; 12-bit values in 16-bit
+    lanes)."""
     mma_k = 32 if (pa == 4 or pb == 4) else 16
     plane_bits = 4 if mma_k == 32 else 8
+    pa = 16 if pa == 12 else pa  # 12-bit values: 16-bit lanes and layouts (top bits clear)
     planes = pa // plane_bits
     plane_bytes = V * mma_k * plane_bits // 8
     chunk_bytes = plane_bytes * planes
@@ -59,3 +61,8 @@ def unpack_spmm_values(dev: np.ndarray, pairs: np.ndarray, csr_offsets: np.ndarr
             out[2 * e] = x & 0xFF
             out[2 * e + 1] = (x >> 8) & 0xFF
     return out
+
+
+def lane_bits(pa: int) -> int:
+    """Bits per stored lane (12-bit values live in 16-bit containers)."""
+    return 16 if pa == 12 else pa

@@ -17,7 +17,7 @@ def bins(cuda):
     return build.BIN
 
 
-@pytest.mark.parametrize("preA,preB", [(4, 4), (8, 4), (16, 4), (8, 8), (16, 8)])
+@pytest.mark.parametrize("preA,preB", [(4, 4), (8, 4), (12, 4), (16, 4), (8, 8), (12, 8), (16, 8), (16, 16)])
 @pytest.mark.parametrize("V", [2, 8])
 @pytest.mark.parametrize("sort", [0, 1])
 def test_spmm_benchmark_cli(bins, tmp_path, preA, preB, V, sort):

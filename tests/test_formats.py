@@ -55,3 +55,21 @@ def test_empty_matrix_packs():
     m = synth.lengths_mask([0, 0, 0], 64, 4, seed=1)
     h = formats.prepare_spmm(m, np.zeros(0, np.uint8), 8, 8)
     assert h.aligned_nnz == 0 and h.values.size == 0
+
+
+@pytest.mark.parametrize("pa,pb", [(12, 4), (12, 8), (16, 16)])
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_pack_then_decode_wide_pairs(pa, pb, V):
+    """12-bit values (16-bit lanes, top 4 bits dropped by the packer) and
+    16 x 16: packer + the oracle's device-layout decoder == oracle on the
+    original layout."""
+    K, N = 128, 64
+    m = synth.lengths_mask([0, 1, 31, 32, 33, 100, 7], K, V, seed=pa + pb + V)
+    vals = synth.random_bytes(m.nnz_vec * V * 2, 1)
+    rhs = synth.random_bytes(K * N * pb // 8, 2)
+    h = formats.prepare_spmm(m, vals, pa, pb)
+    modes = (oracle.UNSIGNED,) if pa == 12 else (oracle.UNSIGNED, oracle.SIGNED)
+    for mode in modes:
+        a = oracle.spmm_host(vals, rhs, m.row_offsets, m.col_indices, m.m_vec, V, K, N, 16, pb, mode, preA_cut=pa)
+        b = oracle.spmm_device(h.row_offsets, h.col_indices, h.values, rhs, m.m_vec, V, K, N, 16, pb, mode)
+        np.testing.assert_array_equal(a, b)

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import oracle
-from golden_util import load, names, unpack_spmm_values
+from golden_util import lane_bits, load, names, unpack_spmm_values
 from magicube_gb300 import formats
 from magicube_gb300.formats import VectorSparse
 
@@ -14,8 +14,9 @@ def test_oracle_literal_equals_reference_spmm_routine(name):
     """compute_ref_integers (reference, compiled from its sources) on full-range
     random data == the oracle's literal mode, bit for bit."""
     d = load(name)
+    pa = int(d["preA"])
     got = oracle.spmm_host(d["values"], d["rhs"], d["row_offsets"], d["col_indices"], int(d["m_vec"]), int(d["V"]),
-                           int(d["K"]), int(d["N"]), int(d["preA"]), int(d["preB"]), oracle.LITERAL)
+                           int(d["K"]), int(d["N"]), lane_bits(pa), int(d["preB"]), oracle.LITERAL, preA_cut=pa)
     np.testing.assert_array_equal(got.ravel(), d["out"])
 
 
@@ -24,10 +25,11 @@ def test_reference_top_lane_quirk_is_visible(name):
     """On full-range data the reference routine's sign-extended top rhs lane
     makes it differ from purely unsigned lanes (the GPU kernels' semantics)."""
     d = load(name)
+    pa = int(d["preA"])
     args = (d["values"], d["rhs"], d["row_offsets"], d["col_indices"], int(d["m_vec"]), int(d["V"]), int(d["K"]),
-            int(d["N"]), int(d["preA"]), int(d["preB"]))
-    lit = oracle.spmm_host(*args, oracle.LITERAL)
-    uns = oracle.spmm_host(*args, oracle.UNSIGNED)
+            int(d["N"]), lane_bits(pa), int(d["preB"]))
+    lit = oracle.spmm_host(*args, oracle.LITERAL, preA_cut=pa)
+    uns = oracle.spmm_host(*args, oracle.UNSIGNED, preA_cut=pa)
     if int(d["row_offsets"][-1]) > 0:
         assert not np.array_equal(lit, uns)
 
@@ -56,8 +58,8 @@ def test_packer_and_oracle_against_reference_spmm_program(name):
     np.testing.assert_array_equal(formats.sorted_row_swizzle(mask), d["row_indices"])
     orig = unpack_spmm_values(d["values"], pairs, mask.row_offsets, V, pa, pb)
     np.testing.assert_array_equal(formats.pack_spmm_values(mask, pairs, n, orig, pa, pb), d["values"])
-    got = oracle.spmm_host(orig, d["rhs"], mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
-                           oracle.LITERAL)
+    got = oracle.spmm_host(orig, d["rhs"], mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, lane_bits(pa),
+                           pb, oracle.LITERAL, preA_cut=pa)
     np.testing.assert_array_equal(got.ravel(), d["out"])
 
 

@@ -10,7 +10,8 @@ from magicube_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
 
-SPMM_FN = {(4, 4): "4b", (8, 4): "8b4b", (16, 4): "16b4b", (8, 8): "8b", (16, 8): "16b8b"}
+SPMM_FN = {(4, 4): "4b", (8, 4): "8b4b", (16, 4): "16b4b", (8, 8): "8b", (16, 8): "16b8b", (12, 4): "12b4b",
+           (12, 8): "12b8b", (16, 16): "16b"}
 SDDMM_FN = {4: "4b", 8: "8b", 16: "16b"}
 
 

@@ -320,12 +320,14 @@ def run_gpu(args) -> None:
                               (args.mma, 1, "per_row_kernel")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
-    attention = serving_res = packer = projection = None
+    attention = serving_res = packer = projection = competitors = None
     if not args.headline_only and rank == 0:
         torch.cuda.empty_cache()
         packer = packer_suite(args, dev, peaks)
         torch.cuda.empty_cache()
         projection = projection_suite(args, dev, peaks)
+        torch.cuda.empty_cache()
+        competitors = competitor_suite(args, dev)
         torch.cuda.empty_cache()
         attention = attention_suite(args, dev)
         torch.cuda.empty_cache()
@@ -366,6 +368,7 @@ def run_gpu(args) -> None:
             "serving": serving_res,
             "device_packer": packer,
             "qkv_projection": projection,
+            "competitors": competitors,
         }
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
@@ -553,6 +556,103 @@ def projection_suite(args, dev, peaks) -> dict:
             "launches": {"fused": 1, "unfused": "F.linear + permute copy + mcQuantize"}}
 
 
+def competitor_suite(args, dev) -> dict:
+    """The reference's competitor baselines (baselines/spmm_benchmark.cpp:
+    cuBLAS int8 / fp16 dense GEMM, cuSPARSE fp16 CSR SpMM; cuSPARSE SDDMM) on
+    this GPU through torch (cuBLASLt, cuSPARSE), against this library's kernels
+    called once per matrix, on the two headline shapes: SpMM A 1024 x 1024 (V=8
+    vectors at sparsity 0.9) x B 1024 x 256, and SDDMM A, B 4096 x 64 with a
+    4096 x 4096 V=8 mask at sparsity 0.9.  Times are device microseconds per
+    matrix: 20 calls captured in a CUDA graph, replayed, CUDA events around
+    the replay (the host launch overhead of single calls would otherwise hide
+    kernels of a few microseconds); "eager" marks a call whose capture failed
+    and that was timed call by call instead."""
+    import torch
+
+    from magicube_gb300 import formats, ops, synth
+    rng = np.random.default_rng(5)
+    modes = {}
+
+    def us(fn, name):
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            try:
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=side):
+                    for _ in range(20):
+                        fn()
+                ms = time_cuda(g.replay, 10, 2, side)
+                modes[name] = "graph"
+                return statistics.median(ms) * 1e3 / 20
+            except Exception:  # noqa: BLE001 -- fall back to per-call timing
+                torch.cuda.synchronize()
+                modes[name] = "eager"
+                return statistics.median(time_cuda(fn, 50, 5, side)) * 1e3
+
+    def csr_of(mask, ncols, dtype, values=None):
+        # element-level CSR of the vector-sparse matrix (each vector = V rows)
+        V = mask.vec_length
+        rows, cols = [], []
+        for i in range(mask.m_vec):
+            c = mask.col_indices[mask.row_offsets[i]:mask.row_offsets[i + 1]]
+            for v in range(V):
+                rows.append(np.full(c.size, i * V + v))
+                cols.append(c)
+        r = np.concatenate(rows)
+        c = np.concatenate(cols)
+        vals = torch.from_numpy(values if values is not None else rng.standard_normal(r.size).astype(np.float32))
+        coo = torch.sparse_coo_tensor(torch.from_numpy(np.stack([r, c])), vals, (mask.m_vec * V, ncols))
+        return coo.to(dtype).to(dev).to_sparse_csr()
+
+    res = {}
+    # ---- SpMM ----
+    M = K = 1024
+    N = 256
+    mask = synth.uniform_mask(M // VEC, K, VEC, SPARSITY, seed=7)
+    vals = rng.integers(0, 256, size=mask.nnz_vec * VEC, dtype=np.uint8)
+    h = formats.prepare_spmm(mask, vals, 8, 8)
+    d = ops.DeviceSpmmLhs.from_host(h, dev)
+    rhs8 = torch.from_numpy(rng.integers(0, 256, size=K * N, dtype=np.uint8)).to(dev)
+    out = torch.empty((M, N), dtype=torch.int32, device=dev)
+    a8 = torch.randint(-128, 128, (M, K), dtype=torch.int8, device=dev)
+    b8 = torch.randint(-128, 128, (K, N), dtype=torch.int8, device=dev)
+    a16, b16 = a8.half(), b8.half()
+    acsr = csr_of(mask, K, torch.float16)
+    res["spmm_1024x1024x256_V8_s0.9"] = {
+        "magicube_L8R8_us": us(lambda: ops.spmm(d, rhs8, N, signed=True, out=out), "spmm_magicube"),
+        "cublas_int8_dense_us": us(lambda: torch._int_mm(a8, b8), "spmm_cublas_int8"),
+        "cublas_fp16_dense_us": us(lambda: torch.mm(a16, b16), "spmm_cublas_fp16"),
+        "cusparse_fp16_csr_us": us(lambda: torch.mm(acsr, b16), "spmm_cusparse"),
+    }
+    # ---- SDDMM ----
+    smask, hm, lhs_h, rhs_h = sddmm_workload(8, 8, 1)
+    dm = ops.DeviceSddmmMask.from_host(hm, dev)
+    lhs = torch.from_numpy(lhs_h).to(dev)
+    rhs = torch.from_numpy(rhs_h).to(dev)
+    sout = torch.empty(hm.aligned_nnz * VEC, dtype=torch.int32, device=dev)
+    qa = torch.randint(-128, 128, (SEQ, HEAD_DIM), dtype=torch.int8, device=dev)
+    qb = torch.randint(-128, 128, (HEAD_DIM, SEQ), dtype=torch.int8, device=dev)
+    fa, fb = qa.half(), qb.half()
+    smask_csr = csr_of(smask, SEQ, torch.float32, np.ones(smask.nnz_vec * VEC, np.float32))
+    fa32, fb32 = qa.float(), qb.float()
+    res["sddmm_4096x4096x64_V8_s0.9"] = {
+        "magicube_L8R8_us": us(lambda: ops.sddmm(dm, lhs, rhs, HEAD_DIM, 8, 8, signed=True, out=sout),
+                               "sddmm_magicube"),
+        "cublas_int8_dense_us": us(lambda: torch._int_mm(qa, qb), "sddmm_cublas_int8"),
+        "cublas_fp16_dense_us": us(lambda: torch.mm(fa, fb), "sddmm_cublas_fp16"),
+        "cusparse_fp32_sddmm_us": us(lambda: torch.sparse.sampled_addmm(smask_csr, fa32, fb32), "sddmm_cusparse"),
+    }
+    for v in res.values():
+        base = v["magicube_L8R8_us"]
+        v["speedup_vs"] = {k[:-3]: round(x / base, 2) for k, x in v.items() if k.endswith("_us") and k != "magicube_L8R8_us"}
+    res["timing"] = modes
+    return res
+
+
 def formats_align(mask, alignment):
     from magicube_gb300 import formats
     pairs, n = formats.align_row_offsets(mask, alignment)
@@ -576,11 +676,18 @@ def serving_suite(args, dev) -> dict:
     serving.serve_sequential(enc, serving.make_requests(2, 0.0, seed=98), device=dev)
     out = []
     for rate in args.serving_rates:
+        # Each server first serves the same request set unmeasured, so both
+        # measured runs see warmed allocator pools for the same shapes.
+        serving.ContinuousBatchingServer(enc, max_inflight=3, overlap_tokens=args.serving_overlap_tokens,
+                                         device=dev).serve(serving.make_requests(args.serving_requests, rate, seed=5))
         reqs = serving.make_requests(args.serving_requests, rate, seed=5)
-        srv = serving.ContinuousBatchingServer(enc, max_inflight=3, device=dev)
+        srv = serving.ContinuousBatchingServer(enc, max_inflight=3, overlap_tokens=args.serving_overlap_tokens,
+                                               device=dev)
         cb = srv.serve(reqs)
+        serving.serve_sequential(enc, serving.make_requests(args.serving_requests, rate, seed=5), device=dev)
         seq = serving.serve_sequential(enc, serving.make_requests(args.serving_requests, rate, seed=5), device=dev)
-        out.append({"arrival_rate": rate, "continuous": cb, "sequential": seq,
+        out.append({"arrival_rate": rate, "overlap_tokens": args.serving_overlap_tokens, "continuous": cb,
+                    "sequential": seq,
                     "mean_batch": float(np.mean([len(b) for b in srv.batches])),
                     "req_per_s_ratio": cb["req_per_s"] / seq["req_per_s"]})
     return {"config": "2-layer sparse encoder, hidden 256, 4x64 heads, FFN 1024, sparsity 0.95, "
@@ -689,6 +796,8 @@ def main() -> None:
     ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")], default=[200.0, 2000.0],
                     help="Poisson arrival rates (requests/s) of the serving runs")
     ap.add_argument("--serving-requests", type=int, default=48, help="requests per serving run (0 skips it)")
+    ap.add_argument("--serving-overlap-tokens", type=int, default=8192,
+                    help="queued tokens at which the server overlaps a new batch with running ones")
     ap.add_argument("--mma", choices=["int8", "f16"], default="int8",
                     help="tensor path (both are bit-exact; see include/magicube_gb300.h)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -1,14 +1,15 @@
 """Continuous-batching server for the sparse encoder.
 
 Requests carry a sequence of their own length and (per encoder layer) their
-own vector-sparse attention mask.  On arrival a request's tokens and masks are
-copied to the device once and stay resident until it completes.  The
-scheduler admits queued requests into a new batch whenever an in-flight slot
-is free and the free HBM covers the batch's estimated working set; a batch
+own vector-sparse attention mask.  On admission a request's tokens and the
+plain CSR of its masks are copied to the device once (the masks are packed
+there by the GPU packer) and stay resident until it completes.  The scheduler
+admits queued requests into a new batch when no batch is in flight, or, for
+overlap, when the queued tokens reach a threshold and an in-flight slot is
+free, always within the free HBM (the batch's estimated working set); a batch
 is one block-diagonal forward pass over the admitted requests (the token
 tensors concatenated, the masks stacked into one mask per layer) launched on
-its own CUDA stream, so batches that are admitted while others still run
-overlap on the device.  Completion is observed through CUDA events, and each
+its own CUDA stream.  Completion is observed through CUDA events, and each
 request's latency is (completion - arrival).
 
 serve_sequential is the baseline: one request at a time, in arrival order,
@@ -23,7 +24,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from . import formats, synth
+from . import device_format, formats, synth
 from .batched import AttentionMaskDev
 from .formats import VectorSparse
 
@@ -65,18 +66,25 @@ def make_requests(n: int, rate: float, hidden: int = 256, layers: int = 2, V: in
 
 
 def _upload(req: Request, alignment: int, device) -> None:
-    """Copy a request's tokens and aligned masks to the device (once)."""
+    """Copy a request's tokens and the plain CSR of its masks to the device
+    (once) and pack the masks there (mcDevicePack, no host round trip: slot
+    arrays sized by the upper bound nnz + m_vec * (alignment - 1))."""
     if req.dev:
         return
-    req.dev["x"] = req.x.to(device, non_blocking=True)
+    dev = torch.device(device)
+    req.dev["x"] = req.x.to(dev, non_blocking=True)
     per_layer = []
     for m in req.masks:
-        pairs, n = formats.align_row_offsets(m, alignment)
-        cols = formats.pad_column_indices(m, pairs, n, shuffle8=False)
-        ri = formats.sorted_row_swizzle(m)
-        per_layer.append((torch.from_numpy(pairs).to(device, non_blocking=True),
-                          torch.from_numpy(cols).to(device, non_blocking=True),
-                          torch.from_numpy(ri).to(device, non_blocking=True), m.m_vec, n))
+        if dev.type == "cuda":
+            ro = torch.from_numpy(m.row_offsets).to(dev, non_blocking=True)
+            ci = torch.from_numpy(m.col_indices).to(dev, non_blocking=True)
+            dm = device_format.prepare_sddmm(ro, ci, m.vec_length, m.ncols, alignment=alignment, sync=False)
+            per_layer.append((dm.row_offsets, dm.col_indices, dm.row_indices, m.m_vec, dm.aligned_nnz))
+        else:  # host tensors: the library's host packer (exact slot counts)
+            pairs, n = formats.align_row_offsets(m, alignment)
+            cols = formats.pad_column_indices(m, pairs, n, shuffle8=False)
+            per_layer.append((torch.from_numpy(pairs), torch.from_numpy(cols),
+                              torch.from_numpy(formats.sorted_row_swizzle(m)), m.m_vec, n))
     req.dev["masks"] = per_layer
 
 
@@ -111,13 +119,21 @@ def footprint_bytes(reqs: list[Request], hidden: int, heads: int, layers: int, V
 
 
 class ContinuousBatchingServer:
+    """Admission: a new batch starts when no batch is in flight, or when the
+    queued tokens reach `overlap_tokens` (then batches overlap on their own
+    streams, up to `max_inflight`); otherwise queued requests wait for the
+    running batch and are admitted together.  Light load therefore runs one
+    request at a time (no device time-sharing between lone requests), heavy
+    load batches and overlaps."""
+
     def __init__(self, model, hidden: int = 256, heads: int = 4, V: int = 8, rhs_bits: int = 8,
                  max_inflight: int = 3, max_batch_tokens: int = 65536, hbm_reserve: int = 2 << 30,
-                 device="cuda"):
+                 overlap_tokens: int = 8192, device="cuda"):
         self.model, self.hidden, self.heads, self.V = model, hidden, heads, V
         self.layers = len(model.layers)
         self.alignment = 16 if rhs_bits == 8 else 32
         self.max_inflight, self.max_batch_tokens, self.hbm_reserve = max_inflight, max_batch_tokens, hbm_reserve
+        self.overlap_tokens = overlap_tokens
         self.device = torch.device(device)
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
         self.batches: list[list[int]] = []
@@ -155,7 +171,8 @@ class ContinuousBatchingServer:
                 # admission of a new batch: as many queued requests as the
                 # token budget and the free HBM allow (the first one always,
                 # when nothing else is on the device)
-                if queue and free_streams:
+                queued_tokens = sum(r.seq_len for r in queue)
+                if queue and free_streams and (not inflight or queued_tokens >= self.overlap_tokens):
                     batch, tokens = [], 0
                     while queue:
                         r = queue[0]

@@ -127,3 +127,24 @@ def test_fused_reports_rows_longer_than_declared(cuda):
     torch.cuda.synchronize()
     assert int(fus.core.status.item()) == 1
     assert torch.all(fus.core.out == 7.0)  # every row exceeds 32 nonzero vectors: nothing written
+
+
+def test_device_packed_request_masks_equal_host_packed(cuda):
+    """Requests uploaded with the GPU packer (upper-bound slot arrays, no host
+    round trip) give the same encoder output as the host-packed block-diagonal
+    mask of the same requests."""
+    torch.manual_seed(1)
+    enc = model.SparseEncoder(layers=2, hidden=128, heads=2, ffn=256).to(cuda).half().eval()
+    reqs = serving.make_requests(3, rate=0.0, hidden=128, layers=2, sparsity=0.9, median=256, clip=(128, 512),
+                                 seed=8)
+    for r in reqs:
+        serving._upload(r, 16, cuda)
+    dev_masks = serving.batch_masks(reqs, 2, 8)
+    host_masks = [batched.to_device(batched.block_diagonal([r.masks[l] for r in reqs])[0], 16, cuda)
+                  for l in range(2)]
+    x = torch.cat([r.dev["x"] for r in reqs], dim=0)
+    with torch.no_grad():
+        a = enc(x, dev_masks)
+        b = enc(x, host_masks)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)

@@ -23,13 +23,14 @@ inline int persistent_ctas(K kernel, int threads, long long work_ctas)
     return n < 1 ? 1 : (int)n;
 }
 
-template <int V, int PA, int PB, bool S, bool H, int W, bool F, bool E>
+template <int V, int PA, int PB, bool S, bool H, int W, bool F, bool E, int MTILES = 2>
 int spmm_launch_stream(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
     const long long ntasks = (long long)d.m_vec * d.batch;
     if (ntasks > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
-    const int ny = d.n / (W * 32);
-    auto kern = spmm_stream_kernel<V, PA, PB, S, W, H, F, E>;
+    constexpr int MT = MTILES;
+    const int ny = d.n / (W * 16 * MT);
+    auto kern = spmm_stream_kernel<V, PA, PB, S, W, H, F, E, MT>;
     // resident CTAs over all SMs, split across the ny column tiles
     const long long resident = persistent_ctas(kern, W * 32, 0x7fffffffLL);
     long long gx = (resident + ny - 1) / ny;
@@ -64,6 +65,12 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
         if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
             return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");
         if (d.kernel_variant != MC_KERNEL_PER_ROW && stream_ok) {
+            if constexpr (PB == 8) {
+                // 8-bit B, n % 256 == 0: four 16-column MMA tiles per warp
+                if (d.n % 256 == 0)
+                    return f16 ? spmm_launch_stream<V, PA, PB, S, H, 4, true, E, 4>(d, p, s)
+                               : spmm_launch_stream<V, PA, PB, S, H, 4, false, E, 4>(d, p, s);
+            }
             if (d.n % 128 == 0)
                 return f16 ? spmm_launch_stream<V, PA, PB, S, H, 4, true, E>(d, p, s)
                            : spmm_launch_stream<V, PA, PB, S, H, 4, false, E>(d, p, s);

@@ -30,20 +30,21 @@ __device__ __forceinline__ void ldsm_x2_trans_b8(uint32_t (&r)[4], const void* p
                  : "r"(smem_u32(p)));
 }
 
-// Shared-memory geometry of one stage's gathered-row slice.
-template <int PREB, int WARPS>
+// Shared-memory geometry of one stage's gathered-row slice (MT 16-column MMA
+// tiles per warp).
+template <int PREB, int WARPS, int MT>
 struct StreamRhs {
-    static constexpr int NT = WARPS * 32;
+    static constexpr int NT = WARPS * 16 * MT;
     static constexpr int RB = NT * PREB / 8;  // packed bytes per row slice
     static constexpr int CH = RB / 16;        // 16-byte chunks per row slice
-    // 8-bit: rows of NT bytes, 16-byte chunks XOR-swizzled over 8 (NT=128) or
-    // 4 (NT=64, two rows per 128-byte line) rows for ldmatrix.
+    // 8-bit: rows of NT bytes, 16-byte chunks XOR-swizzled over 8 (NT >= 128)
+    // or 4 (NT = 64, two rows per 128-byte line) rows for ldmatrix.
     // 4-bit: the layout of mc_spmm.cuh's RhsSmem (16-bit loads).
     static constexpr int STRIDE = PREB == 8 ? RB : (CH == 4 ? 64 : 48);
     __device__ __forceinline__ static int swz(int r, int c)
     {
         if constexpr (PREB == 8) {
-            if constexpr (CH == 8) return c ^ (r & 7);
+            if constexpr (CH >= 8) return c ^ (r & 7);
             else return c ^ ((r >> 1) & 3);
         } else {
             if constexpr (CH == 4) return c ^ ((r >> 2) & 3);
@@ -56,14 +57,18 @@ struct StreamTask {
     int task, step, row, b, start, nnz, steps;
 };
 
-template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT, bool F16, bool EXT>
+// MT: 16-column MMA tiles per warp (2, or 4 for 8-bit B): more columns per
+// warp spread each step's bookkeeping (barrier, copies, cursor, header) over
+// more MMAs.
+template <int V, int PREA, int PREB, bool SIGNED, int WARPS, bool HALF_OUT, bool F16, bool EXT, int MT = 2>
 __global__ void __launch_bounds__(WARPS * 32)
 spmm_stream_kernel(const SpmmParams p, const int ntasks)
 {
+    static_assert(MT == 2 || PREB == 8, "4-bit B runs with two MMA tiles per warp");
     using L = SpmmLayout<PREA, PREB, EXT>;
-    using S = StreamRhs<PREB, WARPS>;
+    using S = StreamRhs<PREB, WARPS, MT>;
     constexpr int STAGES = 4;
-    constexpr int NT = WARPS * 32;
+    constexpr int NT = WARPS * 16 * MT;
     constexpr int THREADS = WARPS * 32;
     constexpr int CPT = (32 * S::CH) / THREADS;  // rhs chunks per thread per stage
     constexpr int BP = L::BYTE_PLANES;
@@ -158,12 +163,12 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
         fetch_cols(cur, cols);
     }
 
-    int acc[BP][2][4];
-    float facc[BP][2][4];
+    int acc[BP][MT][4];
+    float facc[BP][MT][4];
 #pragma unroll
     for (int bp = 0; bp < BP; ++bp)
 #pragma unroll
-        for (int m = 0; m < 2; ++m)
+        for (int m = 0; m < MT; ++m)
 #pragma unroll
             for (int e = 0; e < 4; ++e) { acc[bp][m][e] = 0; facc[bp][m][e] = 0.f; }
 
@@ -217,14 +222,14 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
                     }
                 }
             }
-            // ---- A fragments of this warp's 32 columns: af[m][0..3] for MMA m
-            uint32_t af[2][4];
+            // ---- A fragments of this warp's 16*MT columns: af[m][0..3] for MMA m
+            uint32_t af[MT][4];
             if constexpr (PREB == 8) {
-                // lanes 0-15: slots 0-15, lanes 16-31: slots 16-31 of column chunk 2*warp+m
+                // lanes 0-15: slots 0-15, lanes 16-31: slots 16-31 of column chunk MT*warp+m
                 const int r = lane;
 #pragma unroll
-                for (int m = 0; m < 2; ++m)
-                    ldsm_x2_trans_b8(af[m], st + r * S::STRIDE + S::swz(r, 2 * warp + m) * 16);
+                for (int m = 0; m < MT; ++m)
+                    ldsm_x2_trans_b8(af[m], st + r * S::STRIDE + S::swz(r, MT * warp + m) * 16);
             } else {
                 const int ncol = warp * 32 + 4 * g;
                 uint32_t tr[2][4];
@@ -251,7 +256,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
                     if (SIGNED && top) { bytes_to_h2<true>(vals[bp][0], v0l, v0h); bytes_to_h2<true>(vals[bp][1], v1l, v1h); }
                     else { bytes_to_h2<false>(vals[bp][0], v0l, v0h); bytes_to_h2<false>(vals[bp][1], v1l, v1h); }
 #pragma unroll
-                    for (int m = 0; m < 2; ++m) {
+                    for (int m = 0; m < MT; ++m) {
                         uint32_t a[4][2];
 #pragma unroll
                         for (int q = 0; q < 4; ++q) bytes_to_h2<SIGNED>(af[m][q], a[q][0], a[q][1]);
@@ -260,7 +265,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
                     }
                 } else {
 #pragma unroll
-                    for (int m = 0; m < 2; ++m) {
+                    for (int m = 0; m < MT; ++m) {
                         if (SIGNED && top)
                             mma_k32<SIGNED, true>(acc[bp][m], af[m][0], af[m][1], af[m][2], af[m][3], vals[bp][0], vals[bp][1]);
                         else
@@ -273,7 +278,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
 #pragma unroll
                     for (int bp = 0; bp < BP; ++bp)
 #pragma unroll
-                        for (int m = 0; m < 2; ++m)
+                        for (int m = 0; m < MT; ++m)
 #pragma unroll
                             for (int e = 0; e < 4; ++e) {
                                 acc[bp][m][e] = (int)((uint32_t)acc[bp][m][e] + (uint32_t)f2i_exact(facc[bp][m][e]));
@@ -290,25 +295,26 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
             for (int e2 = 0; e2 < 2; ++e2) {
                 const int v = 2 * t + e2;
                 if (v >= V) continue;
-                int r4[4];
+                int r4[2 * MT];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
+                for (int q = 0; q < 2 * MT; ++q) {
                     const int m = q >> 1, e = 2 * (q & 1) + e2;
                     uint32_t x = (uint32_t)acc[0][m][e];
                     if constexpr (BP == 2) x += (uint32_t)acc[1][m][e] << 8;
                     r4[q] = (int)x;
                 }
-                const long long obase = (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + warp * 32;
+                const long long obase =
+                    (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + warp * 16 * MT;
                 if constexpr (PREB == 8) {
-                    // columns g, g+8, g+16, g+24
+                    // columns g, g+8, ..., g + 8 (2 MT - 1)
                     if constexpr (HALF_OUT) {
                         __half* o = reinterpret_cast<__half*>(p.out) + obase + g;
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) o[8 * q] = deq_half(r4[q], p.scale);
+                        for (int q = 0; q < 2 * MT; ++q) o[8 * q] = deq_half(r4[q], p.scale);
                     } else {
                         int* o = reinterpret_cast<int*>(p.out) + obase + g;
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) stg_cs_s32(o + 8 * q, r4[q]);
+                        for (int q = 0; q < 2 * MT; ++q) stg_cs_s32(o + 8 * q, r4[q]);
                     }
                 } else {
                     // columns 4g .. 4g+3
@@ -323,7 +329,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
 #pragma unroll
             for (int bp = 0; bp < BP; ++bp)
 #pragma unroll
-                for (int m = 0; m < 2; ++m)
+                for (int m = 0; m < MT; ++m)
 #pragma unroll
                     for (int e = 0; e < 4; ++e) { acc[bp][m][e] = 0; facc[bp][m][e] = 0.f; }
         }

@@ -30,7 +30,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-MMA_NAMES = {1: "int8mma", 2: "f16mma"}
+MMA_NAMES = {1: "int8mma", 2: "f16mma", 3: "tcgen05"}
 METRIC = "quantized SpMM/SDDMM TOP/s vs roofline; sparse-attn req/s + p50/p99 latency"
 UNIT = "TOP/s"
 SEQ, HEAD_DIM, VEC, SPARSITY = 4096, 64, 8, 0.9
@@ -307,17 +307,20 @@ def run_gpu(args) -> None:
 
     variants = {}
     if not args.headline_only:
-        alt = 1 if args.mma == 2 else 2
-        for pa, pb, name, mma, var in [(4, 4, "sddmm_L4R4", args.mma, 0), (16, 8, "sddmm_L16R8", args.mma, 0),
-                                       (8, 8, f"sddmm_L8R8_{MMA_NAMES[alt]}", alt, 0),
-                                       (8, 8, "sddmm_L8R8_per_row_kernel", args.mma, 1)]:
+        # the other tensor paths of the headline SDDMM; the other precision
+        # pairs and the SpMM run on mma.sync (int8 unless --mma f16)
+        others = [m for m in (1, 2, 3) if m != args.mma]
+        sync_mma = 2 if args.mma == 2 else 1
+        cases = [(4, 4, "sddmm_L4R4", sync_mma, 0), (16, 8, "sddmm_L16R8", sync_mma, 0)]
+        cases += [(8, 8, f"sddmm_L8R8_{MMA_NAMES[m]}", m, 0) for m in others]
+        cases += [(8, 8, "sddmm_L8R8_per_row_kernel", sync_mma, 1)]
+        for pa, pb, name, mma, var in cases:
             r = sddmm_case(pa, pb, mma=mma, variant=var)
             variants[name] = {"tops": r["tops"], "ms": r["ms"], "gbs": r["gbs"],
                               "hbm_frac": r["gbs"] / peaks["hbm_gbs"]}
             del r
             torch.cuda.empty_cache()
-        for mma, var, tag in ((args.mma, 0, MMA_NAMES[args.mma]), (alt, 0, MMA_NAMES[alt]),
-                              (args.mma, 1, "per_row_kernel")):
+        for mma, var, tag in ((1, 0, MMA_NAMES[1]), (2, 0, MMA_NAMES[2]), (sync_mma, 1, "per_row_kernel")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
     attention = serving_res = packer = projection = competitors = None
@@ -335,6 +338,13 @@ def run_gpu(args) -> None:
             serving_res = serving_suite(args, dev)
 
     tpk = tensor_peaks(dev)
+    if args.mma == 3:
+        mp = ROOT / "MEASURED_PEAKS.json"
+        tensor_peak = float(json.loads(mp.read_text())["bf16_tflops"]) if mp.exists() else 1900.0
+        tensor_peak_source = "measured dense bf16 GEMM burst (MEASURED_PEAKS.json)" if mp.exists() else "fallback"
+    else:
+        tensor_peak = tpk["int8_mma_sync" if args.mma == 1 else "f16_mma_sync"]
+        tensor_peak_source = "measured mma.sync probe (mcProbeTensorPeak)"
     if rank == 0:
         gbs = head["gbs"]
         line = {
@@ -352,13 +362,11 @@ def run_gpu(args) -> None:
                                      if measured_traffic_per_instance() and args.mma == 1 else None),
                          "traffic_source": "ncu capture of 32 instances scaled to the launch (see profiles/)",
                          "algorithmic_bytes": head["bytes"], "peak_source": peaks["source"]},
-            # The int8 contraction runs on mma.sync (sm_103a has no tcgen05
-            # integer MMA); its measured peak bounds this kernel before HBM does.
-            "tensor_roofline": {"achieved": head["tops"], "peak": tpk["int8_mma_sync" if args.mma == 1 else
-                                                                      "f16_mma_sync"],
-                                "unit": "TOP/s", "frac": head["tops"] / tpk["int8_mma_sync" if args.mma == 1 else
-                                                                            "f16_mma_sync"],
-                                "peak_source": "measured mma.sync probe (mcProbeTensorPeak)",
+            # The contraction's tensor path and its measured peak: mma.sync int8
+            # / f16 (probe), or tcgen05 kind::f16 (the measured dense bf16/f16
+            # GEMM rate); sm_103a has no integer tcgen05.mma.
+            "tensor_roofline": {"achieved": head["tops"], "peak": tensor_peak, "unit": "TOP/s",
+                                "frac": head["tops"] / tensor_peak, "peak_source": tensor_peak_source,
                                 "probe_tops": tpk},
             "e2e": e2e,
             "gpu_launches": args.steps * launches_per_step,
@@ -798,13 +806,14 @@ def main() -> None:
     ap.add_argument("--serving-requests", type=int, default=48, help="requests per serving run (0 skips it)")
     ap.add_argument("--serving-overlap-tokens", type=int, default=8192,
                     help="queued tokens at which the server overlaps a new batch with running ones")
-    ap.add_argument("--mma", choices=["int8", "f16"], default="int8",
-                    help="tensor path (both are bit-exact; see include/magicube_gb300.h)")
+    ap.add_argument("--mma", choices=["int8", "f16", "tc"], default="int8",
+                    help="tensor path of the headline SDDMM: int8 / f16 mma.sync or tcgen05 (all bit-exact; "
+                         "see include/magicube_gb300.h)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    args.mma = 2 if args.mma == "f16" else 1
+    args.mma = {"int8": 1, "f16": 2, "tc": 3}[args.mma]
     if args.profile:
         if args.batch == 64 and args.profile == "spmm":
             args.batch = 128

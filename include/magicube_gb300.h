@@ -88,7 +88,14 @@ int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* row_indices, const int* 
  *              partial sum is an integer below 2^24, so nothing rounds); on
  *              sm_103a the f16 tensor rate is several times the int8 one.
  * MC_MMA_DEFAULT selects the library default (mcSetDefaultMmaKind). */
-enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2 };
+/* MC_MMA_TCGEN05 (SDDMM L8-R8 with k == 64 only): operands converted exactly
+ *              to f16 in shared memory, tcgen05.mma kind::f16 (M = 128
+ *              nonzeros, N = 16, K = 64) with the f32 accumulator in TMEM;
+ *              exact because 64 products of 8-bit integers stay below 2^24. */
+enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2, MC_MMA_TCGEN05 = 3 };
+/* Number of bounded waits in the tcgen05 SDDMM that ran out (0 unless the
+ * device stalled; an affected launch's results are incomplete).  Synchronous. */
+unsigned mcTensorCoreTimeouts(void);
 /* Sets the default tensor path; returns the previous one (or -1 if invalid). */
 int mcSetDefaultMmaKind(int kind);
 

@@ -81,7 +81,7 @@ class McDevicePackDesc(ctypes.Structure):
 
 
 REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
-MMA_DEFAULT, MMA_INT8, MMA_F16 = 0, 1, 2
+MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05 = 0, 1, 2, 3
 KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM = 0, 1, 2
 VALUES_PACKED, VALUES_SOFTMAX = 0, 1
 
@@ -91,6 +91,7 @@ _SIGNATURES = {
     "mcGetLastErrorString": (ctypes.c_char_p, []),
     "mcVersion": (ctypes.c_char_p, []),
     "mcSetDefaultMmaKind": (_c_int, [_c_int]),
+    "mcTensorCoreTimeouts": (ctypes.c_uint, []),
     "mcSpmm": (_c_int, [ctypes.POINTER(McSpmmDesc), _c_vp]),
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
     "mcQuantize": (_c_int, [_c_vp, _c_vp, _c_ll, _c_int, _c_float, _c_vp]),

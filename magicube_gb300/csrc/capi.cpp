@@ -47,7 +47,8 @@ static int check_spmm(const mcSpmmDesc& d)
         return fail(1, "mcSpmm: half output is built for the softmax value layout and int32 output for the "
                        "packer layout");
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSpmm: half output requires a nonzero scale");
-    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16) return fail(1, "mcSpmm: invalid mma_kind");
+    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16)
+        return fail(1, "mcSpmm: invalid mma_kind (the SpMM runs on MC_MMA_INT8 or MC_MMA_F16)");
     if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_STREAM)
         return fail(1, "mcSpmm: invalid kernel_variant");
     if (d.m_vec == 0) return 0;
@@ -80,7 +81,9 @@ static int check_sddmm(const mcSddmmDesc& d)
     if (d.out_half && (!d.is_signed || !d.out_vecmajor))
         return fail(1, "mcSddmm: half output requires is_signed = 1 and out_vecmajor = 1");
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSddmm: half output requires a nonzero scale");
-    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16) return fail(1, "mcSddmm: invalid mma_kind");
+    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_TCGEN05) return fail(1, "mcSddmm: invalid mma_kind");
+    if (d.mma_kind == MC_MMA_TCGEN05 && (d.lhs_bits != 8 || d.rhs_bits != 8 || d.k != 64))
+        return fail(1, "mcSddmm: the tcgen05 path computes L8-R8 with k == 64");
     if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_STREAM)
         return fail(1, "mcSddmm: invalid kernel_variant");
     if (d.m_vec == 0) return 0;

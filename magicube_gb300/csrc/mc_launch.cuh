@@ -120,9 +120,13 @@ int sddmm_launch_k64(const mcSddmmDesc& d, const SddmmParams& p, int split, cuda
     return (int)cudaGetLastError();
 }
 
+// The tcgen05 SDDMM (sddmm_tc.cu).
+int sddmm_tc_launch(const mcSddmmDesc& d, const SddmmParams& p, cudaStream_t s);
+
 template <int V, int PA, int PB, bool S, bool VM, bool H>
 int sddmm_launch_v(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaStream_t s)
 {
+    if (resolve_mma_kind(d.mma_kind) == MC_MMA_TCGEN05) return sddmm_tc_launch(d, p, s);
     const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
     if (d.kernel_variant == MC_KERNEL_STREAM && d.k != 64)
         return fail(1, "mcSddmm: the streaming kernel needs k == 64");

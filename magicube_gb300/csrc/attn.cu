@@ -68,17 +68,17 @@ __device__ __forceinline__ void load_vec(const __half* p, float (&x)[V], float s
         int4 r = *reinterpret_cast<const int4*>(p);
         const __half* h = reinterpret_cast<const __half*>(&r);
 #pragma unroll
-        for (int v = 0; v < 8; ++v) x[v] = __half2float(h[v]) * s;
+        for (int v = 0; v < 8; ++v) x[v] = __fmul_rn(__half2float(h[v]), s);
     } else if constexpr (V == 4) {
         int2 r = *reinterpret_cast<const int2*>(p);
         const __half* h = reinterpret_cast<const __half*>(&r);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) x[v] = __half2float(h[v]) * s;
+        for (int v = 0; v < 4; ++v) x[v] = __fmul_rn(__half2float(h[v]), s);
     } else {
         int r = *reinterpret_cast<const int*>(p);
         const __half* h = reinterpret_cast<const __half*>(&r);
-        x[0] = __half2float(h[0]) * s;
-        x[1] = __half2float(h[1]) * s;
+        x[0] = __fmul_rn(__half2float(h[0]), s);
+        x[1] = __fmul_rn(__half2float(h[1]), s);
     }
 }
 

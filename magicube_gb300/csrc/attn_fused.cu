@@ -7,8 +7,8 @@
 //      (mma.m16n8k32 s8, K rows gathered with 128-bit loads straight into the
 //      A fragment, Q rows in registers), dequantised exactly as the separate
 //      SDDMM does (half(acc / scale_qkv^2)) and multiplied by the softmax
-//      scaling, kept as f32 [v][slot] (MC_REQUANT_ROWMAX scales the int32
-//      accumulator straight to f32 instead, skipping the half rounding);
+//      scaling, kept as the half [v][slot] (MC_REQUANT_ROWMAX keeps the int32
+//      accumulator times scaling / scale^2, rounded once to half);
 //   2. softmax per vector lane: max, sum of exp, requantization to int8
 //      [v][slot] -- warp w owns lanes 2w, 2w+1 and visits slots in the same
 //      per-thread order and reduction tree as the separate softmax kernel,
@@ -64,14 +64,13 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
     constexpr int STAGES = 2;   // per-warp V-row ring depth
     constexpr int ROW = 64;     // bytes of one int8 row of d = 64
     extern __shared__ __align__(128) uint8_t smem[];
-    const int SP = p.nnzp + 4;    // f32 score row stride (bank offset 4 words per lane)
-    const int PP = p.nnzp + 16;   // int8 probability row stride
-    // S (scores) and, after the softmax, the cross-warp reduction buffer
-    float* S = reinterpret_cast<float*>(smem);
-    int* RED = reinterpret_cast<int*>(smem);
-    const size_t s_bytes = ((size_t)V * SP * 4 > 8192 ? (size_t)V * SP * 4 : 8192);
-    uint8_t* P = smem + s_bytes;
-    int* C = reinterpret_cast<int*>(P + (size_t)V * PP);
+    const int SP = p.nnzp + 8;    // half score row stride (bank offset 4 words per vector lane)
+    // Score row v (half) is overwritten from its start by the int8
+    // probabilities of lane v: slot j's byte lies in score j / 2, already read.
+    __half* S = reinterpret_cast<__half*>(smem);
+    uint8_t* P = smem;
+    const int PP = 2 * SP;        // probability row stride in bytes
+    int* C = reinterpret_cast<int*>(smem + (size_t)V * SP * 2);
     float* DEN = reinterpret_cast<float*>(C + p.nnzp);
     float* MAXW = DEN + 8;  // [4 warps][8 lanes] partial row maxima of the scores
     uint8_t* rings = reinterpret_cast<uint8_t*>(
@@ -95,7 +94,7 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
         const uint8_t* kh = p.k + (long long)h * p.head_stride;
         const uint8_t* vh = p.v + (long long)h * p.head_stride;
 
-        __syncthreads();  // the previous item is done with S/RED, C, P, DEN and MAXW
+        __syncthreads();  // the previous item is done with S/P, C, DEN, MAXW and the rings
         for (int j = tid; j < nnz; j += 128) C[j] = __ldg(p.col_indices + start + j);
         int4 qf = make_int4(0, 0, 0, 0);
         if (g < V) qf = ldg_nc_v4(qh + (long long)(row * V + g) * ROW + 16 * t);
@@ -133,11 +132,14 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
                 if (j >= nnz) continue;
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {
+                    // Fixed mode keeps the separate SDDMM's half output
+                    // (scaled on every read); row-max mode the half-rounded
+                    // scaled score.  The maximum is taken of what is stored.
                     const int a = acc[2 * hh + e];
-                    const float x = ROWMAX ? __int2float_rn(a) * sfac
-                                           : __half2float(deq_half(a, p.score_scale)) * p.scaling;
-                    S[(2 * t + e) * SP + j] = x;
-                    mxl[e] = fmaxf(mxl[e], x);
+                    const __half hs = ROWMAX ? __float2half_rn(__int2float_rn(a) * sfac)
+                                             : deq_half(a, p.score_scale);
+                    S[(2 * t + e) * SP + j] = hs;
+                    mxl[e] = fmaxf(mxl[e], ROWMAX ? __half2float(hs) : __fmul_rn(__half2float(hs), p.scaling));
                 }
             }
         };
@@ -178,15 +180,19 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
         for (int e = 0; e < 2; ++e) {
             const int v = 2 * warp + e;
             if (v >= V) break;
-            float* sv = S + v * SP;
+            const __half* sv = S + v * SP;
             const float mx = fmaxf(fmaxf(MAXW[v], MAXW[8 + v]), fmaxf(MAXW[16 + v], MAXW[24 + v]));
             uint8_t* pv = P + v * PP;
             float sum = 0.f;
+            // In every pass that writes probabilities, a __syncwarp separates
+            // the scores read in an iteration from the bytes written over them.
             if constexpr (ROWMAX) {
                 for (int j = lane; j < nround; j += 32) {
+                    const bool in = j < nnz;
+                    const float ex = in ? __expf(__half2float(sv[j]) - mx) : 0.f;
+                    __syncwarp();
                     int qv = 0;
-                    if (j < nnz) {
-                        const float ex = __expf(sv[j] - mx);
+                    if (in) {
                         sum += ex;
                         qv = __float2int_rn(127.f * ex);
                     }
@@ -195,17 +201,17 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
             } else {
-                for (int j = lane; j < nnz; j += 32) {
-                    const float ex = __expf(sv[j] - mx);
-                    sum += ex;
-                    sv[j] = ex;
-                }
+                for (int j = lane; j < nnz; j += 32) sum += __expf(__fmul_rn(__half2float(sv[j]), p.scaling) - mx);
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
                 for (int j = lane; j < nround; j += 32) {
+                    const bool in = j < nnz;
+                    // the exponent is recomputed: same inputs, same value
+                    const float ex = in ? __expf(__fmul_rn(__half2float(sv[j]), p.scaling) - mx) : 0.f;
+                    __syncwarp();
                     int qv = 0;
-                    if (j < nnz) {
-                        float f = sv[j] / sum * p.prob_scale;
+                    if (in) {
+                        float f = ex / sum * p.prob_scale;
                         f = fminf(fmaxf(f, -128.f), 127.f);
                         qv = (int)f;
                     }
@@ -243,19 +249,24 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
             issue(s + 8, slot);
             slot ^= 1;
         }
+        // Cross-warp sum of the partial products (exact integer adds) through
+        // the first 2 KB of each warp's own ring: its copies have landed and
+        // every lane is past its last read of the ring.
         cp_async_wait<0>();
-        // cross-warp sum of the partial products (exact integer adds)
+        __syncwarp();
+        int* red = reinterpret_cast<int*>(ring);
 #pragma unroll
         for (int m = 0; m < 4; ++m)
 #pragma unroll
-            for (int e = 0; e < 4; ++e) RED[(warp * 16 + m * 4 + e) * 32 + lane] = acc[m][e];
+            for (int e = 0; e < 4; ++e) red[(m * 4 + e) * 32 + lane] = acc[m][e];
         __syncthreads();
         int tot[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
             uint32_t x = 0;
 #pragma unroll
-            for (int w = 0; w < 4; ++w) x += (uint32_t)RED[(w * 16 + warp * 4 + e) * 32 + lane];
+            for (int w = 0; w < 4; ++w)
+                x += (uint32_t)reinterpret_cast<const int*>(rings + w * STAGES * 32 * ROW)[(warp * 4 + e) * 32 + lane];
             tot[e] = (int)x;
         }
         // tot: column n = 16 warp + g (+8 for tot[2], tot[3]), lane v = 2t (+1 for odd)
@@ -272,9 +283,8 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
 
 inline size_t attn_smem_bytes(int V, int nnzp)
 {
-    size_t sb = (size_t)V * (nnzp + 4) * 4;
-    if (sb < 8192) sb = 8192;  // doubles as the 4 x 16 x 32-int reduction buffer
-    const size_t s = sb + (size_t)V * (nnzp + 16) + (size_t)nnzp * 4 + 8 * 4 + 32 * 4;
+    // score / probability rows, column indices, DEN and MAXW
+    const size_t s = (size_t)V * (nnzp + 8) * 2 + (size_t)nnzp * 4 + 8 * 4 + 32 * 4;
     return (s + 127) / 128 * 128 + 128 + 4 * 2 * 32 * 64;  // + four private 2-stage rings
 }
 

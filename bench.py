@@ -703,20 +703,130 @@ def serving_suite(args, dev) -> dict:
 
 
 def tensor_peaks(dev) -> dict:
-    """Measured mma.sync peaks (TOP/s) of the int8, int4 and f16 paths."""
+    """Measured mma.sync peaks (TOP/s) of the int8 (k = 32 and k = 16), int4
+    and f16 paths."""
     import torch
 
     from magicube_gb300 import _lib
     sink = torch.empty(4 * 256 * 8 * torch.cuda.get_device_properties(dev).multi_processor_count,
                        dtype=torch.uint8, device=dev)
     out = {}
-    for kind, name in ((0, "int8_mma_sync"), (1, "int4_mma_sync"), (2, "f16_mma_sync")):
+    for kind, name in ((0, "int8_mma_sync"), (1, "int4_mma_sync"), (2, "f16_mma_sync"), (3, "int8_k16_mma_sync")):
         ms, ops = ctypes.c_float(), ctypes.c_double()
         _lib.check(_lib.lib().mcProbeTensorPeak(kind, sink.data_ptr(), sink.numel(), 2048, ctypes.byref(ms),
                                                 ctypes.byref(ops), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                    "mcProbeTensorPeak")
         out[name] = ops.value / (ms.value * 1e-3) / 1e12
     return out
+
+
+SWEEP_SIZES = (512, 1024, 2048, 4096)
+SWEEP_SPARSITY = (0.5, 0.7, 0.8, 0.9, 0.95, 0.98)
+SWEEP_PAIRS = ((16, 8), (8, 8), (8, 4), (4, 4), (16, 4))
+SWEEP_COLUMNS = ("M", "K", "N", "sparsity", "V", "pair", "batch", "nnz_vec", "us_per_instance", "tops", "gbs",
+                 "hbm_frac", "tensor_util", "roofline_frac", "bound")
+
+
+def run_sweep(args) -> None:
+    """SpMM precision/shape sweep on synthetic pruned-weight matrices.
+
+    M, K in {512, 1024, 2048, 4096} (every pair with `--sweep full`, M = K
+    with `--sweep square`), N in {128, 256}, sparsity in {0.5, 0.7, 0.8, 0.9,
+    0.95, 0.98}, V in {2, 4, 8}, per-vector-row lengths ~ Normal(mu, 0.3 mu)
+    clipped to [0, K] with mu = (1 - sparsity) K, pairs L16-R8, L8-R8, L8-R4,
+    L4-R4, L16-R4, signed lanes, int32 output.  Each point is one batched
+    launch over enough instances (own packed values, B and C; one mask) that
+    a step moves more than 2.5x L2, timed with CUDA events (median of
+    `--steps`).  The values and B are uniformly random bytes generated on the
+    device in the packed layouts (every bit pattern is a valid operand).
+    Algorithmic bytes per launch: unpadded values nnz V bits_A/8, B K N
+    bits_B/8 and C M N 4 per instance, column indices and offsets once;
+    ops 2 nnz V N per instance.  The roofline time is max(bytes / HBM peak,
+    MMA ops / measured int8 mma.sync peak), MMA ops counting both byte planes
+    of a 16-bit A (4-bit operands run unpacked on the int8 MMA)."""
+    import torch
+
+    from magicube_gb300 import formats, ops, synth
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream()
+    peaks = _peaks()
+    int8_peak = tensor_peaks(dev)["int8_mma_sync"]
+    l2 = int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0)) or 129 * 2 ** 20
+    target = int(2.5 * l2)
+    shapes = ([(m, k) for m in SWEEP_SIZES for k in SWEEP_SIZES] if args.sweep == "full"
+              else [(s, s) for s in SWEEP_SIZES])
+    steps, warmup = max(args.steps, 1), max(args.warmup, 3)
+    rows = []
+    t_start = time.time()
+    with ClockSampler(0) as clk:
+        for M, K in shapes:
+            for V in (2, 4, 8):
+                for sp in SWEEP_SPARSITY:
+                    mask = synth.normal_mask(M // V, K, V, sp, cv=0.3, seed=M * 7 + K * 13 + V * 101 + int(sp * 1000))
+                    if mask.nnz_vec == 0:
+                        continue
+                    ri = torch.from_numpy(formats.sorted_row_swizzle(mask)).to(dev)
+                    layouts = {}
+                    for chunk in (16, 32):
+                        pairs, n_al = formats.align_row_offsets(mask, chunk)
+                        cols = formats.pad_column_indices(mask, pairs, n_al, shuffle8=(chunk == 32))
+                        layouts[chunk] = (torch.from_numpy(pairs).to(dev), torch.from_numpy(cols).to(dev), n_al)
+                    idx_bytes = 4 * mask.nnz_vec + 4 * (mask.m_vec + 1)
+                    for pa, pb in SWEEP_PAIRS:
+                        ro_d, ci_d, n_al = layouts[formats.spmm_chunk(pa, pb)]
+                        vstride = n_al * V * formats.lane_bits(pa) // 8
+                        for N in (128, 256):
+                            per_inst = vstride + K * N * pb // 8 + M * N * 4
+                            B = max(1, min(4096, -(-target // per_inst)))
+                            vals = torch.randint(0, 256, (B * vstride,), dtype=torch.uint8, device=dev)
+                            rhs = torch.randint(0, 256, (B, K * N * pb // 8), dtype=torch.uint8, device=dev)
+                            out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
+                            d = ops.DeviceSpmmLhs(M // V, V, K, pa, pb, ri, ro_d, ci_d, vals)
+                            fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=vstride)
+                            t = statistics.median(time_cuda(fn, steps, warmup, stream)) / 1e3
+                            opc = 2.0 * mask.nnz_vec * V * N * B
+                            mma_ops = opc * (2 if pa == 16 else 1)
+                            byts = B * (mask.nnz_vec * V * pa / 8 + K * N * pb / 8 + M * N * 4) + idx_bytes
+                            t_hbm, t_tc = byts / (peaks["hbm_gbs"] * 1e9), mma_ops / (int8_peak * 1e12)
+                            rows.append([M, K, N, sp, V, f"L{pa}-R{pb}", B, mask.nnz_vec, round(t / B * 1e6, 4),
+                                         round(opc / t / 1e12, 3), round(byts / t / 1e9, 1),
+                                         round(byts / t / 1e9 / peaks["hbm_gbs"], 4),
+                                         round(mma_ops / t / 1e12 / int8_peak, 4),
+                                         round(max(t_hbm, t_tc) / t, 4), "hbm" if t_hbm >= t_tc else "tensor"])
+                            del vals, rhs, out, d
+            print(f"sweep: M={M} K={K} done, {len(rows)} points, {time.time() - t_start:.0f} s",
+                  file=sys.stderr, flush=True)
+    col = {c: i for i, c in enumerate(SWEEP_COLUMNS)}
+    summary = {}
+    for pa, pb in SWEEP_PAIRS:
+        name = f"L{pa}-R{pb}"
+        sel = [r for r in rows if r[col["pair"]] == name]
+        hi = [r for r in sel if r[col["sparsity"]] >= 0.9]
+        if not sel:
+            continue
+        summary[name] = {
+            "points": len(sel),
+            "geomean_gbs": float(np.exp(np.mean(np.log([r[col["gbs"]] for r in sel])))),
+            "max_gbs": max(r[col["gbs"]] for r in sel),
+            "max_tops": max(r[col["tops"]] for r in sel),
+            "median_roofline_frac": statistics.median(r[col["roofline_frac"]] for r in sel),
+            "sparsity_ge_0.9": {
+                "points": len(hi),
+                "median_hbm_frac": statistics.median(r[col["hbm_frac"]] for r in hi) if hi else None,
+                "median_roofline_frac": statistics.median(r[col["roofline_frac"]] for r in hi) if hi else None,
+                "points_at_ge_60pct_roofline": sum(r[col["roofline_frac"]] >= 0.6 for r in hi)},
+        }
+    line = {"sweep": "spmm precision/shape", "shapes": args.sweep, "steps": steps, "warmup": warmup,
+            "data": "synthetic (normal row lengths, cv 0.3; random packed operands)",
+            "l2": f"each step moves > 2.5x L2 ({target / 1e6:.0f} MB)",
+            "peaks": {"hbm_gbs": peaks["hbm_gbs"], "hbm_source": peaks["source"], "int8_mma_sync_tops": int8_peak},
+            "seconds": round(time.time() - t_start, 1), "clocks": clk.summary(), "summary": summary,
+            "columns": list(SWEEP_COLUMNS), "points": rows}
+    text = json.dumps(line)
+    if args.sweep_out:
+        Path(args.sweep_out).parent.mkdir(parents=True, exist_ok=True)
+        Path(args.sweep_out).write_text(text + "\n")
+    print(text)
 
 
 def run_profile_case(args) -> None:
@@ -810,11 +920,16 @@ def main() -> None:
                     help="tensor path of the headline SDDMM: int8 / f16 mma.sync or tcgen05 (all bit-exact; "
                          "see include/magicube_gb300.h)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep", choices=["square", "full"], default=None,
+                    help="run only the SpMM precision/shape sweep (M = K, or every M, K pair)")
+    ap.add_argument("--sweep-out", default=None, help="also write the sweep's JSON line to this file")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     args.mma = {"int8": 1, "f16": 2, "tc": 3}[args.mma]
-    if args.profile:
+    if args.sweep:
+        run_sweep(args)
+    elif args.profile:
         if args.batch == 64 and args.profile == "spmm":
             args.batch = 128
         run_profile_case(args)

@@ -93,8 +93,9 @@ int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* row_indices, const int* 
  *              nonzeros, N = 16, K = 64) with the f32 accumulator in TMEM;
  *              exact because 64 products of 8-bit integers stay below 2^24. */
 enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2, MC_MMA_TCGEN05 = 3 };
-/* Number of bounded waits in the tcgen05 SDDMM that ran out (0 unless the
- * device stalled; an affected launch's results are incomplete).  Synchronous. */
+/* Number of bounded mbarrier waits that ran out in the tcgen05 SDDMM and the
+ * TMA SpMM (0 unless the device stalled; an affected launch's results are
+ * incomplete).  Synchronous. */
 unsigned mcTensorCoreTimeouts(void);
 /* Sets the default tensor path; returns the previous one (or -1 if invalid). */
 int mcSetDefaultMmaKind(int kind);
@@ -106,8 +107,16 @@ int mcSetDefaultMmaKind(int kind);
  *                    stream many vector-rows through one cp.async ring (needs
  *                    16-byte aligned values); SDDMM -- the k == 64 kernel with
  *                    a warp per 16-nonzero tile at full occupancy (needs k == 64).
- * MC_KERNEL_AUTO:    the pipelined kernel where it applies, else per-row. */
-enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2 };
+ * MC_KERNEL_TMA:     SpMM only, 8-bit B on the int8 path: persistent
+ *                    warp-specialised CTAs -- one producer warp gathers B rows
+ *                    with TMA (tile::gather4) into an mbarrier ring, four
+ *                    consumer warps multiply (needs n % 128 == 0, 16-byte
+ *                    aligned values, values_stride and rhs, rhs_stride a
+ *                    multiple of n).
+ * MC_KERNEL_AUTO:    SpMM: the TMA kernel where it applies and n % 256 == 0,
+ *                    else the streaming kernel, else per-row; SDDMM: the
+ *                    pipelined kernel where it applies, else per-row. */
+enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2, MC_KERNEL_TMA = 3 };
 
 /* ---- Value layouts of the SpMM sparse operand --------------------------------
  * MC_VALUES_PACKED:  the reference host packer's layout (what
@@ -145,7 +154,7 @@ typedef struct mcSpmmDesc {
     const void* rhs;      long long rhs_stride;     /* bytes */
     void* out;            long long out_stride;     /* elements */
     int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
-    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM */
+    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM / _TMA */
     int value_layout;           /* MC_VALUES_PACKED / MC_VALUES_SOFTMAX */
 } mcSpmmDesc;
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream);

@@ -82,7 +82,7 @@ class McDevicePackDesc(ctypes.Structure):
 
 REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
 MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05 = 0, 1, 2, 3
-KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM = 0, 1, 2
+KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA = 0, 1, 2, 3
 VALUES_PACKED, VALUES_SOFTMAX = 0, 1
 
 # name -> (restype, argtypes)

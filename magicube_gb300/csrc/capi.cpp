@@ -49,7 +49,7 @@ static int check_spmm(const mcSpmmDesc& d)
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSpmm: half output requires a nonzero scale");
     if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16)
         return fail(1, "mcSpmm: invalid mma_kind (the SpMM runs on MC_MMA_INT8 or MC_MMA_F16)");
-    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_STREAM)
+    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_TMA)
         return fail(1, "mcSpmm: invalid kernel_variant");
     if (d.m_vec == 0) return 0;
     if (!d.row_indices || !d.row_offsets || !d.column_indices || !d.values || !d.rhs || !d.out)

@@ -7,6 +7,8 @@
 #include "mc_sddmm_stream.cuh"
 #include "mc_spmm.cuh"
 #include "mc_spmm_stream.cuh"
+#include "mc_spmm_tma.cuh"
+#include "mc_tma_host.h"
 
 namespace mc {
 
@@ -40,6 +42,55 @@ int spmm_launch_stream(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     return (int)cudaGetLastError();
 }
 
+// The TMA SpMM (mc_spmm_tma.cuh) applies to 8-bit B on the int8 path with
+// n % 128 == 0, 16-byte aligned values (and values_stride), and batch
+// entries of B a whole number of rows apart.
+inline bool spmm_tma_eligible(const mcSpmmDesc& d)
+{
+    if (d.rhs_bits != 8 || d.n % 128 || resolve_mma_kind(d.mma_kind) != MC_MMA_INT8) return false;
+    if (reinterpret_cast<uintptr_t>(d.values) % 16 || d.values_stride % 16) return false;
+    if (reinterpret_cast<uintptr_t>(d.rhs) % 16) return false;
+    if (d.batch > 1 && d.rhs_stride % d.n) return false;
+    const long long per_entry = d.batch > 1 ? d.rhs_stride / d.n : 0;
+    return per_entry * (d.batch - 1) + d.k <= 0x7fffffffLL;
+}
+
+template <int V, int PA, bool S, bool H, int NT>
+int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
+{
+    constexpr int STAGES = 4;
+    using G = SpmmTmaGeom<V, PA, NT, STAGES>;
+    const long long ntasks = (long long)d.m_vec * d.batch;
+    if (ntasks > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
+    const long long per_entry = d.batch > 1 ? d.rhs_stride / d.n : 0;
+    CUtensorMap map;
+    if (!encode_row_gather_u8(&map, d.rhs, per_entry * (d.batch - 1) + d.k, d.n, 128))
+        return fail(1, "mcSpmm: TMA tensor map encoding failed");
+    unsigned int* timeouts = async_timeout_counter();
+    if (!timeouts) return fail(1, "mcSpmm: timeout counter unavailable");
+    auto kern = spmm_tma_kernel<V, PA, S, H, H, NT, STAGES>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
+        return (int)cudaGetLastError();
+    // resident CTAs per SM from registers, shared memory and warps
+    int per_sm = 1;
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kern) == cudaSuccess) {
+        const int regs = (fa.numRegs + 7) & ~7;
+        const int by_regs = regs > 0 ? 65536 / (regs * G::THREADS) : 1;
+        const int by_smem = (int)((228u * 1024u) / (unsigned)(G::SMEM + fa.sharedSizeBytes + 1024));
+        const int by_warps = 64 / (G::THREADS / 32);
+        per_sm = by_regs < by_smem ? by_regs : by_smem;
+        if (per_sm > by_warps) per_sm = by_warps;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int ny = d.n / NT;
+    long long gx = ((long long)per_sm * sm_count() + ny - 1) / ny;
+    if (gx > ntasks) gx = ntasks;
+    kern<<<dim3((unsigned)(gx < 1 ? 1 : gx), (unsigned)ny, 1), G::THREADS, G::SMEM, s>>>(map, p, (int)ntasks,
+                                                                                        (int)per_entry, timeouts);
+    return (int)cudaGetLastError();
+}
+
 // H (half output) is compiled only with the softmax value layout (E), the
 // combination the extension's batched SpMM uses; int32 output only with the
 // packer layout.
@@ -50,7 +101,8 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     if constexpr (PB == 16) {
         // 16-bit B: the per-row kernel on the int8 path (the f16 path gives the
         // same integers; it is not built for four byte-plane products).
-        if (d.kernel_variant == MC_KERNEL_STREAM) return fail(1, "mcSpmm: 16-bit B runs on the per-row kernel");
+        if (d.kernel_variant == MC_KERNEL_STREAM || d.kernel_variant == MC_KERNEL_TMA)
+            return fail(1, "mcSpmm: 16-bit B runs on the per-row kernel");
         if (d.n % 128 == 0) {
             dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 128), (unsigned)d.batch);
             spmm_kernel<V, PA, PB, S, 4, H, false, E><<<grid, 128, 0, s>>>(p);
@@ -64,6 +116,20 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
         const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
         if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
             return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");
+        if constexpr (PB == 8) {
+            if (d.kernel_variant == MC_KERNEL_TMA && !spmm_tma_eligible(d))
+                return fail(1, "mcSpmm: the TMA kernel needs the int8 path, n % 128 == 0, 16-byte aligned values, "
+                               "values_stride and rhs, and rhs_stride a multiple of n");
+            // AUTO takes the TMA kernel for 256-column tiles only: with 128
+            // columns a stage carries too few MMAs for the producer's per-step
+            // cost, and the streaming kernel measured faster.
+            if (spmm_tma_eligible(d) &&
+                (d.kernel_variant == MC_KERNEL_TMA || (d.kernel_variant == MC_KERNEL_AUTO && d.n % 256 == 0)))
+                return d.n % 256 == 0 ? spmm_launch_tma<V, PA, S, H, 256>(d, p, s)
+                                      : spmm_launch_tma<V, PA, S, H, 128>(d, p, s);
+        } else {
+            if (d.kernel_variant == MC_KERNEL_TMA) return fail(1, "mcSpmm: the TMA kernel needs 8-bit B");
+        }
         if (d.kernel_variant != MC_KERNEL_PER_ROW && stream_ok) {
             if constexpr (PB == 8) {
                 // 8-bit B, n % 256 == 0: four 16-column MMA tiles per warp

@@ -30,10 +30,10 @@
 
 #include <cmath>
 #include <cstdint>
-#include <mutex>
 
 #include "mc_host.h"
 #include "mc_sm100.cuh"
+#include "mc_tma_host.h"
 
 namespace mc {
 namespace {
@@ -288,25 +288,10 @@ size_t proj_smem_bytes(int BN, int K)
            (size_t)BN * 4;
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
-{
-    static std::once_flag once;
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    std::call_once(once, [] {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    });
-    return fn;
-}
-
 // Row-major [rows][K] f16 matrix, boxes of box_rows x 64, 128-byte swizzle.
 bool encode_kmajor(CUtensorMap* map, const void* base, long long rows, int K, int box_rows)
 {
-    auto fn = encode_fn();
+    auto fn = tensor_map_encoder();
     if (!fn) return false;
     const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)K * 2};

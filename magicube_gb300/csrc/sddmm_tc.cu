@@ -56,5 +56,6 @@ extern "C" unsigned mcTensorCoreTimeouts(void)
 {
     unsigned v = 0;
     if (cudaMemcpyFromSymbol(&v, mc::g_tc_timeouts, sizeof v) != cudaSuccess) return 0xFFFFFFFFu;
-    return v;
+    const unsigned w = mc::async_timeouts();
+    return w == 0xFFFFFFFFu ? w : v + w;
 }

@@ -113,9 +113,9 @@ int mcSetDefaultMmaKind(int kind);
  *                    consumer warps multiply (needs n % 128 == 0, 16-byte
  *                    aligned values, values_stride and rhs, rhs_stride a
  *                    multiple of n).
- * MC_KERNEL_AUTO:    SpMM: the TMA kernel where it applies and n % 256 == 0,
- *                    else the streaming kernel, else per-row; SDDMM: the
- *                    pipelined kernel where it applies, else per-row. */
+ * MC_KERNEL_AUTO:    SpMM: the TMA kernel where it applies, else the
+ *                    streaming kernel, else per-row; SDDMM: the pipelined
+ *                    kernel where it applies, else per-row. */
 enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2, MC_KERNEL_TMA = 3 };
 
 /* ---- Value layouts of the SpMM sparse operand --------------------------------

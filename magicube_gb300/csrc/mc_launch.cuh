@@ -55,11 +55,10 @@ inline bool spmm_tma_eligible(const mcSpmmDesc& d)
     return per_entry * (d.batch - 1) + d.k <= 0x7fffffffLL;
 }
 
-template <int V, int PA, bool S, bool H, int NT>
-int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
+template <int V, int PA, bool S, bool H, int NT, int STAGES = 4, int CW = 4>
+int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
-    constexpr int STAGES = 4;
-    using G = SpmmTmaGeom<V, PA, NT, STAGES>;
+    using G = SpmmTmaGeom<V, PA, NT, STAGES, CW>;
     const long long ntasks = (long long)d.m_vec * d.batch;
     if (ntasks > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
     const long long per_entry = d.batch > 1 ? d.rhs_stride / d.n : 0;
@@ -68,7 +67,7 @@ int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
         return fail(1, "mcSpmm: TMA tensor map encoding failed");
     unsigned int* timeouts = async_timeout_counter();
     if (!timeouts) return fail(1, "mcSpmm: timeout counter unavailable");
-    auto kern = spmm_tma_kernel<V, PA, S, H, H, NT, STAGES>;
+    auto kern = spmm_tma_kernel<V, PA, S, H, H, NT, STAGES, CW>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
         return (int)cudaGetLastError();
     // resident CTAs per SM from registers, shared memory and warps
@@ -89,6 +88,17 @@ int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     kern<<<dim3((unsigned)(gx < 1 ? 1 : gx), (unsigned)ny, 1), G::THREADS, G::SMEM, s>>>(map, p, (int)ntasks,
                                                                                         (int)per_entry, timeouts);
     return (int)cudaGetLastError();
+}
+
+// Ring depth and consumer warps per column tile, measured on GB300: a
+// 256-column tile runs 4 consumer warps (four 16-column MMA tiles each)
+// over 4 stages; a 128-column tile 2 consumer warps (four tiles each) over
+// 6 stages.  Deeper rings cost resident CTAs, which matter more.
+template <int V, int PA, bool S, bool H, int NT>
+int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
+{
+    if constexpr (NT == 256) return spmm_launch_tma_cfg<V, PA, S, H, 256, 4, 4>(d, p, s);
+    else return spmm_launch_tma_cfg<V, PA, S, H, 128, 6, 2>(d, p, s);
 }
 
 // H (half output) is compiled only with the softmax value layout (E), the
@@ -120,11 +130,7 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
             if (d.kernel_variant == MC_KERNEL_TMA && !spmm_tma_eligible(d))
                 return fail(1, "mcSpmm: the TMA kernel needs the int8 path, n % 128 == 0, 16-byte aligned values, "
                                "values_stride and rhs, and rhs_stride a multiple of n");
-            // AUTO takes the TMA kernel for 256-column tiles only: with 128
-            // columns a stage carries too few MMAs for the producer's per-step
-            // cost, and the streaming kernel measured faster.
-            if (spmm_tma_eligible(d) &&
-                (d.kernel_variant == MC_KERNEL_TMA || (d.kernel_variant == MC_KERNEL_AUTO && d.n % 256 == 0)))
+            if ((d.kernel_variant == MC_KERNEL_TMA || d.kernel_variant == MC_KERNEL_AUTO) && spmm_tma_eligible(d))
                 return d.n % 256 == 0 ? spmm_launch_tma<V, PA, S, H, 256>(d, p, s)
                                       : spmm_launch_tma<V, PA, S, H, 128>(d, p, s);
         } else {

@@ -5,13 +5,14 @@
 // 8-bit B and the int8 tensor path.  A task is one (batch entry, vector-row);
 // CTA x of the grid owns tasks x, x + gridDim.x, ... for one NT-column tile
 // of C, and their 32-slot steps flow through a STAGES-deep ring:
-//  * warp 4, the producer, loads a step's column indices (one per lane) and
+//  * warp CWARPS, the producer, loads a step's column indices (one per lane) and
 //    issues TMA tile::gather4 copies -- four B rows x 128 columns per copy,
 //    straight from the row coordinates -- plus one bulk copy of the step's
 //    value chunk, all completing the stage's "full" mbarrier; lane 0 writes a
 //    16-byte step header (row, batch entry, nonzero count, step, last/empty
 //    flags) beside them before arriving with the expected byte count;
-//  * warps 0-3, the consumers, wait for the stage, read the header, turn the
+//  * warps 0 .. CWARPS-1, the consumers (NT / (16 CWARPS) 16-column MMA
+//    tiles each), wait for the stage, read the header, turn the
 //    128-byte-swizzled [slot][column] bytes into mma.m16n8k32 A fragments with
 //    ldmatrix.m16n16.x2.trans.b8 (the value chunk is the B fragment), release
 //    the stage through its "empty" mbarrier and write finished rows of C from
@@ -29,9 +30,9 @@
 
 namespace mc {
 
-template <int V, int PREA, int NT, int STAGES>
+template <int V, int PREA, int NT, int STAGES, int CWARPS = 4>
 struct SpmmTmaGeom {
-    static constexpr int CW = 4;                      // consumer warps
+    static constexpr int CW = CWARPS;                 // consumer warps
     static constexpr int THREADS = (CW + 1) * 32;
     static constexpr int MT = NT / (16 * CW);         // 16-column MMA tiles per consumer warp
     static constexpr int SLOT_BYTES = V * PREA / 8;   // value bytes per vector slot
@@ -40,14 +41,14 @@ struct SpmmTmaGeom {
     static constexpr size_t SMEM = 1024 + (size_t)STAGES * (RHS_BYTES + AUX_BYTES) + 2 * STAGES * 8;
 };
 
-template <int V, int PREA, bool SIGNED, bool HALF_OUT, bool EXT, int NT, int STAGES>
-__global__ void __launch_bounds__(160)
+template <int V, int PREA, bool SIGNED, bool HALF_OUT, bool EXT, int NT, int STAGES, int CWARPS = 4>
+__global__ void __launch_bounds__((CWARPS + 1) * 32)
 spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, const int ntasks,
                 const int rows_per_entry, unsigned int* timeouts)
 {
     using namespace sm100;
     using L = SpmmLayout<PREA, 8, EXT>;
-    using G = SpmmTmaGeom<V, PREA, NT, STAGES>;
+    using G = SpmmTmaGeom<V, PREA, NT, STAGES, CWARPS>;
     constexpr int CW = G::CW, MT = G::MT, BP = L::BYTE_PLANES;
     constexpr int SLOT_BYTES = G::SLOT_BYTES, RHS_BYTES = G::RHS_BYTES, AUX_BYTES = G::AUX_BYTES;
     constexpr int HDR = 32 * SLOT_BYTES;              // header offset inside a stage's aux block

@@ -186,8 +186,9 @@ int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream);
 int mcQuantize(const void* in, void* out, long long count, int bits, float scale, cudaStream_t stream);
 
 /* mcQuantSoftmax: row softmax of SDDMM scores over each vector-row's stored
- * nonzeros, per vector lane: p = exp(score * scaling - max) / sum,
- * q = trunc(clamp(p * scale)) in `bits` (4, 8, 16) bits, written in the
+ * nonzeros, per vector lane: q = trunc(clamp(exp(score * scaling - max) *
+ * (scale / sum))) -- the reference's trunc(clamp(exp(..) / sum * scale)) with
+ * one division per row and lane -- in `bits` (4, 8, 16) bits, written in the
  * MC_VALUES_SOFTMAX layout at the aligned slots [start, end) of each row
  * (padding slots are not written) -- q_softmax_kernel.cu:181-271.  scores are
  * half, vector-major (j*V + v), as mcSddmm writes with out_half. */
@@ -218,7 +219,7 @@ int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, flo
  * (mcQuantize output), out: half [heads][tokens][64]; the mask in the
  * attention layout (rows aligned to 16, columns unshuffled).
  *   scores  s = half(acc / score_scale) * scaling           (as mcSddmm + softmax)
- *   MC_REQUANT_FIXED:  q = trunc(clamp(exp(s - max) / sum * prob_scale)),
+ *   MC_REQUANT_FIXED:  q = trunc(clamp(exp(s - max) * (prob_scale / sum))),
  *                      out = half(acc / out_scale) -- bit-identical to
  *                      mcSddmm + mcQuantSoftmax + mcSpmm with the same scales;
  *   MC_REQUANT_ROWMAX: q = round(127 * exp(s - max)),

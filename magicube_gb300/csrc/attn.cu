@@ -7,7 +7,9 @@
 //    quantizationKernel_{8b,4b} (sparse_transformer_magicube/src/cuda/
 //    quantization_kernel.cu:14-131), for any element count divisible by 8.
 //  * mcQuantSoftmax: per vector-row and vector lane, over the row's stored
-//    nonzeros, p = exp(x * scaling - max) / sum, q = trunc(clamp(p * scale)),
+//    nonzeros, q = trunc(clamp(exp(x * scaling - max) * (scale / sum))) (the
+//    reference divides each p by the sum, then scales; here one division per
+//    row and lane gives scale / sum),
 //    written in the value layout the SpMM reads (MC_VALUES_SOFTMAX) -- the
 //    reference's csrSoftmaxKernel_ (q_softmax_kernel.cu:181-271).  One warp per
 //    vector-row; three passes over the row (max, sum, write) read the scores
@@ -109,15 +111,25 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
     for (int v = 0; v < V; ++v)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx[v] = fmaxf(mx[v], __shfl_xor_sync(0xffffffffu, mx[v], o));
-    for (int j = lane; j < nnz; j += 32) {
+    // Lane l sums slots 2l, 2l+1, 2l+64, 2l+65, ... in that order (the order
+    // of the fused attention kernel, which reads two slots per load).
+    for (int j = 2 * lane; j < nnz; j += 64) {
         load_vec<V>(sc + (long long)j * V, x, p.scaling);
 #pragma unroll
         for (int v = 0; v < V; ++v) sum[v] += __expf(x[v] - mx[v]);
-    }
+        if (j + 1 < nnz) {
+            load_vec<V>(sc + (long long)(j + 1) * V, x, p.scaling);
 #pragma unroll
-    for (int v = 0; v < V; ++v)
+            for (int v = 0; v < V; ++v) sum[v] += __expf(x[v] - mx[v]);
+        }
+    }
+    float rs[V];  // scale / sum: one division per vector lane
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
+        rs[v] = __fdiv_rn(p.scale, sum[v]);
+    }
 
     // Every lane of the warp runs the same number of iterations (the loop
     // bound is rounded up to the warp) so the 4-bit pairing shuffle is safe.
@@ -129,7 +141,7 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
             load_vec<V>(sc + (long long)j * V, x, p.scaling);
 #pragma unroll
             for (int v = 0; v < V; ++v) {
-                float f = __expf(x[v] - mx[v]) / sum[v] * p.scale;
+                float f = __expf(x[v] - mx[v]) * rs[v];
                 f = fminf(fmaxf(f, LO), HI);
                 q[v] = (int)f;
             }

@@ -174,8 +174,13 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
         __syncthreads();
 
         // ---- 2. softmax + requantization (warp w: lanes 2w, 2w+1) ------------
-        // The maximum is exact in any order; the sum keeps the per-thread order
-        // and reduction tree of the separate softmax kernel.
+        // Lane l visits slot pairs (2l, 2l+1), (2l+64, 2l+65), ...: one 32-bit
+        // load of two half scores, one 16-bit store of two probabilities.
+        // The maximum is exact in any order; the sum keeps the per-thread
+        // order and reduction tree of the separate softmax kernel.  Every
+        // lane runs the same iterations; a __syncwarp separates the scores
+        // read in an iteration from the probability bytes written over them.
+        const int npit = (nround + 63) >> 6;
 #pragma unroll
         for (int e = 0; e < 2; ++e) {
             const int v = 2 * warp + e;
@@ -184,38 +189,50 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
             const float mx = fmaxf(fmaxf(MAXW[v], MAXW[8 + v]), fmaxf(MAXW[16 + v], MAXW[24 + v]));
             uint8_t* pv = P + v * PP;
             float sum = 0.f;
-            // In every pass that writes probabilities, a __syncwarp separates
-            // the scores read in an iteration from the bytes written over them.
             if constexpr (ROWMAX) {
-                for (int j = lane; j < nround; j += 32) {
-                    const bool in = j < nnz;
-                    const float ex = in ? __expf(__half2float(sv[j]) - mx) : 0.f;
-                    __syncwarp();
-                    int qv = 0;
-                    if (in) {
-                        sum += ex;
-                        qv = __float2int_rn(127.f * ex);
+                for (int i = 0; i < npit; ++i) {
+                    const int j = 64 * i + 2 * lane;
+                    float e0 = 0.f, e1 = 0.f;
+                    if (j < nnz) {
+                        const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
+                        e0 = __expf(x.x - mx);
+                        sum += e0;
+                        if (j + 1 < nnz) {
+                            e1 = __expf(x.y - mx);
+                            sum += e1;
+                        }
                     }
-                    pv[j] = (uint8_t)qv;
+                    __syncwarp();
+                    if (j < nround)
+                        *reinterpret_cast<uint16_t*>(pv + j) =
+                            (uint16_t)((__float2int_rn(127.f * e0) & 0xFF) | ((__float2int_rn(127.f * e1) & 0xFF) << 8));
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
             } else {
-                for (int j = lane; j < nnz; j += 32) sum += __expf(__fmul_rn(__half2float(sv[j]), p.scaling) - mx);
+                for (int i = 0; i < npit; ++i) {
+                    const int j = 64 * i + 2 * lane;
+                    if (j < nnz) {
+                        const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
+                        sum += __expf(__fmul_rn(x.x, p.scaling) - mx);
+                        if (j + 1 < nnz) sum += __expf(__fmul_rn(x.y, p.scaling) - mx);
+                    }
+                }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-                for (int j = lane; j < nround; j += 32) {
-                    const bool in = j < nnz;
-                    // the exponent is recomputed: same inputs, same value
-                    const float ex = in ? __expf(__fmul_rn(__half2float(sv[j]), p.scaling) - mx) : 0.f;
-                    __syncwarp();
-                    int qv = 0;
-                    if (in) {
-                        float f = ex / sum * p.prob_scale;
-                        f = fminf(fmaxf(f, -128.f), 127.f);
-                        qv = (int)f;
+                const float rs = __fdiv_rn(p.prob_scale, sum);
+                for (int i = 0; i < npit; ++i) {
+                    const int j = 64 * i + 2 * lane;
+                    // the exponents are recomputed: same inputs, same values
+                    int q0 = 0, q1 = 0;
+                    if (j < nnz) {
+                        const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
+                        q0 = (int)fminf(fmaxf(__expf(__fmul_rn(x.x, p.scaling) - mx) * rs, -128.f), 127.f);
+                        if (j + 1 < nnz)
+                            q1 = (int)fminf(fmaxf(__expf(__fmul_rn(x.y, p.scaling) - mx) * rs, -128.f), 127.f);
                     }
-                    pv[j] = (uint8_t)qv;
+                    __syncwarp();
+                    if (j < nround) *reinterpret_cast<uint16_t*>(pv + j) = (uint16_t)((q0 & 0xFF) | ((q1 & 0xFF) << 8));
                 }
             }
             if (lane == 0) DEN[v] = ROWMAX ? 127.f * sum * p.out_scale : p.out_scale;

@@ -156,6 +156,10 @@ typedef struct mcSpmmDesc {
     int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
     int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM / _TMA */
     int value_layout;           /* MC_VALUES_PACKED / MC_VALUES_SOFTMAX */
+    /* Optional, half output only: out[row][c] = half(acc / row_div[row]) per
+     * output row (M = m_vec * vec_length floats per batch entry, e.g. the
+     * divisors mcQuantSoftmax writes with MC_REQUANT_ROWMAX) instead of / scale. */
+    const void* row_div;  long long row_div_stride;  /* floats between batch entries */
 } mcSpmmDesc;
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream);
 
@@ -191,7 +195,12 @@ int mcQuantize(const void* in, void* out, long long count, int bits, float scale
  * one division per row and lane -- in `bits` (4, 8, 16) bits, written in the
  * MC_VALUES_SOFTMAX layout at the aligned slots [start, end) of each row
  * (padding slots are not written) -- q_softmax_kernel.cu:181-271.  scores are
- * half, vector-major (j*V + v), as mcSddmm writes with out_half. */
+ * half, vector-major (j*V + v), as mcSddmm writes with out_half.
+ * requant = MC_REQUANT_ROWMAX (bits 8) instead writes q = round(127 *
+ * exp(score * scaling - max)) and, per vector-row and lane, the divisor
+ * row_div[row * V + v] = 127 * sum * scale for mcSpmm's row_div -- the
+ * separate-launch form of mcSparseAttention's row-max mode. */
+enum { MC_REQUANT_FIXED = 0, MC_REQUANT_ROWMAX = 1 };
 typedef struct mcSoftmaxDesc {
     int m_vec, vec_length, batch, bits;
     float scaling;              /* applied to each score (1/sqrt(head_dim)) */
@@ -200,6 +209,8 @@ typedef struct mcSoftmaxDesc {
     const int* row_offsets;
     const void* scores;   long long scores_stride;  /* halves between batch entries */
     void* out;            long long out_stride;     /* bytes between batch entries */
+    int requant;                /* MC_REQUANT_FIXED (0) or MC_REQUANT_ROWMAX */
+    void* row_div;        long long row_div_stride; /* ROWMAX: float divisors, floats between batch entries */
 } mcSoftmaxDesc;
 int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
 
@@ -218,15 +229,18 @@ int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, flo
  * scores and probabilities kept on chip).  q, k, v: int8 [heads][tokens][64]
  * (mcQuantize output), out: half [heads][tokens][64]; the mask in the
  * attention layout (rows aligned to 16, columns unshuffled).
- *   scores  s = half(acc / score_scale) * scaling           (as mcSddmm + softmax)
- *   MC_REQUANT_FIXED:  q = trunc(clamp(exp(s - max) * (prob_scale / sum))),
+ *   MC_REQUANT_FIXED:  s = half(acc / score_scale) * scaling,
+ *                      q = trunc(clamp(exp(s - max) * (prob_scale / sum))),
  *                      out = half(acc / out_scale) -- bit-identical to
  *                      mcSddmm + mcQuantSoftmax + mcSpmm with the same scales;
- *   MC_REQUANT_ROWMAX: q = round(127 * exp(s - max)),
- *                      out = half(acc / (127 * sum * out_scale)).
+ *   MC_REQUANT_ROWMAX: s = half(acc / (score_scale / scaling)) (float
+ *                      quotient of the two scales), q = round(127 * exp(s -
+ *                      max)), out = half(acc / (127 * sum * out_scale)) --
+ *                      bit-identical to mcSddmm (scale = score_scale /
+ *                      scaling) + mcQuantSoftmax (ROWMAX, scaling 1, scale =
+ *                      out_scale) + mcSpmm (row_div).
  * max_row_nnz must be at least every row's nonzero count (at most 4096); a
  * longer row is skipped and *status (if given) set to 1. */
-enum { MC_REQUANT_FIXED = 0, MC_REQUANT_ROWMAX = 1 };
 typedef struct mcAttnDesc {
     int m_vec, vec_length, heads, head_dim, max_row_nnz;
     int lhs_bits, rhs_bits;     /* probabilities, Q/K/V: 8, 8 */

@@ -25,6 +25,7 @@ class McSpmmDesc(ctypes.Structure):
         ("rhs", _c_vp), ("rhs_stride", _c_ll),
         ("out", _c_vp), ("out_stride", _c_ll),
         ("mma_kind", _c_int), ("kernel_variant", _c_int), ("value_layout", _c_int),
+        ("row_div", _c_vp), ("row_div_stride", _c_ll),
     ]
 
 
@@ -48,6 +49,7 @@ class McSoftmaxDesc(ctypes.Structure):
         ("row_indices", _c_vp), ("row_offsets", _c_vp),
         ("scores", _c_vp), ("scores_stride", _c_ll),
         ("out", _c_vp), ("out_stride", _c_ll),
+        ("requant", _c_int), ("row_div", _c_vp), ("row_div_stride", _c_ll),
     ]
 
 

@@ -78,9 +78,12 @@ def to_device(mask: VectorSparse, alignment: int, device) -> AttentionMaskDev:
 
 class _AttentionCore:
     """quantize -> SDDMM -> quantized softmax -> SpMM on one mask (heads
-    batched), or quantize -> the fused attention kernel (`fused`; requant
-    "fixed" reproduces the separate steps bit for bit, "rowmax" requantizes the
-    probabilities relative to each row's maximum)."""
+    batched), or quantize -> the fused attention kernel (`fused`).  requant
+    "fixed" is the reference's absolute probability scale; "rowmax"
+    requantizes the probabilities relative to each row's maximum (the SDDMM
+    then dequantizes by scale_qkv^2 / scaling, the softmax writes per-row
+    divisors and the SpMM divides by them).  Either mode gives the same bits
+    fused and unfused."""
 
     def __init__(self, mask: AttentionMaskDev, heads: int, head_dim: int, lhs_bits: int, rhs_bits: int,
                  scale_qkv: float, scale_sfmx: float, device, tune: bool, fused: bool = False,
@@ -89,8 +92,10 @@ class _AttentionCore:
         self.requant = _lib.REQUANT_ROWMAX if requant == "rowmax" else _lib.REQUANT_FIXED
         if fused and (lhs_bits, rhs_bits, head_dim) != (8, 8, 64):
             raise ValueError("the fused attention kernel computes L8-R8 with head_dim 64")
-        if not fused and requant != "fixed":
-            raise ValueError("row-max requantization needs the fused kernel")
+        if requant not in ("fixed", "rowmax"):
+            raise ValueError("requant must be 'fixed' or 'rowmax'")
+        if requant == "rowmax" and lhs_bits != 8:
+            raise ValueError("row-max requantization writes 8-bit probabilities")
         self.status = torch.zeros(1, dtype=torch.int32, device=device)
         if head_dim % 64:
             raise ValueError("head_dim must be a multiple of 64")
@@ -107,6 +112,11 @@ class _AttentionCore:
         self.probs = None if fused else torch.zeros((heads, mask.aligned_nnz * V * lhs_bits // 32),
                                                     dtype=torch.int32, device=device)
         self.out = torch.empty((heads, L, head_dim), dtype=torch.float16, device=device)
+        # row-max mode, unfused: the softmax's per-row divisors for the SpMM
+        self.row_div = (torch.empty((heads, L), dtype=torch.float32, device=device)
+                        if not fused and self.requant == _lib.REQUANT_ROWMAX else None)
+        # the float quotient the fused kernel computes from its two scales
+        self.score_div = float(np.float32(np.float32(scale_qkv ** 2) / np.float32(self.scaling)))
         self.sddmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO, "row_split": 0}
         self.spmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO}
         self._tune = tune
@@ -121,7 +131,8 @@ class _AttentionCore:
         bytes_per_head = self.q_words * 4
         d = _lib.McSddmmDesc(
             m_vec=m.m_vec, vec_length=m.vec_length, n=m.seq_len, k=self.d, lhs_bits=self.rb, rhs_bits=self.rb,
-            is_signed=1, out_half=1, out_vecmajor=1, scale=float(self.scale_qkv ** 2), batch=self.H,
+            is_signed=1, out_half=1, out_vecmajor=1,
+            scale=self.score_div if self.row_div is not None else float(self.scale_qkv ** 2), batch=self.H,
             row_split=cfg.get("row_split", 0), row_indices=m.row_indices.data_ptr(),
             row_offsets=m.row_offsets.data_ptr(), column_indices=m.col_indices.data_ptr(),
             lhs=self.qkv_q[0].data_ptr(), lhs_stride=bytes_per_head, rhs=self.qkv_q[1].data_ptr(),
@@ -131,11 +142,14 @@ class _AttentionCore:
 
     def _softmax(self, stream) -> None:
         m = self.m
+        rowmax = self.row_div is not None
         d = _lib.McSoftmaxDesc(
-            m_vec=m.m_vec, vec_length=m.vec_length, batch=self.H, bits=self.lb, scaling=float(self.scaling),
-            scale=float(self.scale_sfmx), row_indices=m.row_indices.data_ptr(), row_offsets=m.row_offsets.data_ptr(),
-            scores=self.scores.data_ptr(), scores_stride=self.scores.shape[1], out=self.probs.data_ptr(),
-            out_stride=self.probs.shape[1] * 4)
+            m_vec=m.m_vec, vec_length=m.vec_length, batch=self.H, bits=self.lb,
+            scaling=1.0 if rowmax else float(self.scaling),
+            scale=float(self.scale_qkv) if rowmax else float(self.scale_sfmx), row_indices=m.row_indices.data_ptr(),
+            row_offsets=m.row_offsets.data_ptr(), scores=self.scores.data_ptr(), scores_stride=self.scores.shape[1],
+            out=self.probs.data_ptr(), out_stride=self.probs.shape[1] * 4, requant=self.requant,
+            row_div=self.row_div.data_ptr() if rowmax else None, row_div_stride=m.seq_len if rowmax else 0)
         _lib.check(_lib.lib().mcQuantSoftmax(ctypes.byref(d), stream), "mcQuantSoftmax")
 
     def _spmm(self, cfg: dict, stream) -> None:
@@ -147,7 +161,9 @@ class _AttentionCore:
             column_indices=m.col_indices.data_ptr(), values=self.probs.data_ptr(),
             values_stride=self.probs.shape[1] * 4, rhs=self.qkv_q[2].data_ptr(), rhs_stride=self.q_words * 4,
             out=self.out.data_ptr(), out_stride=m.seq_len * self.d, mma_kind=cfg["mma_kind"],
-            kernel_variant=cfg["variant"], value_layout=_lib.VALUES_SOFTMAX)
+            kernel_variant=cfg["variant"], value_layout=_lib.VALUES_SOFTMAX,
+            row_div=self.row_div.data_ptr() if self.row_div is not None else None,
+            row_div_stride=m.seq_len if self.row_div is not None else 0)
         _lib.check(_lib.lib().mcSpmm(ctypes.byref(d), stream), "mcSpmm")
 
     def tune(self, qkv: torch.Tensor) -> None:
@@ -243,10 +259,11 @@ class PerInstanceSparseAttention:
     """The plain baseline: the same steps launched separately per instance."""
 
     def __init__(self, masks: list[VectorSparse], heads: int, head_dim: int = 64, lhs_bits: int = 8,
-                 rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 32.0, device="cuda"):
+                 rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 32.0, device="cuda",
+                 requant: str = "fixed"):
         align = 16 if rhs_bits == 8 else 32
         self.cores = [_AttentionCore(to_device(m, align, device), heads, head_dim, lhs_bits, rhs_bits, scale_qkv,
-                                     scale_sfmx, device, tune=False) for m in masks]
+                                     scale_sfmx, device, tune=False, requant=requant) for m in masks]
         self.seq_lens = [m.ncols for m in masks]
 
     def __call__(self, qkvs: list[torch.Tensor]) -> list[torch.Tensor]:

@@ -61,6 +61,8 @@ struct SoftmaxParams {
     uint8_t* out;             // per batch entry: aligned_nnz * V * BITS / 8 bytes
     long long out_stride;     // bytes
     float scaling, scale;
+    float* row_div;           // MC_REQUANT_ROWMAX: per batch entry, m_vec * V divisors
+    long long row_div_stride; // floats
 };
 
 template <int V>
@@ -84,9 +86,13 @@ __device__ __forceinline__ void load_vec(const __half* p, float (&x)[V], float s
     }
 }
 
-template <int V, int BITS>
+// ROWMAX (8 bits): q = round(127 exp(x - max)), and lane 0 writes the row
+// divisors 127 * sum * scale -- the separate-launch form of the fused
+// kernel's row-max mode (same expressions, same summation order).
+template <int V, int BITS, bool ROWMAX = false>
 __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams p)
 {
+    static_assert(!ROWMAX || BITS == 8, "row-max requantization writes 8-bit probabilities");
     constexpr float LO = BITS == 16 ? -32768.f : (BITS == 8 ? -128.f : -8.f);
     constexpr float HI = BITS == 16 ? 32767.f : (BITS == 8 ? 127.f : 7.f);
     const int lane = threadIdx.x & 31;
@@ -128,7 +134,14 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
     for (int v = 0; v < V; ++v) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
-        rs[v] = __fdiv_rn(p.scale, sum[v]);
+        rs[v] = ROWMAX ? 0.f : __fdiv_rn(p.scale, sum[v]);
+    }
+    if constexpr (ROWMAX) {
+        if (lane == 0) {
+            float* dv = p.row_div + (long long)b * p.row_div_stride + (long long)row * V;
+#pragma unroll
+            for (int v = 0; v < V; ++v) dv[v] = 127.f * sum[v] * p.scale;
+        }
     }
 
     // Every lane of the warp runs the same number of iterations (the loop
@@ -141,9 +154,13 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
             load_vec<V>(sc + (long long)j * V, x, p.scaling);
 #pragma unroll
             for (int v = 0; v < V; ++v) {
-                float f = __expf(x[v] - mx[v]) * rs[v];
-                f = fminf(fmaxf(f, LO), HI);
-                q[v] = (int)f;
+                if constexpr (ROWMAX) {
+                    q[v] = __float2int_rn(127.f * __expf(x[v] - mx[v]));
+                } else {
+                    float f = __expf(x[v] - mx[v]) * rs[v];
+                    f = fminf(fmaxf(f, LO), HI);
+                    q[v] = (int)f;
+                }
             }
         } else {
 #pragma unroll
@@ -213,13 +230,27 @@ extern "C" int mcQuantSoftmax(const mcSoftmaxDesc* d, cudaStream_t stream)
     if (!d->row_indices || !d->row_offsets || !d->scores || !d->out) return mc::fail(1, "mcQuantSoftmax: null pointer");
     if (reinterpret_cast<uintptr_t>(d->scores) % 16 || d->scores_stride % 8)
         return mc::fail(1, "mcQuantSoftmax: scores must be 16-byte aligned, stride a multiple of 8 halves");
+    if (d->requant != MC_REQUANT_FIXED && d->requant != MC_REQUANT_ROWMAX)
+        return mc::fail(1, "mcQuantSoftmax: requant must be MC_REQUANT_FIXED or MC_REQUANT_ROWMAX");
+    if (d->requant == MC_REQUANT_ROWMAX &&
+        (d->bits != 8 || !d->row_div || reinterpret_cast<uintptr_t>(d->row_div) % 4 || d->row_div_stride < 0))
+        return mc::fail(1, "mcQuantSoftmax: row-max requantization needs bits 8 and a 4-byte aligned row_div");
     mc::SoftmaxParams p;
     p.m_vec = d->m_vec; p.batch = d->batch;
     p.row_indices = d->row_indices; p.row_offsets = d->row_offsets;
     p.scores = static_cast<const __half*>(d->scores); p.scores_stride = d->scores_stride;
     p.out = static_cast<uint8_t*>(d->out); p.out_stride = d->out_stride;
     p.scaling = d->scaling; p.scale = d->scale;
+    p.row_div = static_cast<float*>(d->row_div); p.row_div_stride = d->row_div_stride;
     dim3 grid((unsigned)((d->m_vec + 3) / 4), (unsigned)d->batch);
+    if (d->requant == MC_REQUANT_ROWMAX) {
+        switch (d->vec_length) {
+            case 2: mc::quant_softmax_kernel<2, 8, true><<<grid, 128, 0, stream>>>(p); break;
+            case 4: mc::quant_softmax_kernel<4, 8, true><<<grid, 128, 0, stream>>>(p); break;
+            default: mc::quant_softmax_kernel<8, 8, true><<<grid, 128, 0, stream>>>(p); break;
+        }
+        return (int)cudaGetLastError();
+    }
 #define MC_SM(V, B) mc::quant_softmax_kernel<V, B><<<grid, 128, 0, stream>>>(p)
 #define MC_SMV(B)                                           \
     switch (d->vec_length) {                                \

@@ -7,15 +7,18 @@
 //      (mma.m16n8k32 s8, K rows gathered with 128-bit loads straight into the
 //      A fragment, Q rows in registers), dequantised exactly as the separate
 //      SDDMM does (half(acc / scale_qkv^2)) and multiplied by the softmax
-//      scaling, kept as the half [v][slot] (MC_REQUANT_ROWMAX keeps the int32
-//      accumulator times scaling / scale^2, rounded once to half);
+//      scaling, kept as the half [v][slot] (MC_REQUANT_ROWMAX keeps
+//      half(acc / (scale_qkv^2 / scaling)), the separate SDDMM's output at
+//      that scale);
 //   2. softmax per vector lane: max, sum of exp, requantization to int8
 //      [v][slot] -- warp w owns lanes 2w, 2w+1 and visits slots in the same
 //      per-thread order and reduction tree as the separate softmax kernel,
 //      so with MC_REQUANT_FIXED every probability equals its output bit for
 //      bit; MC_REQUANT_ROWMAX instead stores q = round(127 exp(s - max)) and
 //      dequantises the output by 127 * sum * scale_qkv per lane (probabilities
-//      keep 7 bits relative to the row maximum instead of an absolute scale);
+//      keep 7 bits relative to the row maximum instead of an absolute scale),
+//      equal bit for bit to the separate softmax's row-max mode followed by
+//      the SpMM with those per-row divisors;
 //   3. SpMM: P (int8, from shared memory) times the gathered V rows, split
 //      over the slots: warp w takes 32-slot steps w, w+4, ..., stages their V
 //      rows through its own 2-deep cp.async ring, transposes them with
@@ -44,7 +47,8 @@ struct AttnParams {
     long long head_stride;      // bytes between heads of q, k, v
     __half* out;
     long long out_head_stride;  // halves between heads of out
-    float score_scale;          // scores = half(acc / score_scale)
+    float score_scale;          // fixed mode: scores = half(acc / score_scale)
+    float score_div;            // row-max mode: scores = half(acc / score_div), score_div = score_scale / scaling
     float scaling;              // softmax input scaling
     float prob_scale;           // fixed requantization scale
     float out_scale;            // output divisor (fixed) or its per-lane factor (row-max)
@@ -122,7 +126,6 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
 
         // ---- 1. scores: warp w takes tiles w, w+4, ...; two tiles in flight ----
         const int ntiles = (nnz + 15) >> 4;
-        const float sfac = p.scaling / p.score_scale;  // row-max mode: no half rounding
         float mxl[2] = {-FLT_MAX, -FLT_MAX};           // running max of lanes 2t, 2t+1
         auto store_scores = [&](int tile, const int (&acc)[4]) {
             if (2 * t >= V) return;
@@ -132,12 +135,12 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
                 if (j >= nnz) continue;
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {
-                    // Fixed mode keeps the separate SDDMM's half output
-                    // (scaled on every read); row-max mode the half-rounded
-                    // scaled score.  The maximum is taken of what is stored.
+                    // Both modes keep the separate SDDMM's half output (fixed
+                    // mode scales it on every read, row-max mode has the
+                    // scaling folded into the divisor).  The maximum is
+                    // taken of what the softmax reads.
                     const int a = acc[2 * hh + e];
-                    const __half hs = ROWMAX ? __float2half_rn(__int2float_rn(a) * sfac)
-                                             : deq_half(a, p.score_scale);
+                    const __half hs = deq_half(a, ROWMAX ? p.score_div : p.score_scale);
                     S[(2 * t + e) * SP + j] = hs;
                     mxl[e] = fmaxf(mxl[e], ROWMAX ? __half2float(hs) : __fmul_rn(__half2float(hs), p.scaling));
                 }
@@ -362,6 +365,7 @@ extern "C" int mcSparseAttention(const mcAttnDesc* d, cudaStream_t stream)
     p.out_head_stride = d->out_head_stride;
     p.score_scale = d->score_scale;
     p.scaling = d->scaling;
+    p.score_div = d->score_scale / d->scaling;
     p.prob_scale = d->prob_scale;
     p.out_scale = d->out_scale;
     p.status = d->status;

@@ -46,7 +46,11 @@ static int check_spmm(const mcSpmmDesc& d)
     if (d.value_layout != (d.out_half ? MC_VALUES_SOFTMAX : MC_VALUES_PACKED))
         return fail(1, "mcSpmm: half output is built for the softmax value layout and int32 output for the "
                        "packer layout");
-    if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSpmm: half output requires a nonzero scale");
+    if (d.out_half && !d.row_div && !(d.scale != 0.0f))
+        return fail(1, "mcSpmm: half output requires a nonzero scale or row divisors");
+    if (d.row_div && !d.out_half) return fail(1, "mcSpmm: row divisors apply to half output only");
+    if (d.row_div && (reinterpret_cast<uintptr_t>(d.row_div) % 4 || (d.batch > 1 && d.row_div_stride < 0)))
+        return fail(1, "mcSpmm: row_div must be 4-byte aligned with a non-negative stride");
     if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16)
         return fail(1, "mcSpmm: invalid mma_kind (the SpMM runs on MC_MMA_INT8 or MC_MMA_F16)");
     if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_TMA)

@@ -172,6 +172,8 @@ int spmm_launch(const mcSpmmDesc& d, cudaStream_t s)
     p.rhs = static_cast<const uint8_t*>(d.rhs); p.rhs_stride = d.rhs_stride;
     p.out = d.out; p.out_stride = d.out_stride;
     p.scale = d.scale;
+    p.row_div = static_cast<const float*>(d.row_div);
+    p.row_div_stride = d.row_div_stride;
 #define MC_V(V)                                                                         \
     if (d.out_half) return spmm_launch_v<V, PA, PB, true, true>(d, p, s);               \
     if (d.is_signed) return spmm_launch_v<V, PA, PB, true, false>(d, p, s);             \

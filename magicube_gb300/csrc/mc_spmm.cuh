@@ -43,7 +43,15 @@ struct SpmmParams {
     void* out;                // M x N (int32 or half)
     long long out_stride;     // elements between batch entries
     float scale;              // dequantisation divisor for half output
+    const float* row_div;     // optional per-output-row divisors for half output (replaces scale)
+    long long row_div_stride; // floats between batch entries of row_div
 };
+
+// Divisor of output row `orow` of batch entry b for half output.
+__device__ __forceinline__ float out_divisor(const SpmmParams& p, int b, int orow)
+{
+    return p.row_div ? __ldg(p.row_div + (long long)b * p.row_div_stride + orow) : p.scale;
+}
 
 // Value layouts.  PACKED (EXT = false): the reference host packer's layout
 // (spmm_benchmark.cpp:224-377): chunks of MMA_K slots holding PLANES bit-planes
@@ -401,8 +409,9 @@ spmm_kernel(const SpmmParams p)
         const long long o = (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + ncol;
         if constexpr (HALF_OUT) {
             __half* out = reinterpret_cast<__half*>(p.out) + o;
-            uint32_t h0 = pack_half2(res[e2][0], res[e2][1], p.scale);
-            uint32_t h1 = pack_half2(res[e2][2], res[e2][3], p.scale);
+            const float dv = out_divisor(p, b, row * V + v);
+            uint32_t h0 = pack_half2(res[e2][0], res[e2][1], dv);
+            uint32_t h1 = pack_half2(res[e2][2], res[e2][3], dv);
             stg_cs_v2(out, (int)h0, (int)h1);
         } else {
             int* out = reinterpret_cast<int*>(p.out) + o;

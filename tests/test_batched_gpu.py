@@ -88,6 +88,31 @@ def test_fused_fixed_equals_separate_steps(cuda, V):
     assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_fused_rowmax_equals_separate_and_per_instance(cuda, V):
+    """Row-max requantization gives the same bits fused (one launch), as
+    separate batched launches (SDDMM, row-max softmax writing per-row
+    divisors, SpMM dividing by them) and as per-instance launches."""
+    lens = [64, 512, 128, 1024, 192]
+    masks = [synth.band_random_mask(L, V, 64, 0.8, seed=60 + i) for i, L in enumerate(lens)]
+    H, d = 2, 64
+    qkv = (torch.randn(3, H, sum(lens), d, generator=torch.Generator().manual_seed(6)) * 0.5).half().to(cuda)
+    kw = dict(scale_qkv=60.0, scale_sfmx=127.0, device=cuda, requant="rowmax")
+    sep = batched.BatchedSparseAttention(masks, H, d, tune=False, **kw)
+    fus = batched.BatchedSparseAttention(masks, H, d, fused=True, **kw)
+    per = batched.PerInstanceSparseAttention(masks, H, d, **kw)
+    a = sep(qkv).clone()
+    b = fus(qkv).clone()
+    offs = sep.token_offsets
+    outs = per([qkv[:, :, int(offs[i]):int(offs[i + 1])].contiguous() for i in range(len(lens))])
+    torch.cuda.synchronize()
+    assert int(fus.core.status.item()) == 0
+    assert torch.isfinite(a).all()
+    assert torch.equal(a, b)
+    for i, o in enumerate(outs):
+        assert torch.equal(fus.instance_output(i), o), f"instance {i}"
+
+
 def test_fused_rowmax_error_vs_fp64(cuda):
     """Row-max requantization keeps 7 bits relative to each row's largest
     probability: the output error against the float64 unquantized attention

@@ -224,6 +224,14 @@ int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
 int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, float* ms_out,
                       double* ops_out, cudaStream_t stream);
 
+/* mcCheckQuotients: compares, bit for bit, the dequantisation quotient the
+ * kernels compute from a prepared divisor (RN(1/d) and two FMA correction
+ * steps) with the IEEE division a / d for every integer numerator a in
+ * [lo, hi) (within the int32 range).  counters: device buffer of two 8-byte
+ * words; word 0 accumulates the mismatches, word 1 (signed) is lowered to the
+ * first mismatching numerator -- initialise them to 0 and hi. */
+int mcCheckQuotients(float divisor, long long lo, long long hi, void* counters, cudaStream_t stream);
+
 /* mcSparseAttention: the quantized sparse attention of every vector-row and
  * head in one persistent kernel (SDDMM, softmax + requantization, SpMM with
  * scores and probabilities kept on chip).  q, k, v: int8 [heads][tokens][64]

@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int g = lane >> 2, t = lane & 3;
     uint8_t* ring = rings + warp * STAGES * 32 * ROW;  // this warp's private V-row ring
+    const Divisor sdiv = make_divisor(ROWMAX ? p.score_div : p.score_scale);  // scores = half(acc / sdiv)
 
 #pragma unroll 1
     for (int item = blockIdx.x; item < p.items; item += gridDim.x) {
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
                     // scaling folded into the divisor).  The maximum is
                     // taken of what the softmax reads.
                     const int a = acc[2 * hh + e];
-                    const __half hs = deq_half(a, ROWMAX ? p.score_div : p.score_scale);
+                    const __half hs = deq_half(a, sdiv);
                     S[(2 * t + e) * SP + j] = hs;
                     mxl[e] = fmaxf(mxl[e], ROWMAX ? __half2float(hs) : __fmul_rn(__half2float(hs), p.scaling));
                 }
@@ -292,11 +293,11 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
         // tot: column n = 16 warp + g (+8 for tot[2], tot[3]), lane v = 2t (+1 for odd)
         if (2 * t < V) {
             __half* o = p.out + (long long)h * p.out_head_stride + (long long)(row * V + 2 * t) * 64 + 16 * warp + g;
-            const float d0 = DEN[2 * t], d1 = DEN[2 * t + 1];
-            o[0] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[0]), d0));
-            o[64] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[1]), d1));
-            o[8] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[2]), d0));
-            o[72] = __float2half_rn(__fdiv_rn(__int2float_rn(tot[3]), d1));
+            const Divisor d0 = make_divisor(DEN[2 * t]), d1 = make_divisor(DEN[2 * t + 1]);
+            o[0] = deq_half(tot[0], d0);
+            o[64] = deq_half(tot[1], d1);
+            o[8] = deq_half(tot[2], d0);
+            o[72] = deq_half(tot[3], d1);
         }
     }
 }

@@ -195,16 +195,47 @@ __device__ __forceinline__ void stg_cs_s32(void* p, int a)
     asm volatile("st.global.cs.s32 [%0], %1;" ::"l"(p), "r"(a) : "memory");
 }
 
+// A divisor prepared once for many correctly rounded quotients a / d.
+// r = RN(1/d) where the fast quotient below applies (|d| in [2^-60, 2^60]),
+// else 0 (the quotient then uses the IEEE division).
+struct Divisor {
+    float d, r;
+};
+__device__ __forceinline__ Divisor make_divisor(float d)
+{
+    const float ad = fabsf(d);
+    return {d, (ad >= 0x1p-60f && ad <= 0x1p60f) ? __frcp_rn(d) : 0.f};
+}
+
+// RN(a / d) by Markstein's correction step (P. Markstein, "Computation of
+// elementary functions on the IBM RISC System/6000 processor", IBM J. Res.
+// Develop. 34(1), 1990): with y = RN(1/d) and a quotient q within one ulp of
+// a/d, the remainder a - q d is exact in one FMA and RN(q + (a - q d) y) is
+// the correctly rounded quotient.  q0 = RN(a y) can be up to 1.5 ulps off,
+// so a first correction makes it faithful and a second one rounds it
+// correctly.  Valid for |a| < 2^32 (integer accumulators) with |d| in
+// [2^-60, 2^60]: no step overflows or leaves the normal range.  Checked bit
+// for bit against __fdiv_rn over every int32 numerator (mcCheckQuotients).
+__device__ __forceinline__ float div_rn(float a, Divisor v)
+{
+    if (v.r == 0.f) return __fdiv_rn(a, v.d);
+    float q = __fmul_rn(a, v.r);
+    float r = __fmaf_rn(-q, v.d, a);
+    q = __fmaf_rn(r, v.r, q);
+    r = __fmaf_rn(-q, v.d, a);
+    return __fmaf_rn(r, v.r, q);
+}
+
 // Dequantised half output: half(float(acc) / scale), both steps rounded to
 // nearest -- the epilogue of the reference's extension kernels
 // (sparse_transformer_magicube/src/cuda/spmm_utils/output_tile.h:119).
-__device__ __forceinline__ __half deq_half(int acc, float scale)
+__device__ __forceinline__ __half deq_half(int acc, Divisor v)
 {
-    return __float2half_rn(__fdiv_rn(__int2float_rn(acc), scale));
+    return __float2half_rn(div_rn(__int2float_rn(acc), v));
 }
-__device__ __forceinline__ uint32_t pack_half2(int a, int b, float scale)
+__device__ __forceinline__ uint32_t pack_half2(int a, int b, Divisor v)
 {
-    __half2 h = __halves2half2(deq_half(a, scale), deq_half(b, scale));
+    __half2 h = __halves2half2(deq_half(a, v), deq_half(b, v));
     return *reinterpret_cast<uint32_t*>(&h);
 }
 

@@ -79,6 +79,7 @@ template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, 
 __global__ void __launch_bounds__(WARPS * 32)
 sddmm_kernel(const SddmmParams p)
 {
+    const Divisor dq = make_divisor(p.scale);  // half output: acc / scale
     constexpr int PA = BytePlanes<PREA>::N, PB = BytePlanes<PREB>::N;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
@@ -230,7 +231,7 @@ sddmm_kernel(const SddmmParams p)
                 if constexpr (VECMAJOR) {
                     const long long o = base + j * V + 2 * t;
                     if constexpr (HALF_OUT) {
-                        stg_cs_s32(reinterpret_cast<__half*>(p.out) + o, (int)pack_half2(d[2 * hh], d[2 * hh + 1], p.scale));
+                        stg_cs_s32(reinterpret_cast<__half*>(p.out) + o, (int)pack_half2(d[2 * hh], d[2 * hh + 1], dq));
                     } else {
                         stg_cs_v2(reinterpret_cast<int*>(p.out) + o, d[2 * hh], d[2 * hh + 1]);
                     }
@@ -239,8 +240,8 @@ sddmm_kernel(const SddmmParams p)
                     const long long o = base + (j >> 3) * 8 * V + 8 * (2 * t) + (j & 7);
                     if constexpr (HALF_OUT) {
                         __half* out = reinterpret_cast<__half*>(p.out) + o;
-                        out[0] = deq_half(d[2 * hh], p.scale);
-                        out[8] = deq_half(d[2 * hh + 1], p.scale);
+                        out[0] = deq_half(d[2 * hh], dq);
+                        out[8] = deq_half(d[2 * hh + 1], dq);
                     } else {
                         int* out = reinterpret_cast<int*>(p.out) + o;
                         stg_cs_s32(out, d[2 * hh]);

@@ -30,6 +30,7 @@ template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, 
 __global__ void __launch_bounds__(WARPS * 32)
 sddmm_k64_kernel(const SddmmParams p)
 {
+    const Divisor dq = make_divisor(p.scale);  // half output: acc / scale
     constexpr int PA = BytePlanes<PREA>::N, PB = BytePlanes<PREB>::N;
     constexpr int RHS_ROW = 64 * PREB / 8, LHS_ROW = 64 * PREA / 8;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -158,15 +159,15 @@ sddmm_k64_kernel(const SddmmParams p)
                     if constexpr (VECMAJOR) {
                         const long long o = obase + jl * V + 2 * t;
                         if constexpr (HALF_OUT)
-                            stg_cs_s32(reinterpret_cast<__half*>(p.out) + o, (int)pack_half2(d[2 * hh], d[2 * hh + 1], p.scale));
+                            stg_cs_s32(reinterpret_cast<__half*>(p.out) + o, (int)pack_half2(d[2 * hh], d[2 * hh + 1], dq));
                         else
                             stg_cs_v2(reinterpret_cast<int*>(p.out) + o, d[2 * hh], d[2 * hh + 1]);
                     } else {
                         const long long o = obase + (jl >> 3) * 8 * V + 16 * t + (jl & 7);
                         if constexpr (HALF_OUT) {
                             __half* out = reinterpret_cast<__half*>(p.out) + o;
-                            out[0] = deq_half(d[2 * hh], p.scale);
-                            out[8] = deq_half(d[2 * hh + 1], p.scale);
+                            out[0] = deq_half(d[2 * hh], dq);
+                            out[8] = deq_half(d[2 * hh + 1], dq);
                         } else {
                             int* out = reinterpret_cast<int*>(p.out) + o;
                             stg_cs_s32(out, d[2 * hh]);

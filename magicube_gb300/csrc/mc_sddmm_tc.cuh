@@ -34,6 +34,7 @@ template <int V, bool SIGNED, bool VECMAJOR, bool HALF_OUT>
 __global__ void __launch_bounds__(128)
 sddmm_tc_kernel(const SddmmParams p, const int items)
 {
+    const Divisor dq = make_divisor(p.scale);  // half output: acc / scale
     using namespace sm100;
     constexpr int ROWS = 128;                 // nonzeros per chunk (MMA M)
     constexpr int N = 16;                     // MMA N (V rows of A, zero-padded)
@@ -158,7 +159,7 @@ sddmm_tc_kernel(const SddmmParams p, const int items)
                         __half* out = reinterpret_cast<__half*>(p.out) + o;
 #pragma unroll
                         for (int v = 0; v < V; v += 2)
-                            *reinterpret_cast<uint32_t*>(out + v) = pack_half2(d[v], d[v + 1], p.scale);
+                            *reinterpret_cast<uint32_t*>(out + v) = pack_half2(d[v], d[v + 1], dq);
                     } else {
                         int* out = reinterpret_cast<int*>(p.out) + o;
 #pragma unroll
@@ -168,7 +169,7 @@ sddmm_tc_kernel(const SddmmParams p, const int items)
                     const long long o = obase + (long long)(j >> 3) * 8 * V + (j & 7);
 #pragma unroll
                     for (int v = 0; v < V; ++v) {
-                        if constexpr (HALF_OUT) reinterpret_cast<__half*>(p.out)[o + 8 * v] = deq_half(d[v], p.scale);
+                        if constexpr (HALF_OUT) reinterpret_cast<__half*>(p.out)[o + 8 * v] = deq_half(d[v], dq);
                         else stg_cs_s32(reinterpret_cast<int*>(p.out) + o + 8 * v, d[v]);
                     }
                 }

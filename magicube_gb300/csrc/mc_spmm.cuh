@@ -48,9 +48,9 @@ struct SpmmParams {
 };
 
 // Divisor of output row `orow` of batch entry b for half output.
-__device__ __forceinline__ float out_divisor(const SpmmParams& p, int b, int orow)
+__device__ __forceinline__ Divisor out_divisor(const SpmmParams& p, int b, int orow)
 {
-    return p.row_div ? __ldg(p.row_div + (long long)b * p.row_div_stride + orow) : p.scale;
+    return make_divisor(p.row_div ? __ldg(p.row_div + (long long)b * p.row_div_stride + orow) : p.scale);
 }
 
 // Value layouts.  PACKED (EXT = false): the reference host packer's layout
@@ -409,7 +409,7 @@ spmm_kernel(const SpmmParams p)
         const long long o = (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + ncol;
         if constexpr (HALF_OUT) {
             __half* out = reinterpret_cast<__half*>(p.out) + o;
-            const float dv = out_divisor(p, b, row * V + v);
+            const Divisor dv = out_divisor(p, b, row * V + v);
             uint32_t h0 = pack_half2(res[e2][0], res[e2][1], dv);
             uint32_t h1 = pack_half2(res[e2][2], res[e2][3], dv);
             stg_cs_v2(out, (int)h0, (int)h1);

@@ -309,7 +309,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
                     // columns g, g+8, ..., g + 8 (2 MT - 1)
                     if constexpr (HALF_OUT) {
                         __half* o = reinterpret_cast<__half*>(p.out) + obase + g;
-                        const float dv = out_divisor(p, b, row * V + v);
+                        const Divisor dv = out_divisor(p, b, row * V + v);
 #pragma unroll
                         for (int q = 0; q < 2 * MT; ++q) o[8 * q] = deq_half(r4[q], dv);
                     } else {
@@ -321,7 +321,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
                     // columns 4g .. 4g+3
                     if constexpr (HALF_OUT) {
                         __half* o = reinterpret_cast<__half*>(p.out) + obase + 4 * g;
-                        const float dv = out_divisor(p, b, row * V + v);
+                        const Divisor dv = out_divisor(p, b, row * V + v);
                         stg_cs_v2(o, (int)pack_half2(r4[0], r4[1], dv), (int)pack_half2(r4[2], r4[3], dv));
                     } else {
                         stg_cs_v4(reinterpret_cast<int*>(p.out) + obase + 4 * g, r4[0], r4[1], r4[2], r4[3]);

@@ -249,7 +249,7 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
                     (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + warp * 16 * MT + g;
                 if constexpr (HALF_OUT) {
                     __half* o = reinterpret_cast<__half*>(p.out) + obase;
-                    const float dv = out_divisor(p, b, row * V + v);
+                    const Divisor dv = out_divisor(p, b, row * V + v);
 #pragma unroll
                     for (int q = 0; q < 2 * MT; ++q) o[8 * q] = deq_half(r4[q], dv);
                 } else {

@@ -4,8 +4,39 @@
 #include <cstdint>
 
 #include "mc_host.h"
+#include "mc_ptx.cuh"
 
 namespace mc {
+
+// Compares div_rn (the kernels' quotient from a prepared divisor) with the
+// IEEE division __fdiv_rn for every integer numerator in [lo, hi), bit for
+// bit; counters[0] += mismatches, counters[1] = min(first mismatching
+// numerator).
+__global__ void __launch_bounds__(256) quotient_check_kernel(float d, long long lo, long long hi,
+                                                             unsigned long long* counters)
+{
+    const Divisor v = make_divisor(d);
+    unsigned long long bad = 0;
+    long long first = hi;
+    const long long step = (long long)gridDim.x * blockDim.x;
+    for (long long a = lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; a < hi; a += step) {
+        const float x = __int2float_rn((int)a);
+        if (__float_as_uint(div_rn(x, v)) != __float_as_uint(__fdiv_rn(x, d))) {
+            ++bad;
+            if (a < first) first = a;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+        const long long f = __shfl_xor_sync(0xffffffffu, first, o);
+        first = f < first ? f : first;
+    }
+    if ((threadIdx.x & 31) == 0 && bad) {
+        atomicAdd(counters, bad);
+        atomicMin(reinterpret_cast<long long*>(counters + 1), first);
+    }
+}
 
 template <int KIND>
 __global__ void __launch_bounds__(256) tensor_peak_kernel(int* out, int iters, unsigned seed)
@@ -72,5 +103,16 @@ extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int
     cudaEventDestroy(e1);
     const double macs = kind == 0 ? 16.0 * 8 * 32 : (kind == 1 ? 16.0 * 8 * 64 : 16.0 * 8 * 16);  // kinds 2, 3: k = 16
     *ops_out = 2.0 * macs * (double)blocks * (threads / 32) * iters * 8;
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mcCheckQuotients(float divisor, long long lo, long long hi, void* counters, cudaStream_t stream)
+{
+    mc::clear_error();
+    if (!counters || reinterpret_cast<uintptr_t>(counters) % 8 || lo < -2147483648LL || hi > 2147483648LL || lo > hi)
+        return mc::fail(1, "mcCheckQuotients: counters must be 8-byte aligned; [lo, hi) must lie in the int32 range");
+    if (lo == hi) return 0;
+    const int blocks = mc::sm_count() * 8;
+    mc::quotient_check_kernel<<<blocks, 256, 0, stream>>>(divisor, lo, hi, static_cast<unsigned long long*>(counters));
     return (int)cudaGetLastError();
 }

@@ -688,34 +688,41 @@ def serving_suite(args, dev) -> dict:
     """Continuous batching of a 2-layer sparse encoder (hidden 256, 4 x 64
     heads, FFN 1024, random-init weights), int8 vector-sparse attention at
     sparsity 0.95; Poisson arrivals at each rate of `--serving-rates`, lengths
-    lognormal (median 2048, clipped to [256, 8192]); against serving the same
-    requests one at a time."""
+    lognormal (median 2048, clipped to [256, 8192]).  The server runs the
+    fused attention kernel; the baseline serves the same requests one at a
+    time on the plain separate SDDMM / softmax / SpMM launches (same bits,
+    fixed requantization)."""
     import torch
 
     from magicube_gb300 import model, serving
     torch.manual_seed(0)
     enc = model.SparseEncoder(2, 256, 4, 1024).to(dev).half().eval()
+    fused = lambda: enc.set_attention("fused")  # noqa: E731
+    plain = lambda: enc.set_attention("separate")  # noqa: E731
     warm = serving.make_requests(4, 0.0, seed=99)
-    serving.ContinuousBatchingServer(enc, device=dev).serve(warm)
-    serving.serve_sequential(enc, serving.make_requests(2, 0.0, seed=98), device=dev)
+    serving.ContinuousBatchingServer(fused(), device=dev).serve(warm)
+    serving.serve_sequential(plain(), serving.make_requests(2, 0.0, seed=98), device=dev)
     out = []
     for rate in args.serving_rates:
         # Each server first serves the same request set unmeasured, so both
         # measured runs see warmed allocator pools for the same shapes.
-        serving.ContinuousBatchingServer(enc, max_inflight=3, overlap_tokens=args.serving_overlap_tokens,
+        serving.ContinuousBatchingServer(fused(), max_inflight=3, overlap_tokens=args.serving_overlap_tokens,
                                          device=dev).serve(serving.make_requests(args.serving_requests, rate, seed=5))
         reqs = serving.make_requests(args.serving_requests, rate, seed=5)
-        srv = serving.ContinuousBatchingServer(enc, max_inflight=3, overlap_tokens=args.serving_overlap_tokens,
+        srv = serving.ContinuousBatchingServer(fused(), max_inflight=3, overlap_tokens=args.serving_overlap_tokens,
                                                device=dev)
         cb = srv.serve(reqs)
-        serving.serve_sequential(enc, serving.make_requests(args.serving_requests, rate, seed=5), device=dev)
-        seq = serving.serve_sequential(enc, serving.make_requests(args.serving_requests, rate, seed=5), device=dev)
+        serving.serve_sequential(plain(), serving.make_requests(args.serving_requests, rate, seed=5), device=dev)
+        seq = serving.serve_sequential(plain(), serving.make_requests(args.serving_requests, rate, seed=5),
+                                       device=dev)
         out.append({"arrival_rate": rate, "overlap_tokens": args.serving_overlap_tokens, "continuous": cb,
                     "sequential": seq,
                     "mean_batch": float(np.mean([len(b) for b in srv.batches])),
                     "req_per_s_ratio": cb["req_per_s"] / seq["req_per_s"]})
     return {"config": "2-layer sparse encoder, hidden 256, 4x64 heads, FFN 1024, sparsity 0.95, "
-                      "lengths lognormal(median 2048) in [256, 8192]", "runs": out}
+                      "lengths lognormal(median 2048) in [256, 8192]",
+            "kernels": {"continuous": "fused attention kernel", "sequential": "separate SDDMM/softmax/SpMM"},
+            "runs": out}
 
 
 def tensor_peaks(dev) -> dict:

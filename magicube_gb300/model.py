@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
 import torch
 import torch.nn as nn
 import torch.nn.functional as F
@@ -23,7 +24,7 @@ from .projection import qkv_project_quantize
 
 def attention_core(qkv: torch.Tensor, mask: AttentionMaskDev, head_dim: int, lhs_bits: int, rhs_bits: int,
                    scale_qkv: float, scale_sfmx: float, sddmm_cfg: dict | None = None,
-                   spmm_cfg: dict | None = None) -> torch.Tensor:
+                   spmm_cfg: dict | None = None, requant: str = "fixed") -> torch.Tensor:
     """qkv: [3, H, T, d] half contiguous -> [H, T, d] half: quantize, SDDMM,
     quantized softmax, SpMM on the current stream."""
     _, H, T, d = qkv.shape
@@ -33,24 +34,35 @@ def attention_core(qkv: torch.Tensor, mask: AttentionMaskDev, head_dim: int, lhs
     _lib.check(_lib.lib().mcQuantize(qkv.data_ptr(), qkv_q.data_ptr(), qkv.numel(), rhs_bits, float(scale_qkv),
                                      stream), "mcQuantize")
     return attention_core_quantized(qkv_q, T, mask, head_dim, lhs_bits, rhs_bits, scale_qkv, scale_sfmx,
-                                    sddmm_cfg, spmm_cfg)
+                                    sddmm_cfg, spmm_cfg, requant)
+
+
+def _score_div(scale_qkv: float, scaling: float) -> float:
+    """The float quotient score_scale / scaling that the fused kernel's
+    row-max mode divides the score accumulators by."""
+    return float(np.float32(np.float32(scale_qkv ** 2) / np.float32(scaling)))
 
 
 def attention_core_quantized(qkv_q: torch.Tensor, T: int, mask: AttentionMaskDev, head_dim: int, lhs_bits: int,
                              rhs_bits: int, scale_qkv: float, scale_sfmx: float, sddmm_cfg: dict | None = None,
-                             spmm_cfg: dict | None = None) -> torch.Tensor:
+                             spmm_cfg: dict | None = None, requant: str = "fixed") -> torch.Tensor:
     """qkv_q: [3, H, T*d*rhs_bits/32] int32 (quantized Q, K, V) -> [H, T, d]
-    half: SDDMM, quantized softmax, SpMM on the current stream."""
+    half: SDDMM, quantized softmax, SpMM on the current stream.  requant
+    "rowmax" (8-bit probabilities) requantizes relative to each row's maximum
+    and divides each output row by its own divisor."""
     H, d = qkv_q.shape[1], head_dim
     dev = qkv_q.device
     V = mask.vec_length
+    rowmax = requant == "rowmax"
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     q_words = T * d * rhs_bits // 32
     scores = torch.empty((H, mask.aligned_nnz * V), dtype=torch.float16, device=dev)
+    row_div = torch.empty((H, T), dtype=torch.float32, device=dev) if rowmax else None
     sc = sddmm_cfg or {}
     sd = _lib.McSddmmDesc(
         m_vec=mask.m_vec, vec_length=V, n=T, k=d, lhs_bits=rhs_bits, rhs_bits=rhs_bits, is_signed=1, out_half=1,
-        out_vecmajor=1, scale=float(scale_qkv ** 2), batch=H, row_split=sc.get("row_split", 0),
+        out_vecmajor=1, scale=_score_div(scale_qkv, d ** -0.5) if rowmax else float(scale_qkv ** 2), batch=H,
+        row_split=sc.get("row_split", 0),
         row_indices=mask.row_indices.data_ptr(), row_offsets=mask.row_offsets.data_ptr(),
         column_indices=mask.col_indices.data_ptr(), lhs=qkv_q[0].data_ptr(), lhs_stride=q_words * 4,
         rhs=qkv_q[1].data_ptr(), rhs_stride=q_words * 4, out=scores.data_ptr(), out_stride=scores.shape[1],
@@ -58,9 +70,11 @@ def attention_core_quantized(qkv_q: torch.Tensor, T: int, mask: AttentionMaskDev
     _lib.check(_lib.lib().mcSddmm(ctypes.byref(sd), stream), "mcSddmm")
     probs = torch.zeros((H, mask.aligned_nnz * V * lhs_bits // 32), dtype=torch.int32, device=dev)
     sm = _lib.McSoftmaxDesc(
-        m_vec=mask.m_vec, vec_length=V, batch=H, bits=lhs_bits, scaling=float(d ** -0.5), scale=float(scale_sfmx),
-        row_indices=mask.row_indices.data_ptr(), row_offsets=mask.row_offsets.data_ptr(), scores=scores.data_ptr(),
-        scores_stride=scores.shape[1], out=probs.data_ptr(), out_stride=probs.shape[1] * 4)
+        m_vec=mask.m_vec, vec_length=V, batch=H, bits=lhs_bits, scaling=1.0 if rowmax else float(d ** -0.5),
+        scale=float(scale_qkv) if rowmax else float(scale_sfmx), row_indices=mask.row_indices.data_ptr(),
+        row_offsets=mask.row_offsets.data_ptr(), scores=scores.data_ptr(), scores_stride=scores.shape[1],
+        out=probs.data_ptr(), out_stride=probs.shape[1] * 4, requant=_lib.REQUANT_ROWMAX if rowmax else 0,
+        row_div=row_div.data_ptr() if rowmax else None, row_div_stride=T if rowmax else 0)
     _lib.check(_lib.lib().mcQuantSoftmax(ctypes.byref(sm), stream), "mcQuantSoftmax")
     out = torch.empty((H, T, d), dtype=torch.float16, device=dev)
     pc = spmm_cfg or {}
@@ -70,8 +84,31 @@ def attention_core_quantized(qkv_q: torch.Tensor, T: int, mask: AttentionMaskDev
         row_offsets=mask.row_offsets.data_ptr(), column_indices=mask.col_indices.data_ptr(),
         values=probs.data_ptr(), values_stride=probs.shape[1] * 4, rhs=qkv_q[2].data_ptr(), rhs_stride=q_words * 4,
         out=out.data_ptr(), out_stride=T * d, mma_kind=pc.get("mma_kind", 0), kernel_variant=pc.get("variant", 0),
-        value_layout=_lib.VALUES_SOFTMAX)
+        value_layout=_lib.VALUES_SOFTMAX, row_div=row_div.data_ptr() if rowmax else None,
+        row_div_stride=T if rowmax else 0)
     _lib.check(_lib.lib().mcSpmm(ctypes.byref(sp), stream), "mcSpmm")
+    return out
+
+
+def attention_fused_quantized(qkv_q: torch.Tensor, T: int, mask: AttentionMaskDev, scale_qkv: float,
+                              scale_sfmx: float, requant: str = "fixed") -> torch.Tensor:
+    """qkv_q: [3, H, T*64/4] int32 (int8 Q, K, V, head_dim 64) -> [H, T, 64]
+    half through the fused attention kernel (mcSparseAttention): the same
+    bits as attention_core_quantized with the same requant mode."""
+    H, d = qkv_q.shape[1], 64
+    q_words = T * d // 4
+    out = torch.empty((H, T, d), dtype=torch.float16, device=qkv_q.device)
+    rowmax = requant == "rowmax"
+    desc = _lib.McAttnDesc(
+        m_vec=mask.m_vec, vec_length=mask.vec_length, heads=H, head_dim=d, max_row_nnz=mask.max_row_nnz, lhs_bits=8,
+        rhs_bits=8, requant=_lib.REQUANT_ROWMAX if rowmax else _lib.REQUANT_FIXED, score_scale=float(scale_qkv ** 2),
+        scaling=float(d ** -0.5), prob_scale=float(scale_sfmx),
+        out_scale=float(scale_qkv) if rowmax else float(scale_qkv * scale_sfmx),
+        row_indices=mask.row_indices.data_ptr(), row_offsets=mask.row_offsets.data_ptr(),
+        column_indices=mask.col_indices.data_ptr(), q=qkv_q[0].data_ptr(), k=qkv_q[1].data_ptr(),
+        v=qkv_q[2].data_ptr(), head_stride=q_words * 4, out=out.data_ptr(), out_head_stride=T * d, status=None)
+    _lib.check(_lib.lib().mcSparseAttention(ctypes.byref(desc), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               "mcSparseAttention")
     return out
 
 
@@ -94,9 +131,19 @@ class SparseEncoderLayer(nn.Module):
         self.linear2 = nn.Linear(ffn, hidden)
         self.sddmm_cfg: dict | None = None
         self.spmm_cfg: dict | None = None
+        # attention kernels: "separate" (SDDMM, softmax, SpMM launches) or
+        # "fused" (mcSparseAttention, int8 with head_dim 64 and rows of at
+        # most 4096 nonzero vectors; otherwise the separate launches run);
+        # requant "fixed" (the reference's scales) or "rowmax"
+        self.attention = "separate"
+        self.requant = "fixed"
         # The fused projection + quantization kernel (tcgen05) where its shape
         # constraints hold; otherwise F.linear, permute and mcQuantize.
         self.fused_projection = hidden % 64 == 0 and 64 <= hidden <= 256 and self.head_dim % 64 == 0
+
+    def _fused_ok(self, mask: AttentionMaskDev) -> bool:
+        return (self.attention == "fused" and self.lhs_bits == 8 and self.rhs_bits == 8 and self.head_dim == 64
+                and 0 < mask.max_row_nnz <= 4096)
 
     def forward(self, x: torch.Tensor, mask: AttentionMaskDev) -> torch.Tensor:
         """x: [T, hidden] half (sequences back to back) -> [T, hidden]."""
@@ -105,13 +152,17 @@ class SparseEncoderLayer(nn.Module):
         if self.fused_projection and h.dtype == torch.float16:
             qkv_q = qkv_project_quantize(h, self.in_proj.weight, self.in_proj.bias, self.heads, self.rhs_bits,
                                          self.scale_qkv)
-            att = attention_core_quantized(qkv_q, T, mask, self.head_dim, self.lhs_bits, self.rhs_bits,
-                                           self.scale_qkv, self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg)
+            if self._fused_ok(mask):
+                att = attention_fused_quantized(qkv_q, T, mask, self.scale_qkv, self.scale_sfmx, self.requant)
+            else:
+                att = attention_core_quantized(qkv_q, T, mask, self.head_dim, self.lhs_bits, self.rhs_bits,
+                                               self.scale_qkv, self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg,
+                                               self.requant)
         else:
             qkv = F.linear(h, self.in_proj.weight, self.in_proj.bias)              # [T, 3E]
             qkv = qkv.view(T, 3, self.heads, self.head_dim).permute(1, 2, 0, 3).contiguous()  # [3, H, T, d]
             att = attention_core(qkv, mask, self.head_dim, self.lhs_bits, self.rhs_bits, self.scale_qkv,
-                                 self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg)  # [H, T, d]
+                                 self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg, self.requant)  # [H, T, d]
         att = att.permute(1, 0, 2).reshape(T, self.hidden)
         out = F.linear(att, self.out_proj.weight, self.out_proj.bias) + x
         out = self.ln2(out)
@@ -127,6 +178,15 @@ class SparseEncoder(nn.Module):
         super().__init__()
         self.layers = nn.ModuleList(SparseEncoderLayer(hidden, heads, ffn, lhs_bits, rhs_bits, **scales)
                                     for _ in range(layers))
+
+    def set_attention(self, kind: str = "separate", requant: str = "fixed") -> "SparseEncoder":
+        """Attention kernels of every layer: "separate" or "fused"; requant
+        "fixed" or "rowmax" (both kinds give the same bits per mode)."""
+        if kind not in ("separate", "fused") or requant not in ("fixed", "rowmax"):
+            raise ValueError("kind must be 'separate' or 'fused', requant 'fixed' or 'rowmax'")
+        for layer in self.layers:
+            layer.attention, layer.requant = kind, requant
+        return self
 
     def forward(self, x: torch.Tensor, masks: list[AttentionMaskDev]) -> torch.Tensor:
         for layer, m in zip(self.layers, masks):

@@ -79,13 +79,19 @@ def _upload(req: Request, alignment: int, device) -> None:
             ro = torch.from_numpy(m.row_offsets).to(dev, non_blocking=True)
             ci = torch.from_numpy(m.col_indices).to(dev, non_blocking=True)
             dm = device_format.prepare_sddmm(ro, ci, m.vec_length, m.ncols, alignment=alignment, sync=False)
-            per_layer.append((dm.row_offsets, dm.col_indices, dm.row_indices, m.m_vec, dm.aligned_nnz))
+            per_layer.append((dm.row_offsets, dm.col_indices, dm.row_indices, m.m_vec, dm.aligned_nnz,
+                              _max_row(m)))
         else:  # host tensors: the library's host packer (exact slot counts)
             pairs, n = formats.align_row_offsets(m, alignment)
             cols = formats.pad_column_indices(m, pairs, n, shuffle8=False)
             per_layer.append((torch.from_numpy(pairs), torch.from_numpy(cols),
-                              torch.from_numpy(formats.sorted_row_swizzle(m)), m.m_vec, n))
+                              torch.from_numpy(formats.sorted_row_swizzle(m)), m.m_vec, n, _max_row(m)))
     req.dev["masks"] = per_layer
+
+
+def _max_row(m) -> int:
+    """Longest vector-row (nonzero vectors) of a host mask."""
+    return int(np.diff(m.row_offsets).max()) if m.m_vec else 0
 
 
 def batch_masks(reqs: list[Request], layers: int, V: int) -> list[AttentionMaskDev]:
@@ -93,9 +99,10 @@ def batch_masks(reqs: list[Request], layers: int, V: int) -> list[AttentionMaskD
     out = []
     for l in range(layers):
         pairs, cols, ri = [], [], []
-        abase = tbase = mbase = 0
+        abase = tbase = mbase = longest = 0
         for r in reqs:
-            p, c, i, m_vec, n = r.dev["masks"][l]
+            p, c, i, m_vec, n, mx = r.dev["masks"][l]
+            longest = max(longest, mx)
             pairs.append(p + abase)
             cols.append(torch.where(c >= 0, c + tbase, c))
             ri.append(i + mbase)
@@ -104,7 +111,8 @@ def batch_masks(reqs: list[Request], layers: int, V: int) -> list[AttentionMaskD
             mbase += m_vec
         if abase == 0:
             cols = [torch.full((1,), -1, dtype=torch.int32, device=pairs[0].device)]
-        out.append(AttentionMaskDev(mbase, V, tbase, abase, torch.cat(ri), torch.cat(pairs), torch.cat(cols)))
+        out.append(AttentionMaskDev(mbase, V, tbase, abase, torch.cat(ri), torch.cat(pairs), torch.cat(cols),
+                                    longest))
     return out
 
 

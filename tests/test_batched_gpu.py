@@ -71,6 +71,48 @@ def test_server_results_same_alone_and_mixed(cuda):
         assert (m - ref).abs().max() <= 2e-2 * ref.abs().max()
 
 
+@pytest.mark.parametrize("requant", ["fixed", "rowmax"])
+def test_encoder_fused_attention_equals_separate(cuda, requant):
+    """The encoder with the fused attention kernel gives the same bits as with
+    the separate SDDMM / softmax / SpMM launches, in either requant mode."""
+    torch.manual_seed(0)
+    enc = model.SparseEncoder(layers=2, hidden=256, heads=4, ffn=512).to(cuda).half().eval()
+    reqs = serving.make_requests(3, rate=0.0, hidden=256, layers=2, sparsity=0.9, median=256, clip=(128, 512),
+                                 seed=8)
+    for r in reqs:
+        serving._upload(r, 16, cuda)
+    masks = serving.batch_masks(reqs, 2, 8)
+    assert all(m.max_row_nnz > 0 for m in masks)
+    x = torch.cat([r.dev["x"] for r in reqs], dim=0)
+    with torch.no_grad():
+        a = enc.set_attention("separate", requant)(x, masks).clone()
+        b = enc.set_attention("fused", requant)(x, masks).clone()
+    torch.cuda.synchronize()
+    assert torch.isfinite(a).all()
+    assert torch.equal(a, b)
+
+
+def test_server_fused_mixed_same_as_sequential_separate(cuda):
+    """Continuous batching on the fused attention kernel against one request
+    at a time on the separate launches: the same results within the fp16
+    tolerance of the dense layers."""
+    torch.manual_seed(0)
+    enc = model.SparseEncoder(layers=2, hidden=256, heads=4, ffn=512).to(cuda).half().eval()
+    kw = dict(rate=0.0, hidden=256, layers=2, sparsity=0.9, median=256, clip=(128, 640), seed=4)
+    reqs = serving.make_requests(8, **kw)
+    srv = serving.ContinuousBatchingServer(enc.set_attention("fused"), hidden=256, heads=4, max_inflight=2,
+                                           max_batch_tokens=1024, device=cuda)
+    srv.serve(reqs)
+    assert any(len(b) > 1 for b in srv.batches)
+    mixed = [r.out.float().cpu() for r in reqs]
+    alone = serving.make_requests(8, **kw)
+    serving.serve_sequential(enc.set_attention("separate"), alone, device=cuda)
+    for a, m in zip(alone, mixed):
+        ref = a.out.float().cpu()
+        assert torch.isfinite(ref).all()
+        assert (m - ref).abs().max() <= 2e-2 * ref.abs().max()
+
+
 @pytest.mark.parametrize("V", [2, 4, 8])
 def test_fused_fixed_equals_separate_steps(cuda, V):
     """The fused kernel with fixed requantization reproduces the separate

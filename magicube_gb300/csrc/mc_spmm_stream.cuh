@@ -12,10 +12,12 @@
 //    B (column slice), the step's value chunk(s) and a 16-byte header
 //    (row, batch entry, nonzero count, step, last/empty flags) written by the
 //    producer, so the consumer reads no global metadata.
-//  * 8-bit B: ldmatrix.m16n16.x2.trans.b8 turns the staged [slot][column]
-//    bytes into the k-contiguous A fragment of mma.m16n8k32 directly (rows
-//    128-byte XOR-swizzled so the eight 16-byte row segments of each phase hit
-//    distinct banks).  4-bit B: 16-bit loads, nibble unpack, prmt transpose.
+//  * ldmatrix.m16n16.x2.trans.b8 turns the staged [slot][byte] rows into the
+//    k-contiguous A fragment of mma.m16n8k32 directly (rows XOR-swizzled so
+//    the 16-byte row segments of each phase hit distinct banks).  8-bit B:
+//    byte c is column c.  4-bit B: byte c holds columns 2c (low nibble) and
+//    2c+1 (high nibble), so masking (and sign-extending) the nibbles of one
+//    fragment gives the A fragments of two MMA tiles: columns 2c and 2c+1.
 //  * Column indices of the next step are fetched one step ahead into
 //    registers; the producer cursor runs STAGES-1 steps ahead of the consumer.
 #pragma once
@@ -37,19 +39,17 @@ struct StreamRhs {
     static constexpr int NT = WARPS * 16 * MT;
     static constexpr int RB = NT * PREB / 8;  // packed bytes per row slice
     static constexpr int CH = RB / 16;        // 16-byte chunks per row slice
-    // 8-bit: rows of NT bytes, 16-byte chunks XOR-swizzled over 8 (NT >= 128)
-    // or 4 (NT = 64, two rows per 128-byte line) rows for ldmatrix.
-    // 4-bit: the layout of mc_spmm.cuh's RhsSmem (16-bit loads).
-    static constexpr int STRIDE = PREB == 8 ? RB : (CH == 4 ? 64 : 48);
+    // Rows of RB packed bytes (8-bit or 4-bit B), 16-byte chunks
+    // XOR-swizzled so that the eight row segments of each ldmatrix phase hit
+    // distinct 16-byte bank groups: over 8 rows (RB >= 128), over 4 pairs of
+    // rows (RB = 64: two rows per 128-byte line) or over 2 groups of 4 rows
+    // (RB = 32: four rows per line).
+    static constexpr int STRIDE = RB;
     __device__ __forceinline__ static int swz(int r, int c)
     {
-        if constexpr (PREB == 8) {
-            if constexpr (CH >= 8) return c ^ (r & 7);
-            else return c ^ ((r >> 1) & 3);
-        } else {
-            if constexpr (CH == 4) return c ^ ((r >> 2) & 3);
-            else return c ^ ((r >> 3) & 1);
-        }
+        if constexpr (CH >= 8) return c ^ (r & 7);
+        else if constexpr (CH == 4) return c ^ ((r >> 1) & 3);
+        else return c ^ ((r >> 2) & 1);
     }
 };
 
@@ -231,22 +231,17 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
                 for (int m = 0; m < MT; ++m)
                     ldsm_x2_trans_b8(af[m], st + r * S::STRIDE + S::swz(r, MT * warp + m) * 16);
             } else {
-                const int ncol = warp * 32 + 4 * g;
-                uint32_t tr[2][4];
+                // this warp's 32 columns are one 16-byte chunk: one ldmatrix,
+                // then MMA 0 takes the low nibbles (column 2c of byte c),
+                // MMA 1 the high nibbles (column 2c + 1)
+                uint32_t nb[4];
+                ldsm_x2_trans_b8(nb, st + lane * S::STRIDE + S::swz(lane, warp) * 16);
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const int r = 16 * h + 4 * t + i;
-                        const int byte = ncol >> 1;
-                        tr[h][i] = unpack4_u16<SIGNED>(
-                            lds16(st + r * S::STRIDE + S::swz(r, byte >> 4) * 16 + (byte & 15)));
-                    }
-                    transpose4x4(tr[h]);
+                for (int q = 0; q < 4; ++q) {
+                    const uint32_t lo = nb[q] & 0x0F0F0F0Fu, hi = (nb[q] >> 4) & 0x0F0F0F0Fu;
+                    af[0][q] = SIGNED ? sext_nibble_bytes(lo) : lo;
+                    af[1][q] = SIGNED ? sext_nibble_bytes(hi) : hi;
                 }
-                // MMA 0: columns ncol, ncol+1; MMA 1: ncol+2, ncol+3
-                af[0][0] = tr[0][0]; af[0][1] = tr[0][1]; af[0][2] = tr[1][0]; af[0][3] = tr[1][1];
-                af[1][0] = tr[0][2]; af[1][1] = tr[0][3]; af[1][2] = tr[1][2]; af[1][3] = tr[1][3];
             }
 #pragma unroll
             for (int bp = 0; bp < BP; ++bp) {
@@ -289,7 +284,7 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
         }
         if (last) {
             // acc[.][m][e]: column c(m, e>>1), vector lane 2t + (e & 1), where
-            // 8-bit B: c = 16m + 8(e>>1) + g;  4-bit B: c = 4g + 2m + (e>>1).
+            // 8-bit B: c = 16m + 8(e>>1) + g;  4-bit B: c = 2g + m + 16(e>>1).
             const int row = hdr.x, b = hdr.y;
 #pragma unroll
             for (int e2 = 0; e2 < 2; ++e2) {
@@ -318,13 +313,16 @@ spmm_stream_kernel(const SpmmParams p, const int ntasks)
                         for (int q = 0; q < 2 * MT; ++q) stg_cs_s32(o + 8 * q, r4[q]);
                     }
                 } else {
-                    // columns 4g .. 4g+3
+                    // r4[0], r4[2]: columns 2g, 2g+1; r4[1], r4[3]: columns 2g+16, 2g+17
                     if constexpr (HALF_OUT) {
-                        __half* o = reinterpret_cast<__half*>(p.out) + obase + 4 * g;
+                        __half* o = reinterpret_cast<__half*>(p.out) + obase + 2 * g;
                         const Divisor dv = out_divisor(p, b, row * V + v);
-                        stg_cs_v2(o, (int)pack_half2(r4[0], r4[1], dv), (int)pack_half2(r4[2], r4[3], dv));
+                        stg_cs_s32(o, (int)pack_half2(r4[0], r4[2], dv));
+                        stg_cs_s32(o + 16, (int)pack_half2(r4[1], r4[3], dv));
                     } else {
-                        stg_cs_v4(reinterpret_cast<int*>(p.out) + obase + 4 * g, r4[0], r4[1], r4[2], r4[3]);
+                        int* o = reinterpret_cast<int*>(p.out) + obase + 2 * g;
+                        stg_cs_v2(o, r4[0], r4[2]);
+                        stg_cs_v2(o + 16, r4[1], r4[3]);
                     }
                 }
             }

@@ -934,9 +934,10 @@ def main() -> None:
     ap.add_argument("--profile", choices=["sddmm", "spmm", "attention", "packer", "projection"], default=None,
                     help="run only a small case of one kernel (for ncu captures)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")
-    ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")], default=[200.0, 2000.0],
+    ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")],
+                    default=[200.0, 2000.0, 20000.0],
                     help="Poisson arrival rates (requests/s) of the serving runs")
-    ap.add_argument("--serving-requests", type=int, default=48, help="requests per serving run (0 skips it)")
+    ap.add_argument("--serving-requests", type=int, default=96, help="requests per serving run (0 skips it)")
     ap.add_argument("--serving-overlap-tokens", type=int, default=8192,
                     help="queued tokens at which the server overlaps a new batch with running ones")
     ap.add_argument("--mma", choices=["int8", "f16", "tc"], default="int8",

@@ -107,12 +107,13 @@ int mcSetDefaultMmaKind(int kind);
  *                    stream many vector-rows through one cp.async ring (needs
  *                    16-byte aligned values); SDDMM -- the k == 64 kernel with
  *                    a warp per 16-nonzero tile at full occupancy (needs k == 64).
- * MC_KERNEL_TMA:     SpMM only, 8-bit B on the int8 path: persistent
- *                    warp-specialised CTAs -- one producer warp gathers B rows
- *                    with TMA (tile::gather4) into an mbarrier ring, four
- *                    consumer warps multiply (needs n % 128 == 0, 16-byte
- *                    aligned values, values_stride and rhs, rhs_stride a
- *                    multiple of n).
+ * MC_KERNEL_TMA:     SpMM only, on the int8 path: persistent warp-specialised
+ *                    CTAs -- one producer warp gathers B rows with TMA
+ *                    (tile::gather4) into an mbarrier ring, consumer warps
+ *                    multiply (needs 8-bit B with n % 128 == 0 or 4-bit B
+ *                    with n % 256 == 0, 16-byte aligned values,
+ *                    values_stride and rhs, rhs_stride a multiple of the B
+ *                    row bytes).
  * MC_KERNEL_AUTO:    SpMM: the TMA kernel where it applies, else the
  *                    streaming kernel, else per-row; SDDMM: the pipelined
  *                    kernel where it applies, else per-row. */

@@ -42,32 +42,36 @@ int spmm_launch_stream(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     return (int)cudaGetLastError();
 }
 
-// The TMA SpMM (mc_spmm_tma.cuh) applies to 8-bit B on the int8 path with
-// n % 128 == 0, 16-byte aligned values (and values_stride), and batch
-// entries of B a whole number of rows apart.
+// The TMA SpMM (mc_spmm_tma.cuh) applies on the int8 path to 8-bit B with
+// n % 128 == 0 and 4-bit B with n % 256 == 0 (rows of whole 128-byte
+// boxes), with 16-byte aligned values (and values_stride) and batch entries
+// of B a whole number of rows apart.
 inline bool spmm_tma_eligible(const mcSpmmDesc& d)
 {
-    if (d.rhs_bits != 8 || d.n % 128 || resolve_mma_kind(d.mma_kind) != MC_MMA_INT8) return false;
+    if (resolve_mma_kind(d.mma_kind) != MC_MMA_INT8) return false;
+    if (!((d.rhs_bits == 8 && d.n % 128 == 0) || (d.rhs_bits == 4 && d.n % 256 == 0))) return false;
     if (reinterpret_cast<uintptr_t>(d.values) % 16 || d.values_stride % 16) return false;
     if (reinterpret_cast<uintptr_t>(d.rhs) % 16) return false;
-    if (d.batch > 1 && d.rhs_stride % d.n) return false;
-    const long long per_entry = d.batch > 1 ? d.rhs_stride / d.n : 0;
+    const long long row_bytes = (long long)d.n * d.rhs_bits / 8;
+    if (d.batch > 1 && d.rhs_stride % row_bytes) return false;
+    const long long per_entry = d.batch > 1 ? d.rhs_stride / row_bytes : 0;
     return per_entry * (d.batch - 1) + d.k <= 0x7fffffffLL;
 }
 
-template <int V, int PA, bool S, bool H, int NT, int STAGES = 4, int CW = 4>
+template <int V, int PA, int PB, bool S, bool H, int NT, int STAGES = 4, int CW = 4>
 int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
-    using G = SpmmTmaGeom<V, PA, NT, STAGES, CW>;
+    using G = SpmmTmaGeom<V, PA, PB, NT, STAGES, CW>;
     const long long ntasks = (long long)d.m_vec * d.batch;
     if (ntasks > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
-    const long long per_entry = d.batch > 1 ? d.rhs_stride / d.n : 0;
+    const long long row_bytes = (long long)d.n * PB / 8;
+    const long long per_entry = d.batch > 1 ? d.rhs_stride / row_bytes : 0;
     CUtensorMap map;
-    if (!encode_row_gather_u8(&map, d.rhs, per_entry * (d.batch - 1) + d.k, d.n, 128))
+    if (!encode_row_gather_u8(&map, d.rhs, per_entry * (d.batch - 1) + d.k, row_bytes, 128))
         return fail(1, "mcSpmm: TMA tensor map encoding failed");
     unsigned int* timeouts = async_timeout_counter();
     if (!timeouts) return fail(1, "mcSpmm: timeout counter unavailable");
-    auto kern = spmm_tma_kernel<V, PA, S, H, H, NT, STAGES, CW>;
+    auto kern = spmm_tma_kernel<V, PA, PB, S, H, H, NT, STAGES, CW>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
         return (int)cudaGetLastError();
     // resident CTAs per SM from registers, shared memory and warps
@@ -90,15 +94,18 @@ int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s
     return (int)cudaGetLastError();
 }
 
-// Ring depth and consumer warps per column tile, measured on GB300: a
-// 256-column tile runs 4 consumer warps (four 16-column MMA tiles each)
-// over 4 stages; a 128-column tile 2 consumer warps (four tiles each) over
-// 6 stages.  Deeper rings cost resident CTAs, which matter more.
-template <int V, int PA, bool S, bool H, int NT>
+// Ring depth and consumer warps per column tile, measured on GB300 (8-bit
+// B): a 256-column tile runs 4 consumer warps (four 16-column MMA tiles
+// each) over 4 stages; a 128-column tile 2 consumer warps (four tiles each)
+// over 6 stages.  Deeper rings cost resident CTAs, which matter more.  4-bit
+// B: 256-column tiles (128-byte rows, half the stage of 8-bit B) over 6
+// stages.
+template <int V, int PA, int PB, bool S, bool H, int NT>
 int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
-    if constexpr (NT == 256) return spmm_launch_tma_cfg<V, PA, S, H, 256, 4, 4>(d, p, s);
-    else return spmm_launch_tma_cfg<V, PA, S, H, 128, 6, 2>(d, p, s);
+    if constexpr (PB == 4) return spmm_launch_tma_cfg<V, PA, 4, S, H, 256, 6, 4>(d, p, s);
+    else if constexpr (NT == 256) return spmm_launch_tma_cfg<V, PA, 8, S, H, 256, 4, 4>(d, p, s);
+    else return spmm_launch_tma_cfg<V, PA, 8, S, H, 128, 6, 2>(d, p, s);
 }
 
 // H (half output) is compiled only with the softmax value layout (E), the
@@ -126,16 +133,13 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
         const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
         if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
             return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");
-        if constexpr (PB == 8) {
-            if (d.kernel_variant == MC_KERNEL_TMA && !spmm_tma_eligible(d))
-                return fail(1, "mcSpmm: the TMA kernel needs the int8 path, n % 128 == 0, 16-byte aligned values, "
-                               "values_stride and rhs, and rhs_stride a multiple of n");
-            if ((d.kernel_variant == MC_KERNEL_TMA || d.kernel_variant == MC_KERNEL_AUTO) && spmm_tma_eligible(d))
-                return d.n % 256 == 0 ? spmm_launch_tma<V, PA, S, H, 256>(d, p, s)
-                                      : spmm_launch_tma<V, PA, S, H, 128>(d, p, s);
-        } else {
-            if (d.kernel_variant == MC_KERNEL_TMA) return fail(1, "mcSpmm: the TMA kernel needs 8-bit B");
-        }
+        if (d.kernel_variant == MC_KERNEL_TMA && !spmm_tma_eligible(d))
+            return fail(1, "mcSpmm: the TMA kernel needs the int8 path, n % 128 == 0 (8-bit B) or n % 256 == 0 "
+                           "(4-bit B), 16-byte aligned values, values_stride and rhs, and rhs_stride a multiple of "
+                           "the B row bytes");
+        if ((d.kernel_variant == MC_KERNEL_TMA || d.kernel_variant == MC_KERNEL_AUTO) && spmm_tma_eligible(d))
+            return d.n % 256 == 0 ? spmm_launch_tma<V, PA, PB, S, H, 256>(d, p, s)
+                                  : spmm_launch_tma<V, PA, PB, S, H, 128>(d, p, s);
         if (d.kernel_variant != MC_KERNEL_PER_ROW && stream_ok) {
             if constexpr (PB == 8) {
                 // 8-bit B, n % 256 == 0: four 16-column MMA tiles per warp

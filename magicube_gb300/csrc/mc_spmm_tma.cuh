@@ -1,20 +1,23 @@
-// mc_spmm_tma.cuh -- warp-specialised SpMM for 8-bit B on sm_103a: B rows are
-// gathered by the tensor memory accelerator.
+// mc_spmm_tma.cuh -- warp-specialised SpMM for 8-bit and 4-bit B on sm_103a:
+// B rows are gathered by the tensor memory accelerator.
 //
-// Same operands and results as spmm_stream_kernel (mc_spmm_stream.cuh) for
-// 8-bit B and the int8 tensor path.  A task is one (batch entry, vector-row);
+// Same operands and results as spmm_stream_kernel (mc_spmm_stream.cuh) on the
+// int8 tensor path.  A task is one (batch entry, vector-row);
 // CTA x of the grid owns tasks x, x + gridDim.x, ... for one NT-column tile
 // of C, and their 32-slot steps flow through a STAGES-deep ring:
 //  * warp CWARPS, the producer, loads a step's column indices (one per lane) and
-//    issues TMA tile::gather4 copies -- four B rows x 128 columns per copy,
-//    straight from the row coordinates -- plus one bulk copy of the step's
+//    issues TMA tile::gather4 copies -- four B rows x 128 bytes per copy
+//    (128 columns of 8-bit B, 256 of 4-bit B), straight from the row
+//    coordinates -- plus one bulk copy of the step's
 //    value chunk, all completing the stage's "full" mbarrier; lane 0 writes a
 //    16-byte step header (row, batch entry, nonzero count, step, last/empty
 //    flags) beside them before arriving with the expected byte count;
 //  * warps 0 .. CWARPS-1, the consumers (NT / (16 CWARPS) 16-column MMA
 //    tiles each), wait for the stage, read the header, turn the
-//    128-byte-swizzled [slot][column] bytes into mma.m16n8k32 A fragments with
-//    ldmatrix.m16n16.x2.trans.b8 (the value chunk is the B fragment), release
+//    128-byte-swizzled [slot][byte] rows into mma.m16n8k32 A fragments with
+//    ldmatrix.m16n16.x2.trans.b8 (4-bit B: the masked low and high nibbles of
+//    one fragment are the A fragments of two MMA tiles, columns 2c and 2c+1;
+//    the value chunk is the B fragment), release
 //    the stage through its "empty" mbarrier and write finished rows of C from
 //    registers.  No CTA barrier inside the loop.
 // Slots past a row's nonzero count gather row 0 of the batch entry's B, so
@@ -30,31 +33,34 @@
 
 namespace mc {
 
-template <int V, int PREA, int NT, int STAGES, int CWARPS = 4>
+template <int V, int PREA, int PREB, int NT, int STAGES, int CWARPS = 4>
 struct SpmmTmaGeom {
     static constexpr int CW = CWARPS;                 // consumer warps
     static constexpr int THREADS = (CW + 1) * 32;
     static constexpr int MT = NT / (16 * CW);         // 16-column MMA tiles per consumer warp
     static constexpr int SLOT_BYTES = V * PREA / 8;   // value bytes per vector slot
-    static constexpr int RHS_BYTES = 32 * NT;         // one stage of gathered rows (1024-byte multiple)
+    static constexpr int RB = NT * PREB / 8;          // bytes of one gathered row slice
+    static constexpr int BOXES = RB / 128;            // 128-byte TMA boxes per row slice
+    static constexpr int RHS_BYTES = 32 * RB;         // one stage of gathered rows (1024-byte multiple)
     static constexpr int AUX_BYTES = (32 * SLOT_BYTES + 16 + 127) / 128 * 128;  // values + header
     static constexpr size_t SMEM = 1024 + (size_t)STAGES * (RHS_BYTES + AUX_BYTES) + 2 * STAGES * 8;
 };
 
-template <int V, int PREA, bool SIGNED, bool HALF_OUT, bool EXT, int NT, int STAGES, int CWARPS = 4>
+template <int V, int PREA, int PREB, bool SIGNED, bool HALF_OUT, bool EXT, int NT, int STAGES, int CWARPS = 4>
 __global__ void __launch_bounds__((CWARPS + 1) * 32)
 spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, const int ntasks,
                 const int rows_per_entry, unsigned int* timeouts)
 {
     using namespace sm100;
-    using L = SpmmLayout<PREA, 8, EXT>;
-    using G = SpmmTmaGeom<V, PREA, NT, STAGES, CWARPS>;
+    using L = SpmmLayout<PREA, PREB, EXT>;
+    using G = SpmmTmaGeom<V, PREA, PREB, NT, STAGES, CWARPS>;
     constexpr int CW = G::CW, MT = G::MT, BP = L::BYTE_PLANES;
-    constexpr int SLOT_BYTES = G::SLOT_BYTES, RHS_BYTES = G::RHS_BYTES, AUX_BYTES = G::AUX_BYTES;
+    constexpr int SLOT_BYTES = G::SLOT_BYTES, RB = G::RB, RHS_BYTES = G::RHS_BYTES, AUX_BYTES = G::AUX_BYTES;
     constexpr int HDR = 32 * SLOT_BYTES;              // header offset inside a stage's aux block
     constexpr long long WAIT = 4000000000LL;          // about 2 s at 2 GHz
-    static_assert(L::VCHUNK == 16, "8-bit B: 16-slot value chunks");
-    static_assert(NT == 128 || NT == 256, "one or two 128-byte TMA boxes per gathered row");
+    static_assert(PREB == 8 || PREB == 4, "8-bit or 4-bit B");
+    static_assert(RB == 128 || RB == 256, "one or two 128-byte TMA boxes per gathered row");
+    static_assert(PREB == 8 || MT % 2 == 0, "4-bit B: two MMA tiles per 16-byte chunk");
     static_assert(HDR % 16 == 0, "header alignment");
 
     extern __shared__ uint8_t smem_raw[];
@@ -95,7 +101,8 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
         };
         auto fetch_col = [&](const StreamTask& x) {
             const int j = 32 * x.step + lane;
-            return (x.task < ntasks && j < x.nnz) ? __ldg(p.col_indices + x.start + j) : -1;
+            return (x.task < ntasks && j < x.nnz) ? __ldg(p.col_indices + x.start + col_slot<L::SHUFFLED_COLS>(j))
+                                                  : -1;
         };
         auto next_of = [&](int task) {  // task + gridDim.x without int overflow
             const long long n = (long long)task + gridDim.x;
@@ -124,7 +131,7 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
             const int rem = c.nnz - 32 * c.step;
             const int nvalid = rem < 0 ? 0 : (rem > 32 ? 32 : rem);
             const int ngroups = (nvalid + 3) >> 2;
-            const int alen = (c.nnz + 15) & ~15;
+            const int alen = (c.nnz + L::MMA_K - 1) / L::MMA_K * L::MMA_K;
             const int vbytes = nvalid > 0 ? min(32, alen - 32 * c.step) * SLOT_BYTES : 0;
             const int ybase = c.b * rows_per_entry;
             const int y = col >= 0 ? ybase + col : ybase;
@@ -139,14 +146,15 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
                 const int last = (c.steps == 0) || (c.step == c.steps - 1);
                 h.w = c.step | (last << 30) | ((c.steps == 0) << 29);
                 *reinterpret_cast<int4*>(aux + HDR) = h;
-                mbar_arrive_expect_tx(full + slot, (uint32_t)(ngroups * 4 * NT + vbytes));
+                mbar_arrive_expect_tx(full + slot, (uint32_t)(ngroups * 4 * RB + vbytes));
             }
             __syncwarp();
             if (lane < ngroups) {
                 uint8_t* dst = rhs_s + slot * RHS_BYTES + lane * 512;  // box rows 4 lane .. 4 lane + 3
 #pragma unroll
-                for (int hf = 0; hf < NT / 128; ++hf)
-                    tma_gather4(dst + hf * 4096, &tmap, full + slot, n0 + hf * 128, yq[0], yq[1], yq[2], yq[3]);
+                for (int hf = 0; hf < G::BOXES; ++hf)
+                    tma_gather4(dst + hf * 4096, &tmap, full + slot, n0 * PREB / 8 + hf * 128, yq[0], yq[1], yq[2],
+                                yq[3]);
             }
             if (lane == 0 && vbytes > 0)
                 bulk_load(aux,
@@ -201,18 +209,51 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const uint32_t keep = whole ? 0xffffffffu : byte_mask(nnz - (step * 32 + 16 * h + 4 * t));
+                    if constexpr (L::VCHUNK == 16) {
 #pragma unroll
-                    for (int bp = 0; bp < BP; ++bp)
-                        vals[bp][h] = lds32(aux + h * 16 * SLOT_BYTES + vword16<V, PREA, 8, EXT>(g, t, bp)) & keep;
+                        for (int bp = 0; bp < BP; ++bp)
+                            vals[bp][h] =
+                                lds32(aux + h * 16 * SLOT_BYTES + vword16<V, PREA, PREB, EXT>(g, t, bp)) & keep;
+                    } else {
+                        // one 32-slot chunk of 4-bit planes [v][slot]
+                        constexpr int PLANE_BYTES = V * 32 * L::PLANE_BITS / 8;
+                        uint32_t nib[L::PLANES];
+#pragma unroll
+                        for (int pl = 0; pl < L::PLANES; ++pl)
+                            nib[pl] = lds16(aux + pl * PLANE_BYTES + g * 16 + 8 * h + 2 * t);
+                        if constexpr (PREA == 4) {
+                            vals[0][h] = unpack4_u16<SIGNED>(nib[0]) & keep;
+                        } else if constexpr (PREA == 8) {
+                            vals[0][h] = merge_nibble_planes(nib[0], nib[1]) & keep;
+                        } else {
+                            vals[0][h] = merge_nibble_planes(nib[0], nib[1]) & keep;
+                            vals[1][h] = merge_nibble_planes(nib[2], nib[3]) & keep;
+                        }
+                    }
                 }
             }
             // A fragments of this warp's 16 MT columns: lane r addresses slot row r
             const uint8_t* st = rhs_s + slot * RHS_BYTES;
             uint32_t af[MT][4];
+            if constexpr (PREB == 8) {
 #pragma unroll
-            for (int m = 0; m < MT; ++m) {
-                const int cc = MT * warp + m;  // 16-byte column chunk in the tile
-                ldsm_x2_trans_b8(af[m], st + (cc >> 3) * 4096 + lane * 128 + (((cc & 7) ^ (lane & 7)) << 4));
+                for (int m = 0; m < MT; ++m) {
+                    const int cc = MT * warp + m;  // 16-byte chunk = 16 columns
+                    ldsm_x2_trans_b8(af[m], st + (cc >> 3) * 4096 + lane * 128 + (((cc & 7) ^ (lane & 7)) << 4));
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < MT / 2; ++k) {
+                    const int cc = (MT / 2) * warp + k;  // 16-byte chunk = 32 columns: tiles 2k (low), 2k+1 (high)
+                    uint32_t nb[4];
+                    ldsm_x2_trans_b8(nb, st + (cc >> 3) * 4096 + lane * 128 + (((cc & 7) ^ (lane & 7)) << 4));
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint32_t lo = nb[q] & 0x0F0F0F0Fu, hi = (nb[q] >> 4) & 0x0F0F0F0Fu;
+                        af[2 * k][q] = SIGNED ? sext_nibble_bytes(lo) : lo;
+                        af[2 * k + 1][q] = SIGNED ? sext_nibble_bytes(hi) : hi;
+                    }
+                }
             }
 #pragma unroll
             for (int bp = 0; bp < BP; ++bp) {
@@ -231,7 +272,8 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
         __syncwarp();  // every lane has read the stage
         if (lane == 0) mbar_arrive(empty + slot);
         if (last) {
-            // acc[.][m][e]: column 16m + 8(e>>1) + g of the warp's slice, vector lane 2t + (e & 1)
+            // acc[.][m][e]: vector lane 2t + (e & 1), column of the warp's slice
+            // 8-bit B: 16m + 8(e>>1) + g;  4-bit B: 32(m>>1) + 2g + (m&1) + 16(e>>1)
             const int row = hdr.x, b = hdr.y;
 #pragma unroll
             for (int e2 = 0; e2 < 2; ++e2) {
@@ -246,16 +288,37 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
                     r4[q] = (int)x;
                 }
                 const long long obase =
-                    (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + warp * 16 * MT + g;
-                if constexpr (HALF_OUT) {
-                    __half* o = reinterpret_cast<__half*>(p.out) + obase;
-                    const Divisor dv = out_divisor(p, b, row * V + v);
+                    (long long)b * p.out_stride + (long long)(row * V + v) * p.n + n0 + warp * 16 * MT;
+                if constexpr (PREB == 8) {
+                    // r4[q]: column 8q + g
+                    if constexpr (HALF_OUT) {
+                        __half* o = reinterpret_cast<__half*>(p.out) + obase + g;
+                        const Divisor dv = out_divisor(p, b, row * V + v);
 #pragma unroll
-                    for (int q = 0; q < 2 * MT; ++q) o[8 * q] = deq_half(r4[q], dv);
+                        for (int q = 0; q < 2 * MT; ++q) o[8 * q] = deq_half(r4[q], dv);
+                    } else {
+                        int* o = reinterpret_cast<int*>(p.out) + obase + g;
+#pragma unroll
+                        for (int q = 0; q < 2 * MT; ++q) stg_cs_s32(o + 8 * q, r4[q]);
+                    }
                 } else {
-                    int* o = reinterpret_cast<int*>(p.out) + obase;
+                    // chunk k: r4[4k], r4[4k+2] -> columns 32k + 2g, +1; r4[4k+1], r4[4k+3] -> +16, +17
+                    if constexpr (HALF_OUT) {
+                        __half* o = reinterpret_cast<__half*>(p.out) + obase + 2 * g;
+                        const Divisor dv = out_divisor(p, b, row * V + v);
 #pragma unroll
-                    for (int q = 0; q < 2 * MT; ++q) stg_cs_s32(o + 8 * q, r4[q]);
+                        for (int k = 0; k < MT / 2; ++k) {
+                            stg_cs_s32(o + 32 * k, (int)pack_half2(r4[4 * k], r4[4 * k + 2], dv));
+                            stg_cs_s32(o + 32 * k + 16, (int)pack_half2(r4[4 * k + 1], r4[4 * k + 3], dv));
+                        }
+                    } else {
+                        int* o = reinterpret_cast<int*>(p.out) + obase + 2 * g;
+#pragma unroll
+                        for (int k = 0; k < MT / 2; ++k) {
+                            stg_cs_v2(o + 32 * k, r4[4 * k], r4[4 * k + 2]);
+                            stg_cs_v2(o + 32 * k + 16, r4[4 * k + 1], r4[4 * k + 3]);
+                        }
+                    }
                 }
             }
 #pragma unroll

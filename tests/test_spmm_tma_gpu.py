@@ -1,6 +1,6 @@
 """The TMA-gather SpMM (MC_KERNEL_TMA: a producer warp gathers B rows with
-tile::gather4 into an mbarrier ring, four consumer warps multiply) against the
-CPU oracle, bit-exact, and against the streaming kernel."""
+tile::gather4 into an mbarrier ring, consumer warps multiply), 8-bit and 4-bit
+B, against the CPU oracle, bit-exact, and against the streaming kernel."""
 import ctypes
 
 import numpy as np
@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 
 RAGGED = [0, 1, 3, 4, 5, 15, 16, 17, 31, 32, 33, 64, 100, 7, 200, 3, 48, 0, 250, 2]
 PAIRS8 = [(8, 8), (16, 8), (12, 8)]
+PAIRS4 = [(4, 4), (8, 4), (16, 4), (12, 4)]
 
 
 def _run(cuda, mask, vals, rhs, pa, pb, N, signed, variant=_lib.KERNEL_TMA, **kw):
@@ -46,67 +47,89 @@ def test_tma_ragged(cuda, pa, pb, V, signed, N):
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("pa", [8, 16])
+@pytest.mark.parametrize("pa,pb", PAIRS4)
+@pytest.mark.parametrize("V", [2, 4, 8])
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("N", [256, 512])
+def test_tma_ragged_4bit_rhs(cuda, pa, pb, V, signed, N):
+    """4-bit B (256 columns per 128-byte row box; column indices shuffled
+    within groups of 8 by the packer), every A precision."""
+    if pa == 12 and signed:
+        pytest.skip("12-bit lanes are unsigned")
+    K = 256
+    mask = synth.lengths_mask(RAGGED, K, V, seed=pa * 10 + V + 1)
+    vals = _vals(mask, V, pa, 32 + V)
+    rhs = synth.random_bytes(K * N // 2, 33 + V)
+    out = _run(cuda, mask, vals, rhs, pa, pb, N, signed)
+    ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N,
+                           16 if pa == 12 else pa, pb, oracle.SIGNED if signed else oracle.UNSIGNED,
+                           **({"preA_cut": 12} if pa == 12 else {}))
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", [(8, 8), (16, 8), (4, 4), (8, 4)])
 @pytest.mark.parametrize("N", [128, 256])
 @pytest.mark.parametrize("shared_rhs", [False, True])
-def test_tma_batched_many_tasks(cuda, pa, N, shared_rhs):
+def test_tma_batched_many_tasks(cuda, pa, pb, N, shared_rhs):
     """Far more tasks than resident CTAs (every CTA streams many rows through
     its ring), per-entry values, B per entry or shared (rhs_stride 0)."""
+    if pb == 4:
+        N *= 2  # 4-bit B runs 256-column tiles
     V, K, B = 8, 512, 4
     lengths = np.random.default_rng(pa + N).integers(0, 90, size=700)
     lengths[::29] = 0
     lengths[3] = 512
     mask = synth.lengths_mask(lengths, K, V, seed=41)
     vals_all = [_vals(mask, V, pa, 50 + b) for b in range(B)]
-    rhs_all = [synth.random_bytes(K * N, 60 + b) for b in range(B)]
+    rhs_all = [synth.random_bytes(K * N * pb // 8, 60 + b) for b in range(B)]
     if shared_rhs:
         rhs_all = [rhs_all[0]] * B
-    packed = [formats.prepare_spmm(mask, v, pa, 8) for v in vals_all]
+    packed = [formats.prepare_spmm(mask, v, pa, pb) for v in vals_all]
     d = ops.DeviceSpmmLhs.from_host(packed[0], cuda)
     d.values = torch.from_numpy(np.concatenate([p.values for p in packed])).to(cuda)
     rhs = torch.from_numpy(rhs_all[0] if shared_rhs else np.concatenate(rhs_all)).to(cuda)
     out = ops.spmm(d, rhs, N, signed=True, batch=B, values_stride=packed[0].values.size,
-                   rhs_stride=0 if shared_rhs else K * N, variant=_lib.KERNEL_TMA)
+                   rhs_stride=0 if shared_rhs else K * N * pb // 8, variant=_lib.KERNEL_TMA)
     for b in range(B):
         ref = oracle.spmm_host(vals_all[b], rhs_all[b], mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N,
-                               pa, 8, oracle.SIGNED)
+                               pa, pb, oracle.SIGNED)
         np.testing.assert_array_equal(out[b].cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("pa", [8, 16])
+@pytest.mark.parametrize("pa,pb", [(8, 8), (16, 8), (4, 4), (8, 4), (16, 4)])
 @pytest.mark.parametrize("signed", [False, True])
 @pytest.mark.parametrize("fill", [0x00, 0xFF, 0x80, 0x7F, "alt"])
-def test_tma_extreme_values_long_rows(cuda, pa, signed, fill):
-    V, K, N = 8, 2048, 128
+def test_tma_extreme_values_long_rows(cuda, pa, pb, signed, fill):
+    V, K, N = 8, 2048, 128 if pb == 8 else 256
     mask = synth.lengths_mask([2048, 1000, 257, 256, 255, 0, 31, 1], K, V, seed=17)
-    nv, nr = mask.nnz_vec * V * pa // 8, K * N
+    nv, nr = mask.nnz_vec * V * pa // 8, K * N * pb // 8
     if fill == "alt":
         vals = np.tile(np.array([0x80, 0x7F], np.uint8), nv // 2 + 1)[:nv]
         rhs = np.tile(np.array([0x7F, 0x80, 0xFF, 0x00], np.uint8), nr // 4 + 1)[:nr]
     else:
         vals, rhs = np.full(nv, fill, np.uint8), np.full(nr, fill, np.uint8)
-    out = _run(cuda, mask, vals, rhs, pa, 8, N, signed)
-    ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, 8,
+    out = _run(cuda, mask, vals, rhs, pa, pb, N, signed)
+    ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
                            oracle.SIGNED if signed else oracle.UNSIGNED)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("pa", [8, 16])
+@pytest.mark.parametrize("pa,pb", [(8, 8), (16, 8), (4, 4), (8, 4)])
 @pytest.mark.parametrize("V", [2, 4, 8])
-def test_tma_half_output_equals_stream(cuda, pa, V):
+def test_tma_half_output_equals_stream(cuda, pa, pb, V):
     """Dequantised half output on the softmax value layout, bit-identical to
     the streaming kernel and to the oracle's integer result / scale."""
     K, N, scale = 512, 256, 36.0 * 32.0
     mask = synth.lengths_mask(RAGGED, K, V, seed=70 + V)
     vals = _vals(mask, V, pa, 71)
-    rhs = synth.random_bytes(K * N, 72)
-    h = formats.prepare_spmm(mask, vals, pa, 8, layout=formats.VALUES_SOFTMAX)
+    rhs = synth.random_bytes(K * N * pb // 8, 72)
+    h = formats.prepare_spmm(mask, vals, pa, pb, layout=formats.VALUES_SOFTMAX)
     d = ops.DeviceSpmmLhs.from_host(h, cuda)
     r = torch.from_numpy(rhs).to(cuda)
     outs = [ops.spmm(d, r, N, signed=True, out_half=True, scale=scale, variant=v)
             for v in (_lib.KERNEL_TMA, _lib.KERNEL_STREAM)]
     assert torch.equal(outs[0], outs[1])
-    acc = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, 8, oracle.SIGNED)
+    acc = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb, oracle.SIGNED)
     ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
     np.testing.assert_array_equal(outs[0].cpu().numpy().view(np.uint16), ref.view(np.uint16))
 
@@ -134,7 +157,7 @@ def test_tma_rejects_ineligible(cuda):
     V, K = 8, 256
     mask = synth.lengths_mask([5, 40], K, V, seed=3)
     for pa, pb, N, mma in ((8, 8, 64, _lib.MMA_INT8), (8, 4, 128, _lib.MMA_INT8), (8, 8, 128, _lib.MMA_F16),
-                           (16, 16, 128, _lib.MMA_INT8)):
+                           (16, 16, 128, _lib.MMA_INT8), (4, 4, 384, _lib.MMA_INT8)):
         vals = _vals(mask, V, pa, 1)
         rhs = synth.random_bytes(K * N * pb // 8, 2)
         with pytest.raises(_lib.MagicubeError):

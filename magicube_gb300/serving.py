@@ -94,6 +94,48 @@ def _max_row(m) -> int:
     return int(np.diff(m.row_offsets).max()) if m.m_vec else 0
 
 
+def _upload_csr(req: Request, device) -> None:
+    """Copy a request's tokens and the plain CSR of its masks to the device
+    (once); the server packs whole batches from these."""
+    if req.dev:
+        return
+    dev = torch.device(device)
+    req.dev["x"] = req.x.to(dev, non_blocking=True)
+    req.dev["csr"] = [(torch.from_numpy(m.row_offsets).to(dev, non_blocking=True),
+                       torch.from_numpy(m.col_indices).to(dev, non_blocking=True), m.m_vec, m.nnz_vec, _max_row(m))
+                      for m in req.masks]
+
+
+def pack_batch_masks(reqs: list[Request], layers: int, V: int, alignment: int, device) -> list[AttentionMaskDev]:
+    """One block-diagonal attention mask per layer over the batch: the
+    requests' CSRs are concatenated on the device (row offsets shifted by the
+    nonzeros before them, column indices by the tokens before them) and
+    packed by one device packer call per layer, rows longest first across
+    the whole batch.  Each row's result is the same as in its own mask."""
+    dev = torch.device(device)
+    lens = [r.seq_len for r in reqs]
+    tok_base = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int32)
+    total_tokens = int(sum(lens))
+    out = []
+    for l in range(layers):
+        csr = [r.dev["csr"][l] for r in reqs]
+        m_vecs = [c[2] for c in csr]
+        nnzs = [c[3] for c in csr]
+        nnz_base = np.concatenate([[0], np.cumsum(nnzs)[:-1]]).astype(np.int32)
+        total_m, total_nnz = int(sum(m_vecs)), int(sum(nnzs))
+        shifts = torch.from_numpy(np.stack([nnz_base, tok_base])).to(dev, non_blocking=True)
+        counts = torch.from_numpy(np.array([m_vecs, nnzs], dtype=np.int64)).to(dev, non_blocking=True)
+        ro = torch.cat([torch.zeros(1, dtype=torch.int32, device=dev)] + [c[0][1:] for c in csr])
+        ro[1:] += torch.repeat_interleave(shifts[0], counts[0], output_size=total_m)
+        ci = torch.cat([c[1] for c in csr]) if total_nnz else torch.zeros(0, dtype=torch.int32, device=dev)
+        if total_nnz:
+            ci += torch.repeat_interleave(shifts[1], counts[1], output_size=total_nnz)
+        dm = device_format.prepare_sddmm(ro, ci, V, total_tokens, alignment=alignment, sync=False)
+        out.append(AttentionMaskDev(total_m, V, total_tokens, dm.aligned_nnz, dm.row_indices, dm.row_offsets,
+                                    dm.col_indices, max(c[4] for c in csr)))
+    return out
+
+
 def batch_masks(reqs: list[Request], layers: int, V: int) -> list[AttentionMaskDev]:
     """One block-diagonal attention mask per layer over the batch (device ops)."""
     out = []
@@ -195,9 +237,9 @@ class ContinuousBatchingServer:
                         s = self.streams[si]
                         with torch.cuda.stream(s):
                             for r in batch:
-                                _upload(r, self.alignment, self.device)
+                                _upload_csr(r, self.device)
                                 r.t_admit = time.perf_counter() - t0
-                            masks = batch_masks(batch, self.layers, self.V)
+                            masks = pack_batch_masks(batch, self.layers, self.V, self.alignment, self.device)
                             x = torch.cat([r.dev["x"] for r in batch], dim=0)
                             y = self.model(x, masks)
                             off = 0

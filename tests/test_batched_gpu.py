@@ -92,6 +92,31 @@ def test_encoder_fused_attention_equals_separate(cuda, requant):
     assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("attention", ["separate", "fused"])
+def test_batch_packed_masks_give_same_output(cuda, attention):
+    """Masks of a whole batch packed by one device call per layer (rows sorted
+    across requests) give the same encoder output, bit for bit, as the
+    per-request packed masks stacked block-diagonally."""
+    torch.manual_seed(0)
+    enc = model.SparseEncoder(layers=2, hidden=256, heads=4, ffn=512).to(cuda).half().eval()
+    enc.set_attention(attention)
+    kw = dict(rate=0.0, hidden=256, layers=2, sparsity=0.9, median=256, clip=(128, 640), seed=9)
+    a_reqs, b_reqs = serving.make_requests(5, **kw), serving.make_requests(5, **kw)
+    for r in a_reqs:
+        serving._upload(r, 16, cuda)
+    for r in b_reqs:
+        serving._upload_csr(r, cuda)
+    ma = serving.batch_masks(a_reqs, 2, 8)
+    mb = serving.pack_batch_masks(b_reqs, 2, 8, 16, cuda)
+    assert [m.max_row_nnz for m in ma] == [m.max_row_nnz for m in mb]
+    x = torch.cat([r.dev["x"] for r in a_reqs], dim=0)
+    with torch.no_grad():
+        ya = enc(x, ma).clone()
+        yb = enc(x, mb).clone()
+    torch.cuda.synchronize()
+    assert torch.equal(ya, yb)
+
+
 def test_server_fused_mixed_same_as_sequential_separate(cuda):
     """Continuous batching on the fused attention kernel against one request
     at a time on the separate launches: the same results within the fp16

@@ -8,6 +8,9 @@ CPU leg).  numpy restatements of:
     / sum over the row's nonzeros, q = trunc(clamp(p * scale)), written in
     the softmax value layout ([v][16] per 16 slots for 8 bits, lo/hi byte
     halves per lane for 16 bits, nibbles [v][32] per 32 slots for 4 bits);
+  * the library's row-max requantization (q = round(127 exp(x - max)) and a
+    divisor 127 * sum * scale per row and lane), which has no reference
+    counterpart;
   * the unquantized sparse attention in float64 (the accuracy reference of
     the quantized pipeline): softmax(Q K^T * s) restricted to the vector mask,
     times V.
@@ -61,6 +64,34 @@ def softmax_quant(scores: np.ndarray, pairs: np.ndarray, row_indices: np.ndarray
                     o = base + (j // 32) * V * 16 + v * 16 + (j % 32) // 2
                     out[o] |= (val & 0xF) << (4 * (j % 2))
     return out, exact
+
+
+def softmax_rowmax(scores: np.ndarray, pairs: np.ndarray, row_indices: np.ndarray, V: int, scaling: float,
+                   scale: float, out_bytes: int, m_vec: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """The library's row-max requantization (no reference counterpart): per
+    vector-row and lane, x = float32(score) * scaling, q = round(127 exp(x -
+    max)) in the 8-bit softmax layout, divisor 127 * sum(exp) * scale.
+    Returns (packed bytes, divisors [m_vec * V], the unrounded 127 exp(x - max)
+    per (slot, lane) for tolerance checks)."""
+    out = np.zeros(out_bytes, dtype=np.uint8)
+    div = np.zeros(m_vec * V, dtype=np.float32)
+    exact = np.zeros(scores.size, dtype=np.float64)
+    for r in row_indices:
+        s, e = int(pairs[2 * r]), int(pairs[2 * r + 1])
+        n = e - s
+        if n == 0:
+            continue
+        x = scores[s * V:e * V].reshape(n, V).astype(np.float32) * np.float32(scaling)
+        ex = np.exp(x - x.max(axis=0))
+        div[r * V:(r + 1) * V] = np.float32(127.0) * ex.sum(axis=0, dtype=np.float32) * np.float32(scale)
+        p = np.float32(127.0) * ex
+        exact[s * V:e * V] = p.ravel()
+        q = np.rint(p).astype(np.int64)
+        base = s * V
+        for j in range(n):
+            for v in range(V):
+                out[base + (j // 16) * V * 16 + v * 16 + j % 16] = int(q[j, v]) & 0xFF
+    return out, div, exact
 
 
 def dense_mask(pairs: np.ndarray, cols: np.ndarray, m_vec: int, V: int, ncols: int) -> np.ndarray:

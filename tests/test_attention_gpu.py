@@ -93,6 +93,40 @@ def test_q_bcsr_softmax(cuda, bits, scale, V):
         np.testing.assert_array_equal(g[safe], r[safe])
 
 
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_softmax_rowmax_and_row_divisors(cuda, V):
+    """mcQuantSoftmax with MC_REQUANT_ROWMAX against the oracle: every
+    probability within 1 of round(127 exp(x - max)) and equal where that value
+    is not within 1e-3 of a rounding boundary; the per-row divisors within
+    1e-5 relative (float32 sums in another order)."""
+    import ctypes
+    from magicube_gb300 import _lib
+    L, B, scale = 256, 2, 44.0
+    m, cols, pairs, ri, n = _mask(L, V, 8, seed=13)
+    rng = np.random.default_rng(7)
+    scores = (rng.standard_normal((B, n * V)) * 3).astype(np.float16)
+    sc = torch.from_numpy(scores).to(cuda)
+    out = torch.zeros((B, n * V), dtype=torch.uint8, device=cuda)
+    div = torch.full((B, m.m_vec * V), -1.0, dtype=torch.float32, device=cuda)
+    d = _lib.McSoftmaxDesc(m_vec=m.m_vec, vec_length=V, batch=B, bits=8, scaling=1.0, scale=scale,
+                           row_indices=ri.data_ptr(), row_offsets=pairs.data_ptr(), scores=sc.data_ptr(),
+                           scores_stride=n * V, out=out.data_ptr(), out_stride=n * V, requant=_lib.REQUANT_ROWMAX,
+                           row_div=div.data_ptr(), row_div_stride=m.m_vec * V)
+    _lib.check(_lib.lib().mcQuantSoftmax(ctypes.byref(d), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               "mcQuantSoftmax")
+    got, gdiv = out.cpu().numpy(), div.cpu().numpy()
+    hp, hr = pairs.cpu().numpy(), ri.cpu().numpy()
+    for b in range(B):
+        ref, rdiv, exact = oatt.softmax_rowmax(scores[b], hp, hr, V, 1.0, scale, n * V, m.m_vec)
+        g = _decode_softmax(got[b], hp, V, 8, n)
+        r = _decode_softmax(ref, hp, V, 8, n)
+        assert np.abs(g - r).max() <= 1
+        frac = np.abs(exact.reshape(n, V) - np.floor(exact.reshape(n, V)) - 0.5)
+        safe = frac > 1e-3
+        np.testing.assert_array_equal(g[safe], r[safe])
+        np.testing.assert_allclose(gdiv[b], rdiv, rtol=1e-5)
+
+
 @pytest.mark.parametrize("pa,pb", [(4, 4), (8, 4), (8, 8), (16, 8)])
 @pytest.mark.parametrize("V", [2, 8])
 def test_bspmm(cuda, pa, pb, V):

@@ -860,18 +860,18 @@ def run_profile_case(args) -> None:
 
     from magicube_gb300 import formats, ops, synth
     dev = torch.device("cuda:0")
-    if args.profile == "attention":
+    if args.profile in ("attention", "attention-steps"):
         from magicube_gb300 import batched, synth
         rng = np.random.default_rng(11)
         lens = (rng.integers(512, 4097, size=args.batch) // 64 * 64).clip(512, 4096).tolist()
         masks = [synth.band_random_mask(L, VEC, 256, 0.9, seed=100 + i) for i, L in enumerate(lens)]
         f = batched.BatchedSparseAttention(masks, 4, 64, 8, 8, scale_qkv=40.0, scale_sfmx=127.0, device=dev,
-                                           fused=True, requant=args.requant)
+                                           fused=args.profile == "attention", requant=args.requant, tune=True)
         f.qkv.copy_((torch.randn(f.qkv.shape, generator=torch.Generator().manual_seed(12)) * 0.5).half())
         for _ in range(args.reps):
             f()
         torch.cuda.synchronize()
-        print(json.dumps({"profile_case": "attention", "instances": args.batch, "reps": args.reps}))
+        print(json.dumps({"profile_case": args.profile, "instances": args.batch, "reps": args.reps}))
         return
     if args.profile == "projection":
         from magicube_gb300.projection import qkv_project_quantize
@@ -931,7 +931,8 @@ def main() -> None:
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--requant", choices=["fixed", "rowmax"], default="rowmax",
                     help="requantization of the --profile attention case")
-    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention", "packer", "projection"], default=None,
+    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention", "attention-steps", "packer", "projection"],
+                    default=None,
                     help="run only a small case of one kernel (for ncu captures)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")
     ap.add_argument("--serving-rates", type=lambda x: [float(v) for v in x.split(",")],

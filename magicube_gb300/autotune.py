@@ -3,7 +3,8 @@
 For a problem signature (operation, precision pair, V, dense width, row-length
 and row-count buckets, batch bucket) it times every candidate configuration on
 the caller's own buffers -- tensor path (int8 or exact f16), kernel variant
-(per-row or pipelined/streaming), and for SDDMM the number of CTAs per
+(per-row, pipelined/streaming, or for SpMM the TMA-gather kernel where it
+applies), and for SDDMM the number of CTAs per
 vector-row -- and keeps the fastest.  Results persist in a JSON cache
 (``$MC_AUTOTUNE_CACHE``, default ``~/.cache/magicube_gb300/autotune.json``) so
 a shape bucket is tuned once per machine.  Every candidate computes the same
@@ -64,8 +65,9 @@ def signature(op: str, lhs_bits: int, rhs_bits: int, V: int, width: int, rows: i
 
 
 def spmm_candidates() -> list[dict]:
-    return [{"mma_kind": m, "variant": v} for m in (_lib.MMA_INT8, _lib.MMA_F16)
-            for v in (_lib.KERNEL_PER_ROW, _lib.KERNEL_STREAM)]
+    out = [{"mma_kind": m, "variant": v} for m in (_lib.MMA_INT8, _lib.MMA_F16)
+           for v in (_lib.KERNEL_PER_ROW, _lib.KERNEL_STREAM)]
+    return out + [{"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_TMA}]
 
 
 def sddmm_candidates(k: int) -> list[dict]:

@@ -726,8 +726,8 @@ def serving_suite(args, dev) -> dict:
 
 
 def tensor_peaks(dev) -> dict:
-    """Measured mma.sync peaks (TOP/s) of the int8 (k = 32 and k = 16), int4
-    and f16 paths."""
+    """Measured tensor peaks (TOP/s): mma.sync int8 (k = 32 and k = 16), int4
+    and f16; tcgen05.mma kind::f16 at M = 128, N = 16 / 64 / 256."""
     import torch
 
     from magicube_gb300 import _lib
@@ -740,6 +740,14 @@ def tensor_peaks(dev) -> dict:
                                                 ctypes.byref(ops), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                    "mcProbeTensorPeak")
         out[name] = ops.value / (ms.value * 1e-3) / 1e12
+    timeouts = torch.zeros(1, dtype=torch.int32, device=dev)
+    for n in (16, 64, 256):  # tcgen05.mma kind::f16, M = 128, K = 16 (padding included)
+        ms, ops = ctypes.c_float(), ctypes.c_double()
+        _lib.check(_lib.lib().mcProbeTensorCorePeak(n, 8000, ctypes.byref(ms), ctypes.byref(ops),
+                                                    timeouts.data_ptr(),
+                                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                   "mcProbeTensorCorePeak")
+        out[f"tcgen05_f16_m128n{n}"] = ops.value / (ms.value * 1e-3) / 1e12
     return out
 
 

@@ -225,6 +225,14 @@ int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
 int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, float* ms_out,
                       double* ops_out, cudaStream_t stream);
 
+/* mcProbeTensorCorePeak: times one launch of one CTA per SM whose single
+ * issuing thread runs iters x 4 back-to-back tcgen05.mma kind::f16 of
+ * M = 128, N = n (16, 64 or 256), K = 16 into TMEM; returns the duration and
+ * the operation count (2 per MAC, padding included).  timeouts: device
+ * counter of completion waits that ran out (0 unless the device stalled). */
+int mcProbeTensorCorePeak(int n, int iters, float* ms_out, double* ops_out, unsigned int* timeouts,
+                          cudaStream_t stream);
+
 /* mcCheckQuotients: compares, bit for bit, the dequantisation quotient the
  * kernels compute from a prepared divisor (RN(1/d) and two FMA correction
  * steps) with the IEEE division a / d for every integer numerator a in

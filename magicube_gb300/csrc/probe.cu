@@ -5,8 +5,56 @@
 
 #include "mc_host.h"
 #include "mc_ptx.cuh"
+#include "mc_sm100.cuh"
 
 namespace mc {
+
+// One CTA per SM; thread 0 issues `iters` x 4 back-to-back tcgen05.mma
+// kind::f16 (M = 128, N, K = 16, f32 accumulator in TMEM) from zeroed
+// 128-byte-swizzled shared-memory tiles, commits once and waits (bounded).
+// *timeouts counts waits that ran out.
+template <int N>
+__global__ void __launch_bounds__(128) tc_peak_kernel(int iters, unsigned int* timeouts)
+{
+    using namespace sm100;
+    constexpr int TCOLS = N < 32 ? 32 : N;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
+    uint8_t* at = smem;                      // 128 rows x 128 B
+    uint8_t* bt = smem + 128 * 128;          // N rows x 128 B
+    uint64_t* done = reinterpret_cast<uint64_t*>(bt + N * 128);
+    uint32_t* tmem_s = reinterpret_cast<uint32_t*>(done + 1);
+    const int tid = threadIdx.x;
+    for (int i = tid; i < (128 + N) * 8; i += 128) reinterpret_cast<uint4*>(smem)[i] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        mbar_init(done, 1);
+        fence_mbar_init();
+    }
+    if (tid < 32) {
+        tmem_alloc(tmem_s, TCOLS);
+        tmem_relinquish();
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_s;
+    if (tid == 0) {
+        const uint64_t ad = desc_sw128_kmajor(saddr(at)), bd = desc_sw128_kmajor(saddr(bt));
+        constexpr uint32_t idesc = idesc_f16_f32(128, N);
+        for (int it = 0; it < iters; ++it)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) mma_f16_ss(tmem, ad + 2 * k, bd + 2 * k, idesc, (it | k) != 0);
+        mma_commit(done);
+        if (!mbar_wait(done, 0, 4000000000LL)) atomicAdd(timeouts, 1u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (tid < 32) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TCOLS);
+    }
+}
 
 // Compares div_rn (the kernels' quotient from a prepared divisor) with the
 // IEEE division __fdiv_rn for every integer numerator in [lo, hi), bit for
@@ -103,6 +151,37 @@ extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int
     cudaEventDestroy(e1);
     const double macs = kind == 0 ? 16.0 * 8 * 32 : (kind == 1 ? 16.0 * 8 * 64 : 16.0 * 8 * 16);  // kinds 2, 3: k = 16
     *ops_out = 2.0 * macs * (double)blocks * (threads / 32) * iters * 8;
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mcProbeTensorCorePeak(int n, int iters, float* ms_out, double* ops_out, unsigned int* timeouts,
+                                     cudaStream_t stream)
+{
+    mc::clear_error();
+    if (!(n == 16 || n == 64 || n == 256) || iters <= 0 || !ms_out || !ops_out || !timeouts)
+        return mc::fail(1, "mcProbeTensorCorePeak: n must be 16, 64 or 256; iters > 0; non-null outputs");
+    const int sms = mc::sm_count();
+    const size_t smem = 1024 + (size_t)(128 + n) * 128 + 64;
+    auto launch = [&]() {
+        if (n == 16) mc::tc_peak_kernel<16><<<sms, 128, smem, stream>>>(iters, timeouts);
+        else if (n == 64) mc::tc_peak_kernel<64><<<sms, 128, smem, stream>>>(iters, timeouts);
+        else mc::tc_peak_kernel<256><<<sms, 128, smem, stream>>>(iters, timeouts);
+    };
+    if (n == 256 && cudaFuncSetAttribute(mc::tc_peak_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem) != cudaSuccess)
+        return (int)cudaGetLastError();
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    launch();  // warm-up
+    cudaEventRecord(e0, stream);
+    launch();
+    cudaEventRecord(e1, stream);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(ms_out, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ops_out = 2.0 * 128.0 * n * 16.0 * 4.0 * (double)iters * sms;
     return (int)cudaGetLastError();
 }
 

@@ -100,3 +100,18 @@ def test_tc_sddmm_rejects_other_shapes(cuda):
         ops.sddmm(dm, lhs, rhs, 128, 8, 8, signed=True, mma_kind=TC)  # k != 64
     with pytest.raises(_lib.MagicubeError):
         ops.sddmm(dm, lhs, rhs, 64, 4, 4, signed=True, mma_kind=TC)  # 4-bit
+
+
+@pytest.mark.parametrize("n", [16, 64, 256])
+def test_tcgen05_throughput_probe(cuda, n):
+    """The tcgen05 probe runs to completion (no wait ran out) and reports a
+    positive rate."""
+    import ctypes
+    timeouts = torch.zeros(1, dtype=torch.int32, device=cuda)
+    ms, ops = ctypes.c_float(), ctypes.c_double()
+    _lib.check(_lib.lib().mcProbeTensorCorePeak(n, 200, ctypes.byref(ms), ctypes.byref(ops), timeouts.data_ptr(),
+                                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               "mcProbeTensorCorePeak")
+    torch.cuda.synchronize()
+    assert int(timeouts.item()) == 0
+    assert ms.value > 0 and ops.value == 2.0 * 128 * n * 16 * 4 * 200 * torch.cuda.get_device_properties(0).multi_processor_count

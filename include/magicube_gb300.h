@@ -228,8 +228,11 @@ int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, flo
 /* mcProbeTensorCorePeak: times one launch of one CTA per SM whose single
  * issuing thread runs iters x 4 back-to-back tcgen05.mma kind::f16 of
  * M = 128, N = n (16, 64 or 256), K = 16 into TMEM; returns the duration and
- * the operation count (2 per MAC, padding included).  timeouts: device
- * counter of completion waits that ran out (0 unless the device stalled). */
+ * the operation count (2 per MAC, padding included).  n < 0 (N = -n)
+ * commits each group of four and waits for it before the next: the
+ * duration / iters is then the issue-to-completion latency of a group.
+ * timeouts: device counter of completion waits that ran out (0 unless the
+ * device stalled). */
 int mcProbeTensorCorePeak(int n, int iters, float* ms_out, double* ops_out, unsigned int* timeouts,
                           cudaStream_t stream);
 

@@ -13,7 +13,7 @@ namespace mc {
 // kind::f16 (M = 128, N, K = 16, f32 accumulator in TMEM) from zeroed
 // 128-byte-swizzled shared-memory tiles, commits once and waits (bounded).
 // *timeouts counts waits that ran out.
-template <int N>
+template <int N, bool LATENCY>
 __global__ void __launch_bounds__(128) tc_peak_kernel(int iters, unsigned int* timeouts)
 {
     using namespace sm100;
@@ -42,11 +42,23 @@ __global__ void __launch_bounds__(128) tc_peak_kernel(int iters, unsigned int* t
     if (tid == 0) {
         const uint64_t ad = desc_sw128_kmajor(saddr(at)), bd = desc_sw128_kmajor(saddr(bt));
         constexpr uint32_t idesc = idesc_f16_f32(128, N);
-        for (int it = 0; it < iters; ++it)
+        uint32_t phase = 0;
+        for (int it = 0; it < iters; ++it) {
 #pragma unroll
             for (int k = 0; k < 4; ++k) mma_f16_ss(tmem, ad + 2 * k, bd + 2 * k, idesc, (it | k) != 0);
-        mma_commit(done);
-        if (!mbar_wait(done, 0, 4000000000LL)) atomicAdd(timeouts, 1u);
+            if (LATENCY) {  // each group of four waited for before the next is issued
+                mma_commit(done);
+                if (!mbar_wait(done, phase, 4000000000LL)) {
+                    atomicAdd(timeouts, 1u);
+                    break;
+                }
+                phase ^= 1u;
+            }
+        }
+        if (!LATENCY) {
+            mma_commit(done);
+            if (!mbar_wait(done, 0, 4000000000LL)) atomicAdd(timeouts, 1u);
+        }
     }
     tc_fence_before();
     __syncthreads();
@@ -158,17 +170,28 @@ extern "C" int mcProbeTensorCorePeak(int n, int iters, float* ms_out, double* op
                                      cudaStream_t stream)
 {
     mc::clear_error();
+    const bool latency = n < 0;  // -n: each group of four MMAs committed and waited for in turn
+    if (latency) n = -n;
     if (!(n == 16 || n == 64 || n == 256) || iters <= 0 || !ms_out || !ops_out || !timeouts)
-        return mc::fail(1, "mcProbeTensorCorePeak: n must be 16, 64 or 256; iters > 0; non-null outputs");
+        return mc::fail(1, "mcProbeTensorCorePeak: |n| must be 16, 64 or 256; iters > 0; non-null outputs");
     const int sms = mc::sm_count();
     const size_t smem = 1024 + (size_t)(128 + n) * 128 + 64;
     auto launch = [&]() {
-        if (n == 16) mc::tc_peak_kernel<16><<<sms, 128, smem, stream>>>(iters, timeouts);
-        else if (n == 64) mc::tc_peak_kernel<64><<<sms, 128, smem, stream>>>(iters, timeouts);
-        else mc::tc_peak_kernel<256><<<sms, 128, smem, stream>>>(iters, timeouts);
+        if (n == 16) {
+            if (latency) mc::tc_peak_kernel<16, true><<<sms, 128, smem, stream>>>(iters, timeouts);
+            else mc::tc_peak_kernel<16, false><<<sms, 128, smem, stream>>>(iters, timeouts);
+        } else if (n == 64) {
+            if (latency) mc::tc_peak_kernel<64, true><<<sms, 128, smem, stream>>>(iters, timeouts);
+            else mc::tc_peak_kernel<64, false><<<sms, 128, smem, stream>>>(iters, timeouts);
+        } else {
+            if (latency) mc::tc_peak_kernel<256, true><<<sms, 128, smem, stream>>>(iters, timeouts);
+            else mc::tc_peak_kernel<256, false><<<sms, 128, smem, stream>>>(iters, timeouts);
+        }
     };
-    if (n == 256 && cudaFuncSetAttribute(mc::tc_peak_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem) != cudaSuccess)
+    if (n == 256 && (cudaFuncSetAttribute(mc::tc_peak_kernel<256, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem) != cudaSuccess ||
+                     cudaFuncSetAttribute(mc::tc_peak_kernel<256, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem) != cudaSuccess))
         return (int)cudaGetLastError();
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);

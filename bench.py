@@ -226,15 +226,12 @@ def run_reference(args) -> None:
 
 def run_gpu(args) -> None:
     import torch
-    import torch.distributed as dist
 
     from magicube_gb300 import ops
+    from magicube_gb300.replicas import Replicas
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
+    reps = Replicas("nccl")
+    world, rank, local = reps.world, reps.rank, reps.local
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
@@ -242,15 +239,10 @@ def run_gpu(args) -> None:
 
     def sync_all():
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
+        reps.barrier()
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reps.max(x, dev)
 
     B = args.batch
     results = {}
@@ -381,8 +373,7 @@ def run_gpu(args) -> None:
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline()
         print(json.dumps(line))
-    if world > 1:
-        dist.destroy_process_group()
+    reps.close()
 
 
 def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma: int, variant: int = 0) -> dict:

@@ -725,7 +725,8 @@ def tensor_peaks(dev) -> dict:
     sink = torch.empty(4 * 256 * 8 * torch.cuda.get_device_properties(dev).multi_processor_count,
                        dtype=torch.uint8, device=dev)
     out = {}
-    for kind, name in ((0, "int8_mma_sync"), (1, "int4_mma_sync"), (2, "f16_mma_sync"), (3, "int8_k16_mma_sync")):
+    for kind, name in ((0, "int8_mma_sync"), (1, "int4_mma_sync"), (2, "f16_mma_sync"), (3, "int8_k16_mma_sync"),
+                       (4, "int8_dp4a")):
         ms, ops = ctypes.c_float(), ctypes.c_double()
         _lib.check(_lib.lib().mcProbeTensorPeak(kind, sink.data_ptr(), sink.numel(), 2048, ctypes.byref(ms),
                                                 ctypes.byref(ops), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),

@@ -218,7 +218,8 @@ int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
 /* ---- Diagnostics ---------------------------------------------------------------
  * mcProbeTensorPeak: times one full-grid launch of back-to-back independent
  * mma.sync of `kind` (0: m16n8k32 s8, 1: m16n8k64 s4, 2: m16n8k16 f16 with f32
- * accumulators, 3: m16n8k16 s8) and returns its duration and operation count (2 per MAC), the
+ * accumulators, 3: m16n8k16 s8; 4: the CUDA-core dp4a.s32.s32, four MACs per
+ * thread instruction) and returns its duration and operation count (2 per MAC), the
  * measured tensor peak its kernels are compared with.  sink: device buffer of
  * at least 4 bytes x 256 threads x 8 CTAs x SMs that receives each thread's
  * (meaningless) accumulator sum, so the MMAs are not optimised away. */

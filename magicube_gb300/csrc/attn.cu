@@ -86,9 +86,83 @@ __device__ __forceinline__ void load_vec(const __half* p, float (&x)[V], float s
     }
 }
 
-// ROWMAX (8 bits): q = round(127 exp(x - max)), and lane 0 writes the row
-// divisors 127 * sum * scale -- the separate-launch form of the fused
-// kernel's row-max mode (same expressions, same summation order).
+// Running maximum and minimum of raw half scores, V lanes as V/2 half2.
+template <int V>
+struct HalfRange {
+    __half2 hi[V / 2], lo[V / 2];
+    __device__ __forceinline__ HalfRange()
+    {
+#pragma unroll
+        for (int i = 0; i < V / 2; ++i) {
+            hi[i] = __half2half2(__ushort_as_half((unsigned short)0xFC00u));  // -inf
+            lo[i] = __half2half2(__ushort_as_half((unsigned short)0x7C00u));  // +inf
+        }
+    }
+    __device__ __forceinline__ void add(const __half* p)
+    {
+        __half2 h[V / 2];
+        if constexpr (V == 8) *reinterpret_cast<int4*>(h) = *reinterpret_cast<const int4*>(p);
+        else if constexpr (V == 4) *reinterpret_cast<int2*>(h) = *reinterpret_cast<const int2*>(p);
+        else *reinterpret_cast<int*>(h) = *reinterpret_cast<const int*>(p);
+#pragma unroll
+        for (int i = 0; i < V / 2; ++i) {
+            hi[i] = __hmax2(hi[i], h[i]);  // a NaN input yields the other operand
+            lo[i] = __hmin2(lo[i], h[i]);
+        }
+    }
+    // max over the slots of x = float(h) * s, with -FLT_MAX for none: the
+    // scaling is monotone in h (non-decreasing for s >= 0, non-increasing for
+    // s < 0), so the maximum is the scaled maximum or the scaled minimum; a
+    // NaN product (s = 0 or infinite against an infinite or zero h) is
+    // ignored by fmaxf as it is when every slot is scaled first.  A lane that
+    // saw no slot, or only NaN, still has min > max (the initial +inf and
+    // -inf) and keeps -FLT_MAX.
+    __device__ __forceinline__ void scaled_max(float s, float (&mx)[V]) const
+    {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const __half a = (v & 1) ? __high2half(hi[v / 2]) : __low2half(hi[v / 2]);
+            const __half b = (v & 1) ? __high2half(lo[v / 2]) : __low2half(lo[v / 2]);
+            mx[v] = __hgt(b, a) ? -FLT_MAX
+                                : fmaxf(-FLT_MAX, fmaxf(__fmul_rn(__half2float(a), s), __fmul_rn(__half2float(b), s)));
+        }
+    }
+};
+
+// Stores the probabilities of slots j (even) and j + 1 of lane v.  `two`:
+// slot j + 1 is in the row (otherwise q1 is 0 and, for 8 and 16 bits, only
+// slot j is written).  Layouts (relative to the row start): 8 bits
+// [j/16][V][16] bytes; 16 bits [j/16][V][low 16 | high 16] bytes; 4 bits
+// [j/32][V][16] bytes, slot j in the low and j + 1 in the high nibble.
+template <int V, int BITS>
+__device__ __forceinline__ void store_pair(uint8_t* out, int j, int v, int q0, int q1, bool two)
+{
+    if constexpr (BITS == 8) {
+        uint8_t* o = out + (j >> 4) * V * 16 + v * 16 + (j & 15);
+        if (two) *reinterpret_cast<uint16_t*>(o) = (uint16_t)((q0 & 0xff) | ((q1 & 0xff) << 8));
+        else *o = (uint8_t)q0;
+    } else if constexpr (BITS == 16) {
+        uint8_t* o = out + (j >> 4) * V * 32 + v * 32 + (j & 15);
+        if (two) {
+            *reinterpret_cast<uint16_t*>(o) = (uint16_t)((q0 & 0xff) | ((q1 & 0xff) << 8));
+            *reinterpret_cast<uint16_t*>(o + 16) = (uint16_t)(((q0 >> 8) & 0xff) | (q1 & 0xff00));
+        } else {
+            o[0] = (uint8_t)(q0 & 0xff);
+            o[16] = (uint8_t)((q0 >> 8) & 0xff);
+        }
+    } else {
+        out[(j >> 5) * V * 16 + v * 16 + ((j & 31) >> 1)] = (uint8_t)((q0 & 0xf) | ((q1 & 0xf) << 4));
+    }
+}
+
+// One warp per vector-row.  The maximum comes from the raw halves (one pass
+// of half2 max/min), the sum and the probabilities walk the slots in pairs:
+// lane l takes slots 2l, 2l+1, 2l+64, 2l+65, ... in that order, the order of
+// the fused attention kernel, which reads two slots per load.
+// ROWMAX (8 bits): q = round(127 exp(x - max)) needs no sum, so the sum and
+// the probabilities come from one pass, and lane 0 writes the row divisors
+// 127 * sum * scale -- the separate-launch form of the fused kernel's row-max
+// mode (same expressions, same summation order).
 template <int V, int BITS, bool ROWMAX = false>
 __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams p)
 {
@@ -106,19 +180,54 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
     uint8_t* out = p.out + (long long)b * p.out_stride + (long long)start * V * BITS / 8;
 
     float mx[V], sum[V], x[V];
-#pragma unroll
-    for (int v = 0; v < V; ++v) { mx[v] = -FLT_MAX; sum[v] = 0.f; }
-    for (int j = lane; j < nnz; j += 32) {
-        load_vec<V>(sc + (long long)j * V, x, p.scaling);
-#pragma unroll
-        for (int v = 0; v < V; ++v) mx[v] = fmaxf(mx[v], x[v]);
+    {
+        HalfRange<V> range;
+        for (int j = lane; j < nnz; j += 32) range.add(sc + (long long)j * V);
+        range.scaled_max(p.scaling, mx);
     }
 #pragma unroll
-    for (int v = 0; v < V; ++v)
+    for (int v = 0; v < V; ++v) {
+        sum[v] = 0.f;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) mx[v] = fmaxf(mx[v], __shfl_xor_sync(0xffffffffu, mx[v], o));
-    // Lane l sums slots 2l, 2l+1, 2l+64, 2l+65, ... in that order (the order
-    // of the fused attention kernel, which reads two slots per load).
+    }
+
+    if constexpr (ROWMAX) {
+        for (int j = 2 * lane; j < nnz; j += 64) {
+            const bool two = j + 1 < nnz;
+            int q0[V], q1[V];
+            load_vec<V>(sc + (long long)j * V, x, p.scaling);
+#pragma unroll
+            for (int v = 0; v < V; ++v) {
+                const float e = __expf(x[v] - mx[v]);
+                sum[v] += e;
+                q0[v] = __float2int_rn(127.f * e);
+                q1[v] = 0;
+            }
+            if (two) {
+                load_vec<V>(sc + (long long)(j + 1) * V, x, p.scaling);
+#pragma unroll
+                for (int v = 0; v < V; ++v) {
+                    const float e = __expf(x[v] - mx[v]);
+                    sum[v] += e;
+                    q1[v] = __float2int_rn(127.f * e);
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < V; ++v) store_pair<V, 8>(out, j, v, q0[v], q1[v], two);
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
+        if (lane == 0) {
+            float* dv = p.row_div + (long long)b * p.row_div_stride + (long long)row * V;
+#pragma unroll
+            for (int v = 0; v < V; ++v) dv[v] = 127.f * sum[v] * p.scale;
+        }
+        return;
+    }
+
     for (int j = 2 * lane; j < nnz; j += 64) {
         load_vec<V>(sc + (long long)j * V, x, p.scaling);
 #pragma unroll
@@ -134,65 +243,28 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
     for (int v = 0; v < V; ++v) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
-        rs[v] = ROWMAX ? 0.f : __fdiv_rn(p.scale, sum[v]);
+        rs[v] = __fdiv_rn(p.scale, sum[v]);
     }
-    if constexpr (ROWMAX) {
-        if (lane == 0) {
-            float* dv = p.row_div + (long long)b * p.row_div_stride + (long long)row * V;
+    for (int j = 2 * lane; j < nnz; j += 64) {
+        const bool two = j + 1 < nnz;
+        int q0[V], q1[V];
+        load_vec<V>(sc + (long long)j * V, x, p.scaling);
 #pragma unroll
-            for (int v = 0; v < V; ++v) dv[v] = 127.f * sum[v] * p.scale;
+        for (int v = 0; v < V; ++v) {
+            const float f = fminf(fmaxf(__expf(x[v] - mx[v]) * rs[v], LO), HI);
+            q0[v] = (int)f;
+            q1[v] = 0;
         }
-    }
-
-    // Every lane of the warp runs the same number of iterations (the loop
-    // bound is rounded up to the warp) so the 4-bit pairing shuffle is safe.
-    const int nround = (nnz + 31) & ~31;
-    for (int j = lane; j < nround; j += 32) {
-        int q[V];
-        const bool in = j < nnz;
-        if (in) {
-            load_vec<V>(sc + (long long)j * V, x, p.scaling);
+        if (two) {
+            load_vec<V>(sc + (long long)(j + 1) * V, x, p.scaling);
 #pragma unroll
             for (int v = 0; v < V; ++v) {
-                if constexpr (ROWMAX) {
-                    q[v] = __float2int_rn(127.f * __expf(x[v] - mx[v]));
-                } else {
-                    float f = __expf(x[v] - mx[v]) * rs[v];
-                    f = fminf(fmaxf(f, LO), HI);
-                    q[v] = (int)f;
-                }
-            }
-        } else {
-#pragma unroll
-            for (int v = 0; v < V; ++v) q[v] = 0;
-        }
-        if constexpr (BITS == 8) {
-            if (in) {
-                uint8_t* o = out + (j >> 4) * V * 16 + (j & 15);
-#pragma unroll
-                for (int v = 0; v < V; ++v) o[v * 16] = (uint8_t)q[v];
-            }
-        } else if constexpr (BITS == 16) {
-            if (in) {
-                uint8_t* o = out + (j >> 4) * V * 32 + (j & 15);
-#pragma unroll
-                for (int v = 0; v < V; ++v) {
-                    o[v * 32] = (uint8_t)(q[v] & 0xff);
-                    o[v * 32 + 16] = (uint8_t)((q[v] >> 8) & 0xff);
-                }
-            }
-        } else {
-            // nonzeros j (even lane) and j+1 (odd lane) share a byte: low, high nibble
-#pragma unroll
-            for (int v = 0; v < V; ++v) {
-                const int hi = __shfl_down_sync(0xffffffffu, q[v], 1);
-                if (in && !(j & 1)) {
-                    uint8_t* o = out + (j >> 5) * V * 16 + v * 16 + ((j & 31) >> 1);
-                    const int hv = (j + 1 < nnz) ? hi : 0;
-                    *o = (uint8_t)((q[v] & 0xf) | ((hv & 0xf) << 4));
-                }
+                const float f = fminf(fmaxf(__expf(x[v] - mx[v]) * rs[v], LO), HI);
+                q1[v] = (int)f;
             }
         }
+#pragma unroll
+        for (int v = 0; v < V; ++v) store_pair<V, BITS>(out, j, v, q0[v], q1[v], two);
     }
 }
 
@@ -230,6 +302,8 @@ extern "C" int mcQuantSoftmax(const mcSoftmaxDesc* d, cudaStream_t stream)
     if (!d->row_indices || !d->row_offsets || !d->scores || !d->out) return mc::fail(1, "mcQuantSoftmax: null pointer");
     if (reinterpret_cast<uintptr_t>(d->scores) % 16 || d->scores_stride % 8)
         return mc::fail(1, "mcQuantSoftmax: scores must be 16-byte aligned, stride a multiple of 8 halves");
+    if (reinterpret_cast<uintptr_t>(d->out) % 2 || d->out_stride % 2)  // slot pairs are stored as 16-bit words
+        return mc::fail(1, "mcQuantSoftmax: out must be 2-byte aligned, stride a multiple of 2 bytes");
     if (d->requant != MC_REQUANT_FIXED && d->requant != MC_REQUANT_ROWMAX)
         return mc::fail(1, "mcQuantSoftmax: requant must be MC_REQUANT_FIXED or MC_REQUANT_ROWMAX");
     if (d->requant == MC_REQUANT_ROWMAX &&

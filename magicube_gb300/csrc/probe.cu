@@ -114,7 +114,11 @@ __global__ void __launch_bounds__(256) tensor_peak_kernel(int* out, int iters, u
                 asm volatile("mma.sync.aligned.m16n8k64.row.col.s32.s4.s4.s32 {%0,%1,%2,%3},{%4,%5,%6,%7},{%8,%9},{%0,%1,%2,%3};"
                              : "+r"(c[q][0]), "+r"(c[q][1]), "+r"(c[q][2]), "+r"(c[q][3])
                              : "r"(a), "r"(b), "r"(a), "r"(b), "r"(a), "r"(b));
-            else if constexpr (KIND == 3)
+            else if constexpr (KIND == 4) {  // CUDA-core dp4a: four independent chains per slot
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    asm volatile("dp4a.s32.s32 %0, %1, %2, %0;" : "+r"(c[q][e]) : "r"(a), "r"(b));
+            } else if constexpr (KIND == 3)
                 asm volatile("mma.sync.aligned.m16n8k16.row.col.s32.s8.s8.s32 {%0,%1,%2,%3},{%4,%5},{%6},{%0,%1,%2,%3};"
                              : "+r"(c[q][0]), "+r"(c[q][1]), "+r"(c[q][2]), "+r"(c[q][3])
                              : "r"(a), "r"(b), "r"(a));
@@ -136,7 +140,7 @@ extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int
                                  double* ops_out, cudaStream_t stream)
 {
     mc::clear_error();
-    if (kind < 0 || kind > 3 || !ms_out || !ops_out || iters <= 0) return mc::fail(1, "mcProbeTensorPeak: bad arguments");
+    if (kind < 0 || kind > 4 || !ms_out || !ops_out || iters <= 0) return mc::fail(1, "mcProbeTensorPeak: bad arguments");
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -151,7 +155,8 @@ extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int
         if (kind == 0) mc::tensor_peak_kernel<0><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
         else if (kind == 1) mc::tensor_peak_kernel<1><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
         else if (kind == 2) mc::tensor_peak_kernel<2><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
-        else mc::tensor_peak_kernel<3><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
+        else if (kind == 3) mc::tensor_peak_kernel<3><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
+        else mc::tensor_peak_kernel<4><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
     };
     launch();  // warm-up
     cudaEventRecord(e0, stream);
@@ -161,7 +166,11 @@ extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int
     cudaEventElapsedTime(ms_out, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const double macs = kind == 0 ? 16.0 * 8 * 32 : (kind == 1 ? 16.0 * 8 * 64 : 16.0 * 8 * 16);  // kinds 2, 3: k = 16
+    // MACs per warp per slot q: an MMA's m x n x k; kind 4: 4 dp4a x 32 lanes x 4
+    const double macs = kind == 0   ? 16.0 * 8 * 32
+                        : kind == 1 ? 16.0 * 8 * 64
+                        : kind == 4 ? 4.0 * 32 * 4
+                                    : 16.0 * 8 * 16;  // kinds 2, 3: k = 16
     *ops_out = 2.0 * macs * (double)blocks * (threads / 32) * iters * 8;
     return (int)cudaGetLastError();
 }

@@ -93,6 +93,76 @@ def test_q_bcsr_softmax(cuda, bits, scale, V):
         np.testing.assert_array_equal(g[safe], r[safe])
 
 
+def _ragged_rows(lengths, align=32):
+    """Row offsets (start, end) with starts on `align` slots, rows in reverse
+    order through row_indices, and the aligned slot count."""
+    pairs, start = [], 0
+    for n in lengths:
+        pairs += [start, start + n]
+        start += -(-n // align) * align
+    ri = np.arange(len(lengths), dtype=np.int32)[::-1].copy()
+    return np.asarray(pairs, dtype=np.int32), ri, max(start, align)
+
+
+@pytest.mark.parametrize("bits,scale", [(8, 127.0), (16, 32767.0), (4, 7.0)])
+@pytest.mark.parametrize("V", [2, 4, 8])
+@pytest.mark.parametrize("scaling", [0.125, -0.0625])
+def test_softmax_short_and_empty_rows(cuda, bits, scale, V, scaling):
+    """Rows shorter than a warp (lanes with no slot), empty rows, odd lengths
+    and a negative scaling: within 1 of the oracle, equal away from rounding
+    boundaries, padding slots untouched."""
+    lengths = [0, 1, 2, 3, 7, 16, 31, 32, 33, 45, 63, 64, 65, 0, 97, 5]
+    hp, hr, n = _ragged_rows(lengths)
+    B = 2
+    rng = np.random.default_rng(21)
+    scores = (rng.standard_normal((B, n * V)) * 20).astype(np.float16)
+    got = q_softmax.q_bcsr_softmax(torch.from_numpy(hr).to(cuda), torch.from_numpy(hp).to(cuda),
+                                   torch.from_numpy(scores).to(cuda), scaling, scale, V, B, bits)
+    got = got.cpu().numpy().view(np.uint8)
+    for b in range(B):
+        ref, exact = oatt.softmax_quant(scores[b], hp, hr, V, bits, scaling, scale, got.shape[1])
+        g, r = _decode_softmax(got[b], hp, V, bits, n), _decode_softmax(ref, hp, V, bits, n)
+        assert np.abs(g - r).max() <= 1
+        frac = np.abs(exact.reshape(n, V) - np.round(exact.reshape(n, V)))
+        safe = frac > 1e-3
+        np.testing.assert_array_equal(g[safe], r[safe])
+        valid = np.zeros(n, bool)
+        for i in range(len(lengths)):
+            valid[hp[2 * i]:hp[2 * i + 1]] = True
+        assert (g[~valid] == 0).all()
+
+
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_softmax_rowmax_short_rows(cuda, V):
+    """Row-max requantization on rows shorter than a warp and empty rows:
+    probabilities within 1 of the oracle, divisors of non-empty rows within
+    1e-5 relative."""
+    import ctypes
+    from magicube_gb300 import _lib
+    lengths = [0, 1, 2, 3, 7, 16, 31, 32, 33, 45, 63, 64, 65, 0, 97, 5]
+    hp, hr, n = _ragged_rows(lengths)
+    B, m_vec, scale = 2, len(lengths), 44.0
+    rng = np.random.default_rng(23)
+    scores = (rng.standard_normal((B, n * V)) * 3).astype(np.float16)
+    out = torch.zeros((B, n * V), dtype=torch.uint8, device=cuda)
+    div = torch.full((B, m_vec * V), -1.0, dtype=torch.float32, device=cuda)
+    sc, dri, dro = (torch.from_numpy(a).to(cuda) for a in (scores, hr, hp))
+    d = _lib.McSoftmaxDesc(m_vec=m_vec, vec_length=V, batch=B, bits=8, scaling=1.0, scale=scale,
+                           row_indices=dri.data_ptr(), row_offsets=dro.data_ptr(), scores=sc.data_ptr(),
+                           scores_stride=n * V, out=out.data_ptr(), out_stride=n * V, requant=_lib.REQUANT_ROWMAX,
+                           row_div=div.data_ptr(), row_div_stride=m_vec * V)
+    _lib.check(_lib.lib().mcQuantSoftmax(ctypes.byref(d), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               "mcQuantSoftmax")
+    got, gdiv = out.cpu().numpy(), div.cpu().numpy()
+    nonempty = np.repeat(np.asarray(lengths) > 0, V)
+    for b in range(B):
+        ref, rdiv, exact = oatt.softmax_rowmax(scores[b], hp, hr, V, 1.0, scale, n * V, m_vec)
+        g = _decode_softmax(got[b], hp, V, 8, n)
+        r = _decode_softmax(ref, hp, V, 8, n)
+        assert np.abs(g - r).max() <= 1
+        np.testing.assert_allclose(gdiv[b][nonempty], rdiv[nonempty], rtol=1e-5)
+
+
 @pytest.mark.parametrize("V", [2, 4, 8])
 def test_softmax_rowmax_and_row_divisors(cuda, V):
     """mcQuantSoftmax with MC_REQUANT_ROWMAX against the oracle: every

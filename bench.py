@@ -30,7 +30,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-MMA_NAMES = {1: "int8mma", 2: "f16mma", 3: "tcgen05"}
+MMA_NAMES = {1: "int8mma", 2: "f16mma", 3: "tcgen05", 4: "dp4a"}
 METRIC = "quantized SpMM/SDDMM TOP/s vs roofline; sparse-attn req/s + p50/p99 latency"
 UNIT = "TOP/s"
 SEQ, HEAD_DIM, VEC, SPARSITY = 4096, 64, 8, 0.9
@@ -99,9 +99,9 @@ class ClockSampler:
 # workload construction
 # ----------------------------------------------------------------------------
 
-def sddmm_workload(pa: int, pb: int, batch: int, seed: int = 42):
+def sddmm_workload(pa: int, pb: int, batch: int, seed: int = 42, V: int = VEC, sparsity: float = SPARSITY):
     from magicube_gb300 import formats, synth
-    mask = synth.uniform_mask(SEQ // VEC, SEQ, VEC, SPARSITY, seed=seed)
+    mask = synth.uniform_mask(SEQ // V, SEQ, V, sparsity, seed=seed)
     hm = formats.prepare_sddmm(mask, alignment=8)
     rng = np.random.default_rng(seed + 1)
     lhs = rng.integers(0, 256, size=(batch, SEQ * HEAD_DIM * pa // 8), dtype=np.uint8)
@@ -122,12 +122,12 @@ def measured_traffic_per_instance() -> float | None:
     return None
 
 
-def sddmm_bytes(hm, pa: int, pb: int, batch: int) -> tuple[float, float]:
+def sddmm_bytes(hm, pa: int, pb: int, batch: int, V: int = VEC) -> tuple[float, float]:
     """(algorithmic bytes per launch, ops per launch) of a batched SDDMM."""
     nnz = hm.mask.nnz_vec
-    per_inst = SEQ * HEAD_DIM * pa / 8 + SEQ * HEAD_DIM * pb / 8 + hm.aligned_nnz * VEC * 4
+    per_inst = SEQ * HEAD_DIM * pa / 8 + SEQ * HEAD_DIM * pb / 8 + hm.aligned_nnz * V * 4
     mask_bytes = hm.aligned_nnz * 4 + hm.mask.m_vec * 2 * 4 + hm.mask.m_vec * 4
-    ops = 2.0 * nnz * VEC * HEAD_DIM * batch
+    ops = 2.0 * nnz * V * HEAD_DIM * batch
     return per_inst * batch + mask_bytes, ops
 
 
@@ -248,12 +248,12 @@ def run_gpu(args) -> None:
     results = {}
     launches_per_step = 1
 
-    def sddmm_case(pa, pb, timed_region_clock=False, mma=args.mma, variant=0):
-        mask, hm, lhs_h, rhs_h = sddmm_workload(pa, pb, B)
+    def sddmm_case(pa, pb, timed_region_clock=False, mma=args.mma, variant=0, V=VEC, sparsity=SPARSITY):
+        mask, hm, lhs_h, rhs_h = sddmm_workload(pa, pb, B, V=V, sparsity=sparsity)
         dm = ops.DeviceSddmmMask.from_host(hm, dev)
         lhs = torch.from_numpy(lhs_h).to(dev)
         rhs = torch.from_numpy(rhs_h).to(dev)
-        out = torch.empty((B, hm.aligned_nnz * VEC), dtype=torch.int32, device=dev)
+        out = torch.empty((B, hm.aligned_nnz * V), dtype=torch.int32, device=dev)
         fn = lambda: ops.sddmm(dm, lhs, rhs, HEAD_DIM, pa, pb, signed=True, out=out, batch=B, mma_kind=mma,
                                     variant=variant)
         sync_all()
@@ -264,7 +264,7 @@ def run_gpu(args) -> None:
         else:
             ms, clocks = time_cuda(fn, args.steps, args.warmup, stream), None
         sync_all()
-        byts, opc = sddmm_bytes(hm, pa, pb, B)
+        byts, opc = sddmm_bytes(hm, pa, pb, B, V)
         t = max_over_ranks(sum(ms) / 1e3)
         avg = t / args.steps
         return {"tops": opc * world * args.steps / t / 1e12, "ms": avg * 1e3, "gbs": byts / avg / 1e9,
@@ -301,13 +301,23 @@ def run_gpu(args) -> None:
     if not args.headline_only:
         # the other tensor paths of the headline SDDMM; the other precision
         # pairs and the SpMM run on mma.sync (int8 unless --mma f16)
-        others = [m for m in (1, 2, 3) if m != args.mma]
+        others = [m for m in (1, 2, 3, 4) if m != args.mma]
         sync_mma = 2 if args.mma == 2 else 1
-        cases = [(4, 4, "sddmm_L4R4", sync_mma, 0), (16, 8, "sddmm_L16R8", sync_mma, 0)]
-        cases += [(8, 8, f"sddmm_L8R8_{MMA_NAMES[m]}", m, 0) for m in others]
-        cases += [(8, 8, "sddmm_L8R8_per_row_kernel", sync_mma, 1)]
-        for pa, pb, name, mma, var in cases:
-            r = sddmm_case(pa, pb, mma=mma, variant=var)
+        cases = [(4, 4, "sddmm_L4R4", sync_mma, 0, VEC), (16, 8, "sddmm_L16R8", sync_mma, 0, VEC)]
+        cases += [(8, 8, f"sddmm_L8R8_{MMA_NAMES[m]}", m, 0, VEC) for m in others]
+        cases += [(8, 8, "sddmm_L8R8_per_row_kernel", sync_mma, 1, VEC)]
+        # V = 2 and 4: the int8 MMA computes 8 lanes of which V are used; dp4a
+        # computes only the V lanes
+        cases += [(8, 8, f"sddmm_L8R8_V{v}_{MMA_NAMES[m]}", m, 0, v) for v in (2, 4) for m in (1, 4)]
+        cases += [(4, 4, f"sddmm_L4R4_V{v}_{MMA_NAMES[m]}", m, 0, v) for v in (2, 4) for m in (1, 4)]
+        cases += [(4, 4, "sddmm_L4R4_dp4a", 4, 0, VEC)]
+        cases = [c + (SPARSITY,) for c in cases]
+        # every score of 128 x 256 tiles on the tcgen05 f16 tensor cores with a
+        # masked epilogue, against the per-nonzero int8 kernel across sparsity
+        for sp in (0.5, 0.7, 0.9):
+            cases += [(8, 8, f"sddmm_L8R8_s{sp}_{tag}", 1, var, VEC, sp) for var, tag in ((0, "k64"), (4, "dense_tile"))]
+        for pa, pb, name, mma, var, v, sp in cases:
+            r = sddmm_case(pa, pb, mma=mma, variant=var, V=v, sparsity=sp)
             variants[name] = {"tops": r["tops"], "ms": r["ms"], "gbs": r["gbs"],
                               "hbm_frac": r["gbs"] / peaks["hbm_gbs"]}
             del r
@@ -726,7 +736,7 @@ def tensor_peaks(dev) -> dict:
                        dtype=torch.uint8, device=dev)
     out = {}
     for kind, name in ((0, "int8_mma_sync"), (1, "int4_mma_sync"), (2, "f16_mma_sync"), (3, "int8_k16_mma_sync"),
-                       (4, "int8_dp4a")):
+                       (4, "int8_dp4a"), (5, "int8_mma_plus_dp4a")):
         ms, ops = ctypes.c_float(), ctypes.c_double()
         _lib.check(_lib.lib().mcProbeTensorPeak(kind, sink.data_ptr(), sink.numel(), 2048, ctypes.byref(ms),
                                                 ctypes.byref(ops), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
@@ -903,7 +913,8 @@ def run_profile_case(args) -> None:
         lhs, rhs = torch.from_numpy(lhs_h).to(dev), torch.from_numpy(rhs_h).to(dev)
         out = torch.empty((args.batch, hm.aligned_nnz * VEC), dtype=torch.int32, device=dev)
         for _ in range(args.reps):
-            ops.sddmm(dm, lhs, rhs, HEAD_DIM, 8, 8, signed=True, out=out, batch=args.batch, mma_kind=args.mma)
+            ops.sddmm(dm, lhs, rhs, HEAD_DIM, 8, 8, signed=True, out=out, batch=args.batch, mma_kind=args.mma,
+                      variant=args.sddmm_kernel)
     else:
         M = K = 1024
         N = 256
@@ -941,9 +952,11 @@ def main() -> None:
     ap.add_argument("--serving-requests", type=int, default=96, help="requests per serving run (0 skips it)")
     ap.add_argument("--serving-overlap-tokens", type=int, default=8192,
                     help="queued tokens at which the server overlaps a new batch with running ones")
-    ap.add_argument("--mma", choices=["int8", "f16", "tc"], default="int8",
-                    help="tensor path of the headline SDDMM: int8 / f16 mma.sync or tcgen05 (all bit-exact; "
-                         "see include/magicube_gb300.h)")
+    ap.add_argument("--mma", choices=["int8", "f16", "tc", "dp4a"], default="int8",
+                    help="arithmetic path of the headline SDDMM: int8 / f16 mma.sync, tcgen05 or CUDA-core dp4a "
+                         "(all bit-exact; see include/magicube_gb300.h)")
+    ap.add_argument("--sddmm-kernel", choices=["auto", "per_row", "stream", "dense"], default="auto",
+                    help="SDDMM kernel variant of the --profile sddmm case")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", choices=["square", "full"], default=None,
                     help="run only the SpMM precision/shape sweep (M = K, or every M, K pair)")
@@ -951,7 +964,8 @@ def main() -> None:
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    args.mma = {"int8": 1, "f16": 2, "tc": 3}[args.mma]
+    args.mma = {"int8": 1, "f16": 2, "tc": 3, "dp4a": 4}[args.mma]
+    args.sddmm_kernel = {"auto": 0, "per_row": 1, "stream": 2, "dense": 4}[args.sddmm_kernel]
     if args.sweep:
         run_sweep(args)
     elif args.profile:

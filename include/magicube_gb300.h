@@ -92,7 +92,10 @@ int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* row_indices, const int* 
  *              to f16 in shared memory, tcgen05.mma kind::f16 (M = 128
  *              nonzeros, N = 16, K = 64) with the f32 accumulator in TMEM;
  *              exact because 64 products of 8-bit integers stay below 2^24. */
-enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2, MC_MMA_TCGEN05 = 3 };
+/* MC_MMA_DP4A (SDDMM with 8-bit or 4-bit operands): no tensor core; each
+ *              vector lane is a chain of CUDA-core dp4a, so V = 2 and V = 4
+ *              compute no padding lanes (an int8 MMA always computes 8). */
+enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2, MC_MMA_TCGEN05 = 3, MC_MMA_DP4A = 4 };
 /* Number of bounded mbarrier waits that ran out in the tcgen05 SDDMM and the
  * TMA SpMM (0 unless the device stalled; an affected launch's results are
  * incomplete).  Synchronous. */
@@ -114,10 +117,20 @@ int mcSetDefaultMmaKind(int kind);
  *                    with n % 256 == 0, 16-byte aligned values,
  *                    values_stride and rhs, rhs_stride a multiple of the B
  *                    row bytes).
+ * MC_KERNEL_DENSE_TILE: SDDMM only, 8-bit operands with k == 64: every score
+ *                    of 128-column x 256-row tiles on the tcgen05 f16 tensor
+ *                    cores (exact: 64 products of int8 values sum below 2^24),
+ *                    accumulators in TMEM, and an epilogue that stores the
+ *                    masked ones, located through the mask's tile bitmap
+ *                    (mcSddmmTileMask; needs strictly increasing columns per
+ *                    vector-row).  Computes every vector-row (row_indices is
+ *                    not read).  Wins where the mask is dense enough that a
+ *                    dense tile costs less than per-nonzero gathers (about
+ *                    sparsity <= 0.95 on GB300).
  * MC_KERNEL_AUTO:    SpMM: the TMA kernel where it applies, else the
  *                    streaming kernel, else per-row; SDDMM: the pipelined
  *                    kernel where it applies, else per-row. */
-enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2, MC_KERNEL_TMA = 3 };
+enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2, MC_KERNEL_TMA = 3, MC_KERNEL_DENSE_TILE = 4 };
 
 /* ---- Value layouts of the SpMM sparse operand --------------------------------
  * MC_VALUES_PACKED:  the reference host packer's layout (what
@@ -180,9 +193,23 @@ typedef struct mcSddmmDesc {
     const void* rhs;      long long rhs_stride;     /* bytes */
     void* out;            long long out_stride;     /* elements */
     int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
-    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM */
+    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM / _DENSE_TILE */
+    /* MC_KERNEL_DENSE_TILE only: the mask's tile bitmap and first-slot table
+     * (mcSddmmTileMask), m_vec x mcSddmmTileMaskWords(n) entries each. */
+    const unsigned* tile_bitmap;
+    const int* tile_prefix;
 } mcSddmmDesc;
 int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream);
+/* Tile bitmap of an SDDMM mask for MC_KERNEL_DENSE_TILE: per vector-row,
+ * bitmap word w has bit c set if column 32w + c is stored, and prefix[w] is
+ * the number of the row's stored columns below 32w.  bitmap and prefix hold
+ * m_vec x mcSddmmTileMaskWords(n) entries (device memory, caller-owned).
+ * *status (device int) is set to 0, or to 1 if some vector-row's columns are
+ * not strictly increasing within [0, n) (the dense-tile kernel must not be
+ * used with that mask).  Asynchronous on `stream`. */
+int mcSddmmTileMaskWords(int n);
+int mcSddmmTileMask(int m_vec, int n, const int* row_offsets, const int* column_indices, unsigned* bitmap,
+                    int* prefix, int* status, cudaStream_t stream);
 
 /* ---- Quantized attention steps ----------------------------------------------
  * mcQuantize: out = packed trunc(clamp(float(in) * scale)) for `count` half
@@ -219,7 +246,8 @@ int mcQuantSoftmax(const mcSoftmaxDesc* desc, cudaStream_t stream);
  * mcProbeTensorPeak: times one full-grid launch of back-to-back independent
  * mma.sync of `kind` (0: m16n8k32 s8, 1: m16n8k64 s4, 2: m16n8k16 f16 with f32
  * accumulators, 3: m16n8k16 s8; 4: the CUDA-core dp4a.s32.s32, four MACs per
- * thread instruction) and returns its duration and operation count (2 per MAC), the
+ * thread instruction; 5: one m16n8k32 s8 and 32 dp4a per step, which shows
+ * whether the two overlap) and returns its duration and operation count (2 per MAC), the
  * measured tensor peak its kernels are compared with.  sink: device buffer of
  * at least 4 bytes x 256 threads x 8 CTAs x SMs that receives each thread's
  * (meaningless) accumulator sum, so the MMAs are not optimised away. */

@@ -39,6 +39,7 @@ class McSddmmDesc(ctypes.Structure):
         ("rhs", _c_vp), ("rhs_stride", _c_ll),
         ("out", _c_vp), ("out_stride", _c_ll),
         ("mma_kind", _c_int), ("kernel_variant", _c_int),
+        ("tile_bitmap", _c_vp), ("tile_prefix", _c_vp),
     ]
 
 
@@ -83,8 +84,8 @@ class McDevicePackDesc(ctypes.Structure):
 
 
 REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
-MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05 = 0, 1, 2, 3
-KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA = 0, 1, 2, 3
+MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05, MMA_DP4A = 0, 1, 2, 3, 4
+KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA, KERNEL_DENSE_TILE = 0, 1, 2, 3, 4
 VALUES_PACKED, VALUES_SOFTMAX = 0, 1
 
 # name -> (restype, argtypes)
@@ -96,6 +97,8 @@ _SIGNATURES = {
     "mcTensorCoreTimeouts": (ctypes.c_uint, []),
     "mcSpmm": (_c_int, [ctypes.POINTER(McSpmmDesc), _c_vp]),
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
+    "mcSddmmTileMaskWords": (_c_int, [_c_int]),
+    "mcSddmmTileMask": (_c_int, [_c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "mcQuantize": (_c_int, [_c_vp, _c_vp, _c_ll, _c_int, _c_float, _c_vp]),
     "mcQuantSoftmax": (_c_int, [ctypes.POINTER(McSoftmaxDesc), _c_vp]),
     "mcSparseAttention": (_c_int, [ctypes.POINTER(McAttnDesc), _c_vp]),

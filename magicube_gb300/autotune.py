@@ -70,9 +70,11 @@ def spmm_candidates() -> list[dict]:
     return out + [{"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_TMA}]
 
 
-def sddmm_candidates(k: int) -> list[dict]:
+def sddmm_candidates(k: int, bits: int = 8) -> list[dict]:
+    """Tensor path x kernel variant x row split; the dp4a path joins for 8-bit
+    and 4-bit operands."""
     out = []
-    for m in (_lib.MMA_INT8, _lib.MMA_F16):
+    for m in (_lib.MMA_INT8, _lib.MMA_F16) + ((_lib.MMA_DP4A,) if bits <= 8 else ()):
         for split in (0, 1, 2, 4):
             out.append({"mma_kind": m, "variant": _lib.KERNEL_PER_ROW, "row_split": split})
             if k == 64:

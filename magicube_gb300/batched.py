@@ -173,7 +173,7 @@ class _AttentionCore:
         avg = m.aligned_nnz / max(1, m.m_vec)
         self._quantize(qkv, stream)
         sig = autotune.signature("sddmm_attn", self.rb, self.rb, m.vec_length, self.d, m.m_vec, avg, self.H)
-        self.sddmm_cfg = autotune.tune(sig, autotune.sddmm_candidates(self.d), lambda c: self._sddmm(c, stream))
+        self.sddmm_cfg = autotune.tune(sig, autotune.sddmm_candidates(self.d, self.rb), lambda c: self._sddmm(c, stream))
         self._sddmm(self.sddmm_cfg, stream)
         self._softmax(stream)
         sig = autotune.signature("spmm_attn", self.lb, self.rb, m.vec_length, self.d, m.m_vec, avg, self.H)

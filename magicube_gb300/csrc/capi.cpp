@@ -85,11 +85,20 @@ static int check_sddmm(const mcSddmmDesc& d)
     if (d.out_half && (!d.is_signed || !d.out_vecmajor))
         return fail(1, "mcSddmm: half output requires is_signed = 1 and out_vecmajor = 1");
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSddmm: half output requires a nonzero scale");
-    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_TCGEN05) return fail(1, "mcSddmm: invalid mma_kind");
+    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_DP4A) return fail(1, "mcSddmm: invalid mma_kind");
+    if (d.mma_kind == MC_MMA_DP4A && (d.lhs_bits > 8 || d.rhs_bits > 8))
+        return fail(1, "mcSddmm: the dp4a path computes 8-bit and 4-bit operands");
     if (d.mma_kind == MC_MMA_TCGEN05 && (d.lhs_bits != 8 || d.rhs_bits != 8 || d.k != 64))
         return fail(1, "mcSddmm: the tcgen05 path computes L8-R8 with k == 64");
-    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_STREAM)
+    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_DENSE_TILE ||
+        d.kernel_variant == MC_KERNEL_TMA)
         return fail(1, "mcSddmm: invalid kernel_variant");
+    if (d.kernel_variant == MC_KERNEL_DENSE_TILE) {
+        if (d.lhs_bits != 8 || d.rhs_bits != 8 || d.k != 64)
+            return fail(1, "mcSddmm: the dense-tile kernel computes L8-R8 with k == 64");
+        if (d.m_vec > 0 && (!d.tile_bitmap || !d.tile_prefix || !aligned(d.tile_bitmap, 4) || !aligned(d.tile_prefix, 4)))
+            return fail(1, "mcSddmm: the dense-tile kernel needs the mask's tile bitmap and prefix (mcSddmmTileMask)");
+    }
     if (d.m_vec == 0) return 0;
     if (!d.row_indices || !d.row_offsets || !d.column_indices || !d.lhs || !d.rhs || !d.out)
         return fail(1, "mcSddmm: null pointer");
@@ -143,6 +152,7 @@ int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream)
     const mcSddmmDesc& d = *desc;
     if (int rc = mc::check_sddmm(d)) return rc;
     if (d.m_vec == 0) return 0;
+    if (d.kernel_variant == MC_KERNEL_DENSE_TILE) return mc::sddmm_dense_launch(d, stream);
     if (d.lhs_bits == 4) return mc::sddmm_launch_4_4(d, stream);
     if (d.lhs_bits == 8) return mc::sddmm_launch_8_8(d, stream);
     if (d.rhs_bits == 8) return mc::sddmm_launch_16_8(d, stream);

@@ -40,5 +40,6 @@ int sddmm_launch_4_4(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_launch_8_8(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_launch_16_8(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_launch_16_16(const mcSddmmDesc& d, cudaStream_t s);
+int sddmm_dense_launch(const mcSddmmDesc& d, cudaStream_t s);
 
 }  // namespace mc

@@ -4,6 +4,7 @@
 #pragma once
 #include "mc_host.h"
 #include "mc_sddmm.cuh"
+#include "mc_sddmm_dp4a.cuh"
 #include "mc_sddmm_stream.cuh"
 #include "mc_spmm.cuh"
 #include "mc_spmm_stream.cuh"
@@ -198,6 +199,19 @@ int sddmm_launch_k64(const mcSddmmDesc& d, const SddmmParams& p, int split, cuda
     return (int)cudaGetLastError();
 }
 
+template <int V, int PA, int PB, bool S, bool VM, bool H>
+int sddmm_launch_dp4a(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaStream_t s)
+{
+    if constexpr (PA == 16 || PB == 16) {
+        return fail(1, "mcSddmm: the dp4a path computes 8-bit and 4-bit operands");
+    } else {
+        dim3 grid((unsigned)d.m_vec, (unsigned)split, (unsigned)d.batch);
+        if (d.k == 64) sddmm_dp4a_kernel<V, PA, PB, S, VM, H, 4, true><<<grid, 128, 0, s>>>(p);
+        else sddmm_dp4a_kernel<V, PA, PB, S, VM, H, 4, false><<<grid, 128, 0, s>>>(p);
+        return (int)cudaGetLastError();
+    }
+}
+
 // The tcgen05 SDDMM (sddmm_tc.cu).
 int sddmm_tc_launch(const mcSddmmDesc& d, const SddmmParams& p, cudaStream_t s);
 
@@ -205,6 +219,7 @@ template <int V, int PA, int PB, bool S, bool VM, bool H>
 int sddmm_launch_v(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaStream_t s)
 {
     if (resolve_mma_kind(d.mma_kind) == MC_MMA_TCGEN05) return sddmm_tc_launch(d, p, s);
+    if (resolve_mma_kind(d.mma_kind) == MC_MMA_DP4A) return sddmm_launch_dp4a<V, PA, PB, S, VM, H>(d, p, split, s);
     const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
     if (d.kernel_variant == MC_KERNEL_STREAM && d.k != 64)
         return fail(1, "mcSddmm: the streaming kernel needs k == 64");

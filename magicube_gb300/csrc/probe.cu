@@ -134,13 +134,39 @@ __global__ void __launch_bounds__(256) tensor_peak_kernel(int* out, int iters, u
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Kind 5: per step one mma.sync m16n8k32 s8 and 32 dp4a (about equal pipe
+// time if the two run on separate units): the combined rate shows whether
+// the int8 MMA and dp4a overlap.
+__global__ void __launch_bounds__(256) mixed_peak_kernel(int* out, int iters, unsigned seed)
+{
+    uint32_t a = seed ^ threadIdx.x, b = seed * 7u + threadIdx.x;
+    int c[8][4] = {};
+    int d[32] = {};
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            asm volatile("mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3},{%4,%5,%6,%7},{%8,%9},{%0,%1,%2,%3};"
+                         : "+r"(c[q][0]), "+r"(c[q][1]), "+r"(c[q][2]), "+r"(c[q][3])
+                         : "r"(a), "r"(b), "r"(a), "r"(b), "r"(a), "r"(b));
+#pragma unroll
+            for (int e = 0; e < 32; ++e) asm volatile("dp4a.s32.s32 %0, %1, %2, %0;" : "+r"(d[e]) : "r"(a), "r"(b));
+        }
+    }
+    int s = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += c[q][0] + c[q][1] + c[q][2] + c[q][3];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) s += d[e];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace mc
 
 extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int iters, float* ms_out,
                                  double* ops_out, cudaStream_t stream)
 {
     mc::clear_error();
-    if (kind < 0 || kind > 4 || !ms_out || !ops_out || iters <= 0) return mc::fail(1, "mcProbeTensorPeak: bad arguments");
+    if (kind < 0 || kind > 5 || !ms_out || !ops_out || iters <= 0) return mc::fail(1, "mcProbeTensorPeak: bad arguments");
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -156,7 +182,8 @@ extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int
         else if (kind == 1) mc::tensor_peak_kernel<1><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
         else if (kind == 2) mc::tensor_peak_kernel<2><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
         else if (kind == 3) mc::tensor_peak_kernel<3><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
-        else mc::tensor_peak_kernel<4><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
+        else if (kind == 4) mc::tensor_peak_kernel<4><<<blocks, threads, 0, stream>>>(out, iters, 1234u);
+        else mc::mixed_peak_kernel<<<blocks, threads, 0, stream>>>(out, iters, 1234u);
     };
     launch();  // warm-up
     cudaEventRecord(e0, stream);
@@ -166,10 +193,12 @@ extern "C" int mcProbeTensorPeak(int kind, void* sink, long long sink_bytes, int
     cudaEventElapsedTime(ms_out, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    // MACs per warp per slot q: an MMA's m x n x k; kind 4: 4 dp4a x 32 lanes x 4
+    // MACs per warp per slot q: an MMA's m x n x k; kind 4: 4 dp4a x 32 lanes
+    // x 4; kind 5: one m16n8k32 and 32 dp4a
     const double macs = kind == 0   ? 16.0 * 8 * 32
                         : kind == 1 ? 16.0 * 8 * 64
                         : kind == 4 ? 4.0 * 32 * 4
+                        : kind == 5 ? 16.0 * 8 * 32 + 32.0 * 32 * 4
                                     : 16.0 * 8 * 16;  // kinds 2, 3: k = 16
     *ops_out = 2.0 * macs * (double)blocks * (threads / 32) * iters * 8;
     return (int)cudaGetLastError();

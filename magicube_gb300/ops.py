@@ -59,11 +59,33 @@ class DeviceSddmmMask:
     row_offsets: torch.Tensor
     col_indices: torch.Tensor
 
+    _tile: tuple | None = None
+
     @classmethod
     def from_host(cls, h: SddmmMask, device="cuda") -> "DeviceSddmmMask":
         cols = h.col_indices if h.col_indices.size else np.full(1, -1, np.int32)
         return cls(h.mask.m_vec, h.mask.vec_length, h.mask.ncols, h.aligned_nnz,
                    _to_dev(h.row_indices, device), _to_dev(h.row_offsets, device), _to_dev(cols, device))
+
+    def tile_mask(self, stream: torch.cuda.Stream | None = None) -> tuple[torch.Tensor, torch.Tensor]:
+        """(bitmap, prefix) of the mask for the dense-tile SDDMM kernel, built
+        on the device once (mcSddmmTileMask) and cached.  Synchronises once to
+        read the status; raises MagicubeError if a vector-row's columns are
+        not strictly increasing."""
+        if self._tile is None:
+            dev = self.row_offsets.device
+            words = _lib.lib().mcSddmmTileMaskWords(self.n)
+            bitmap = torch.empty((max(1, self.m_vec), words), dtype=torch.int32, device=dev)
+            prefix = torch.empty((max(1, self.m_vec), words), dtype=torch.int32, device=dev)
+            status = torch.empty(1, dtype=torch.int32, device=dev)
+            _lib.check(_lib.lib().mcSddmmTileMask(self.m_vec, self.n, self.row_offsets.data_ptr(),
+                                                  self.col_indices.data_ptr(), bitmap.data_ptr(), prefix.data_ptr(),
+                                                  status.data_ptr(), _stream_handle(stream)), "mcSddmmTileMask")
+            if int(status.item()) != 0:
+                raise _lib.MagicubeError("mcSddmmTileMask: the mask's columns are not strictly increasing per "
+                                         "vector-row; the dense-tile SDDMM cannot use it")
+            self._tile = (bitmap, prefix)
+        return self._tile
 
 
 def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, out: torch.Tensor | None = None,
@@ -122,5 +144,8 @@ def sddmm(mask: DeviceSddmmMask, lhs: torch.Tensor, rhs: torch.Tensor, k: int, l
         column_indices=mask.col_indices.data_ptr(), lhs=lhs.data_ptr(), lhs_stride=lhs_stride,
         rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride, mma_kind=mma_kind,
         kernel_variant=variant)
+    if variant == _lib.KERNEL_DENSE_TILE:
+        bitmap, prefix = mask.tile_mask(stream)
+        d.tile_bitmap, d.tile_prefix = bitmap.data_ptr(), prefix.data_ptr()
     _lib.check(_lib.lib().mcSddmm(ctypes.byref(d), _stream_handle(stream)), "mcSddmm")
     return out

@@ -141,3 +141,101 @@ def test_reference_entry_points(cuda, name, bits):
     ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, bits, bits,
                             oracle.UNSIGNED)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+DP4A_PAIRS = [(4, 4), (8, 8)]
+
+
+@pytest.mark.parametrize("pa,pb", DP4A_PAIRS)
+@pytest.mark.parametrize("V", [2, 4, 8])
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("K", [64, 192])
+@pytest.mark.parametrize("vecmajor", [False, True])
+def test_sddmm_dp4a_ragged(cuda, pa, pb, V, signed, K, vecmajor):
+    """The CUDA-core dp4a path: bit-exact against the oracle on ragged rows
+    (empty, shorter than a tile, odd lengths), every V, both layouts."""
+    N = 256
+    mask, lhs, rhs = _case(pa, pb, V, K, N, RAGGED, seed=pa + pb + V + K + 1)
+    hm = formats.prepare_sddmm(mask, alignment=16 if vecmajor else 8)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, pa, pb,
+                    signed=signed, vecmajor=vecmajor, mma_kind=_lib.MMA_DP4A)
+    ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, pa, pb,
+                            oracle.SIGNED if signed else oracle.UNSIGNED, alignment=8,
+                            layout=oracle.OUT_VECMAJOR if vecmajor else oracle.OUT_BLOCKED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", DP4A_PAIRS)
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("fill", [0x00, 0xFF, 0x80, 0x7F, "alt"])
+@pytest.mark.parametrize("V", [2, 8])
+def test_sddmm_dp4a_extreme_values(cuda, pa, pb, signed, fill, V):
+    """Extreme lane values with K = 1024: the int32 dp4a chains hold every
+    exact sum."""
+    K, N = 1024, 128
+    mask = synth.lengths_mask([128, 3, 17, 0, 64, 8, 100, 1], N, V, seed=19)
+    nl, nr = mask.rows * K * pa // 8, N * K * pb // 8
+    if fill == "alt":
+        lhs = np.tile(np.array([0x80, 0x7F], np.uint8), nl // 2 + 1)[:nl]
+        rhs = np.tile(np.array([0x7F, 0x80, 0xFF, 0x00], np.uint8), nr // 4 + 1)[:nr]
+    else:
+        lhs, rhs = np.full(nl, fill, np.uint8), np.full(nr, fill, np.uint8)
+    hm = formats.prepare_sddmm(mask)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, pa, pb, signed=signed,
+                    mma_kind=_lib.MMA_DP4A)
+    ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, pa, pb,
+                            oracle.SIGNED if signed else oracle.UNSIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("V", [2, 4, 8])
+@pytest.mark.parametrize("vecmajor", [False, True])
+def test_sddmm_dp4a_many_tasks_batched(cuda, V, vecmajor):
+    """Many rows per launch (one row 1024 long), several batch entries, row
+    split chosen by the library."""
+    pa = pb = 8
+    K, N, B = 64, 1024, 3
+    lengths = np.random.default_rng(V).integers(0, 60, size=1024)
+    lengths[::29] = 0
+    lengths[3] = 1024
+    mask = synth.lengths_mask(lengths, N, V, seed=31)
+    hm = formats.prepare_sddmm(mask, alignment=16 if vecmajor else 8)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    lhs_all = [synth.random_bytes(mask.rows * K * pa // 8, 90 + b) for b in range(B)]
+    rhs_all = [synth.random_bytes(N * K * pb // 8, 95 + b) for b in range(B)]
+    out = ops.sddmm(dm, torch.from_numpy(np.concatenate(lhs_all)).to(cuda),
+                    torch.from_numpy(np.concatenate(rhs_all)).to(cuda), K, pa, pb, signed=True, batch=B,
+                    vecmajor=vecmajor, mma_kind=_lib.MMA_DP4A)
+    for b in range(B):
+        ref = oracle.sddmm_host(lhs_all[b], rhs_all[b], hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N,
+                                pa, pb, oracle.SIGNED,
+                                layout=oracle.OUT_VECMAJOR if vecmajor else oracle.OUT_BLOCKED)
+        np.testing.assert_array_equal(out[b].cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", DP4A_PAIRS)
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_sddmm_dp4a_half_equals_int8_path(cuda, pa, pb, V):
+    """Half output (the attention scores): the same bits as the int8 MMA path."""
+    K, N, scale = 64, 256, 36.0 * 36.0
+    mask, lhs, rhs = _case(pa, pb, V, K, N, RAGGED, seed=41 + V)
+    hm = formats.prepare_sddmm(mask, alignment=16)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    args = (dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, pa, pb)
+    a = ops.sddmm(*args, signed=True, vecmajor=True, out_half=True, scale=scale, mma_kind=_lib.MMA_DP4A)
+    b = ops.sddmm(*args, signed=True, vecmajor=True, out_half=True, scale=scale, mma_kind=_lib.MMA_INT8)
+    written = np.zeros(hm.aligned_nnz * V, bool)
+    for i in range(mask.m_vec):
+        written[hm.row_offsets[2 * i] * V:hm.row_offsets[2 * i + 1] * V] = True
+    np.testing.assert_array_equal(a.cpu().numpy().view(np.uint16)[written], b.cpu().numpy().view(np.uint16)[written])
+
+
+def test_sddmm_dp4a_rejects_16_bit(cuda):
+    V, K, N = 8, 64, 128
+    mask, lhs, rhs = _case(16, 8, V, K, N, [8, 16], seed=3)
+    dm = ops.DeviceSddmmMask.from_host(formats.prepare_sddmm(mask), cuda)
+    with pytest.raises(_lib.MagicubeError, match="dp4a"):
+        ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, 16, 8, signed=True,
+                  mma_kind=_lib.MMA_DP4A)

@@ -272,6 +272,13 @@ int mcProbeTensorCorePeak(int n, int iters, float* ms_out, double* ops_out, unsi
  * words; word 0 accumulates the mismatches, word 1 (signed) is lowered to the
  * first mismatching numerator -- initialise them to 0 and hi. */
 int mcCheckQuotients(float divisor, long long lo, long long hi, void* counters, cudaStream_t stream);
+/* mcCheckSmallIntConversions: compares the kernels' float-to-int conversion
+ * for |f| < 2^22 (one add of 1.5 * 2^23, then the bit pattern) with the
+ * hardware conversions, round-to-nearest-even and toward zero, for every
+ * float whose 32-bit pattern is in [lo, hi).  counters: two device uint64,
+ * zeroed and UINT64_MAX by the caller; receives the number of mismatches and
+ * the smallest mismatching pattern.  Asynchronous. */
+int mcCheckSmallIntConversions(unsigned long long lo, unsigned long long hi, void* counters, cudaStream_t stream);
 
 /* mcSparseAttention: the quantized sparse attention of every vector-row and
  * head in one persistent kernel (SDDMM, softmax + requantization, SpMM with

@@ -105,6 +105,7 @@ _SIGNATURES = {
     "mcProbeTensorPeak": (_c_int, [_c_int, _c_vp, _c_ll, _c_int, ctypes.POINTER(ctypes.c_float),
                                    ctypes.POINTER(ctypes.c_double), _c_vp]),
     "mcCheckQuotients": (_c_int, [_c_float, _c_ll, _c_ll, _c_vp, _c_vp]),
+    "mcCheckSmallIntConversions": (_c_int, [ctypes.c_ulonglong, ctypes.c_ulonglong, _c_vp, _c_vp]),
     "mcProbeTensorCorePeak": (_c_int, [_c_int, _c_int, ctypes.POINTER(ctypes.c_float),
                                        ctypes.POINTER(ctypes.c_double), _c_vp, _c_vp]),
     "mcAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp]),

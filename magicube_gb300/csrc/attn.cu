@@ -17,6 +17,7 @@
 //    starts lanes 1..V-1 from 0, which only shifts the exponent's argument).
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
 #include "mc_host.h"
 #include "mc_ptx.cuh"
@@ -65,25 +66,23 @@ struct SoftmaxParams {
     long long row_div_stride; // floats
 };
 
+// V raw halves of one slot (one 16-, 8- or 4-byte load) and their scaled
+// floats.
 template <int V>
-__device__ __forceinline__ void load_vec(const __half* p, float (&x)[V], float s)
+struct RawVec {
+    using T = typename std::conditional<V == 8, int4, typename std::conditional<V == 4, int2, int>::type>::type;
+};
+template <int V>
+__device__ __forceinline__ typename RawVec<V>::T ld_raw(const __half* p)
 {
-    if constexpr (V == 8) {
-        int4 r = *reinterpret_cast<const int4*>(p);
-        const __half* h = reinterpret_cast<const __half*>(&r);
+    return *reinterpret_cast<const typename RawVec<V>::T*>(p);
+}
+template <int V>
+__device__ __forceinline__ void cvt_vec(const typename RawVec<V>::T& r, float (&x)[V], float s)
+{
+    const __half* h = reinterpret_cast<const __half*>(&r);
 #pragma unroll
-        for (int v = 0; v < 8; ++v) x[v] = __fmul_rn(__half2float(h[v]), s);
-    } else if constexpr (V == 4) {
-        int2 r = *reinterpret_cast<const int2*>(p);
-        const __half* h = reinterpret_cast<const __half*>(&r);
-#pragma unroll
-        for (int v = 0; v < 4; ++v) x[v] = __fmul_rn(__half2float(h[v]), s);
-    } else {
-        int r = *reinterpret_cast<const int*>(p);
-        const __half* h = reinterpret_cast<const __half*>(&r);
-        x[0] = __fmul_rn(__half2float(h[0]), s);
-        x[1] = __fmul_rn(__half2float(h[1]), s);
-    }
+    for (int v = 0; v < V; ++v) x[v] = __fmul_rn(__half2float(h[v]), s);
 }
 
 // Running maximum and minimum of raw half scores, V lanes as V/2 half2.
@@ -98,12 +97,10 @@ struct HalfRange {
             lo[i] = __half2half2(__ushort_as_half((unsigned short)0x7C00u));  // +inf
         }
     }
-    __device__ __forceinline__ void add(const __half* p)
+    __device__ __forceinline__ void add(const typename RawVec<V>::T& r)
     {
         __half2 h[V / 2];
-        if constexpr (V == 8) *reinterpret_cast<int4*>(h) = *reinterpret_cast<const int4*>(p);
-        else if constexpr (V == 4) *reinterpret_cast<int2*>(h) = *reinterpret_cast<const int2*>(p);
-        else *reinterpret_cast<int*>(h) = *reinterpret_cast<const int*>(p);
+        *reinterpret_cast<typename RawVec<V>::T*>(h) = r;
 #pragma unroll
         for (int i = 0; i < V / 2; ++i) {
             hi[i] = __hmax2(hi[i], h[i]);  // a NaN input yields the other operand
@@ -181,8 +178,18 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
 
     float mx[V], sum[V], x[V];
     {
+        // four independent loads per lane in flight: the scores come from
+        // DRAM on this pass, and the maximum does not depend on the order
         HalfRange<V> range;
-        for (int j = lane; j < nnz; j += 32) range.add(sc + (long long)j * V);
+        for (int j0 = lane; j0 < nnz; j0 += 128) {
+            typename RawVec<V>::T r[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j0 + 32 * u < nnz) r[u] = ld_raw<V>(sc + (long long)(j0 + 32 * u) * V);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (j0 + 32 * u < nnz) range.add(r[u]);
+        }
         range.scaled_max(p.scaling, mx);
     }
 #pragma unroll
@@ -193,28 +200,41 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
     }
 
     if constexpr (ROWMAX) {
-        for (int j = 2 * lane; j < nnz; j += 64) {
-            const bool two = j + 1 < nnz;
-            int q0[V], q1[V];
-            load_vec<V>(sc + (long long)j * V, x, p.scaling);
+        // two slot pairs per iteration (j, j+1, j+64, j+65: the lane's order),
+        // their four loads issued first
+        for (int jj = 2 * lane; jj < nnz; jj += 128) {
+            typename RawVec<V>::T r[4];
 #pragma unroll
-            for (int v = 0; v < V; ++v) {
-                const float e = __expf(x[v] - mx[v]);
-                sum[v] += e;
-                q0[v] = __float2int_rn(127.f * e);
-                q1[v] = 0;
+            for (int u = 0; u < 4; ++u) {
+                const int j = jj + 64 * (u >> 1) + (u & 1);
+                if (j < nnz) r[u] = ld_raw<V>(sc + (long long)j * V);
             }
-            if (two) {
-                load_vec<V>(sc + (long long)(j + 1) * V, x, p.scaling);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = jj + 64 * h;
+                if (j >= nnz) break;
+                const bool two = j + 1 < nnz;
+                int q0[V], q1[V];
+                cvt_vec<V>(r[2 * h], x, p.scaling);
 #pragma unroll
                 for (int v = 0; v < V; ++v) {
-                    const float e = __expf(x[v] - mx[v]);
+                    const float e = exp_flush(x[v] - mx[v]);
                     sum[v] += e;
-                    q1[v] = __float2int_rn(127.f * e);
+                    q0[v] = __float2int_rn(127.f * e);
+                    q1[v] = 0;
                 }
-            }
+                if (two) {
+                    cvt_vec<V>(r[2 * h + 1], x, p.scaling);
 #pragma unroll
-            for (int v = 0; v < V; ++v) store_pair<V, 8>(out, j, v, q0[v], q1[v], two);
+                    for (int v = 0; v < V; ++v) {
+                        const float e = exp_flush(x[v] - mx[v]);
+                        sum[v] += e;
+                        q1[v] = __float2int_rn(127.f * e);
+                    }
+                }
+#pragma unroll
+                for (int v = 0; v < V; ++v) store_pair<V, 8>(out, j, v, q0[v], q1[v], two);
+            }
         }
 #pragma unroll
         for (int v = 0; v < V; ++v)
@@ -228,14 +248,19 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
         return;
     }
 
-    for (int j = 2 * lane; j < nnz; j += 64) {
-        load_vec<V>(sc + (long long)j * V, x, p.scaling);
+    for (int jj = 2 * lane; jj < nnz; jj += 128) {  // slots jj, jj+1, jj+64, jj+65 in this order
+        typename RawVec<V>::T r[4];
 #pragma unroll
-        for (int v = 0; v < V; ++v) sum[v] += __expf(x[v] - mx[v]);
-        if (j + 1 < nnz) {
-            load_vec<V>(sc + (long long)(j + 1) * V, x, p.scaling);
+        for (int u = 0; u < 4; ++u) {
+            const int j = jj + 64 * (u >> 1) + (u & 1);
+            if (j < nnz) r[u] = ld_raw<V>(sc + (long long)j * V);
+        }
 #pragma unroll
-            for (int v = 0; v < V; ++v) sum[v] += __expf(x[v] - mx[v]);
+        for (int u = 0; u < 4; ++u) {
+            if (jj + 64 * (u >> 1) + (u & 1) >= nnz) continue;
+            cvt_vec<V>(r[u], x, p.scaling);
+#pragma unroll
+            for (int v = 0; v < V; ++v) sum[v] += exp_flush(x[v] - mx[v]);
         }
     }
     float rs[V];  // scale / sum: one division per vector lane
@@ -245,26 +270,37 @@ __global__ void __launch_bounds__(128) quant_softmax_kernel(const SoftmaxParams 
         for (int o = 16; o > 0; o >>= 1) sum[v] += __shfl_xor_sync(0xffffffffu, sum[v], o);
         rs[v] = __fdiv_rn(p.scale, sum[v]);
     }
-    for (int j = 2 * lane; j < nnz; j += 64) {
-        const bool two = j + 1 < nnz;
-        int q0[V], q1[V];
-        load_vec<V>(sc + (long long)j * V, x, p.scaling);
+    for (int jj = 2 * lane; jj < nnz; jj += 128) {
+        typename RawVec<V>::T r[4];
 #pragma unroll
-        for (int v = 0; v < V; ++v) {
-            const float f = fminf(fmaxf(__expf(x[v] - mx[v]) * rs[v], LO), HI);
-            q0[v] = (int)f;
-            q1[v] = 0;
+        for (int u = 0; u < 4; ++u) {
+            const int j = jj + 64 * (u >> 1) + (u & 1);
+            if (j < nnz) r[u] = ld_raw<V>(sc + (long long)j * V);
         }
-        if (two) {
-            load_vec<V>(sc + (long long)(j + 1) * V, x, p.scaling);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = jj + 64 * h;
+            if (j >= nnz) break;
+            const bool two = j + 1 < nnz;
+            int q0[V], q1[V];
+            cvt_vec<V>(r[2 * h], x, p.scaling);
 #pragma unroll
             for (int v = 0; v < V; ++v) {
-                const float f = fminf(fmaxf(__expf(x[v] - mx[v]) * rs[v], LO), HI);
-                q1[v] = (int)f;
+                const float f = fminf(fmaxf(exp_flush(x[v] - mx[v]) * rs[v], LO), HI);
+                q0[v] = (int)f;
+                q1[v] = 0;
             }
-        }
+            if (two) {
+                cvt_vec<V>(r[2 * h + 1], x, p.scaling);
 #pragma unroll
-        for (int v = 0; v < V; ++v) store_pair<V, BITS>(out, j, v, q0[v], q1[v], two);
+                for (int v = 0; v < V; ++v) {
+                    const float f = fminf(fmaxf(exp_flush(x[v] - mx[v]) * rs[v], LO), HI);
+                    q1[v] = (int)f;
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < V; ++v) store_pair<V, BITS>(out, j, v, q0[v], q1[v], two);
+        }
     }
 }
 

@@ -199,10 +199,10 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
                     float e0 = 0.f, e1 = 0.f;
                     if (j < nnz) {
                         const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
-                        e0 = __expf(x.x - mx);
+                        e0 = exp_flush(x.x - mx);
                         sum += e0;
                         if (j + 1 < nnz) {
-                            e1 = __expf(x.y - mx);
+                            e1 = exp_flush(x.y - mx);
                             sum += e1;
                         }
                     }
@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
                     const int j = 64 * i + 2 * lane;
                     if (j < nnz) {
                         const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
-                        sum += __expf(__fmul_rn(x.x, p.scaling) - mx);
-                        if (j + 1 < nnz) sum += __expf(__fmul_rn(x.y, p.scaling) - mx);
+                        sum += exp_flush(__fmul_rn(x.x, p.scaling) - mx);
+                        if (j + 1 < nnz) sum += exp_flush(__fmul_rn(x.y, p.scaling) - mx);
                     }
                 }
 #pragma unroll
@@ -231,9 +231,9 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
                     int q0 = 0, q1 = 0;
                     if (j < nnz) {
                         const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
-                        q0 = (int)fminf(fmaxf(__expf(__fmul_rn(x.x, p.scaling) - mx) * rs, -128.f), 127.f);
+                        q0 = (int)fminf(fmaxf(exp_flush(__fmul_rn(x.x, p.scaling) - mx) * rs, -128.f), 127.f);
                         if (j + 1 < nnz)
-                            q1 = (int)fminf(fmaxf(__expf(__fmul_rn(x.y, p.scaling) - mx) * rs, -128.f), 127.f);
+                            q1 = (int)fminf(fmaxf(exp_flush(__fmul_rn(x.y, p.scaling) - mx) * rs, -128.f), 127.f);
                     }
                     __syncwarp();
                     if (j < nround) *reinterpret_cast<uint16_t*>(pv + j) = (uint16_t)((q0 & 0xFF) | ((q1 & 0xFF) << 8));

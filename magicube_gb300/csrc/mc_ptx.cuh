@@ -125,6 +125,40 @@ __device__ __forceinline__ void bytes_to_h2(uint32_t w, uint32_t& lo, uint32_t& 
 // f32 accumulator holding an exact integer -> int32.
 __device__ __forceinline__ int f2i_exact(float f) { return __float2int_rn(f); }
 
+// e^y for the softmax: 2^(y log2 e) on the MUFU unit (ex2.approx, relative
+// error about 2^-22), results below 2^-126 flushed to zero.  A flushed term
+// cannot change a row sum that contains e^0 = 1, and it quantizes to 0 for
+// any probability scale below 2^126, so the flush changes no output there;
+// without it the non-flushing ex2 needs extra instructions around the MUFU
+// operation in this (non-ftz) build.  The separate and the fused softmax both
+// use it, which keeps them bit-identical.
+__device__ __forceinline__ float exp_flush(float y)
+{
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__fmul_rn(y, 1.4426950408889634f)));
+    return r;
+}
+
+// float -> int for |f| < 2^22 on the FMA and integer pipes instead of the
+// quarter-rate conversion unit: f + 1.5 * 2^23 lies in [2^23, 2^24), where
+// the f32 spacing is 1, so rounding the sum rounds f to an integer, and the
+// sum's bit pattern is 0x4B400000 plus that integer.
+// f2i_rn_small(f) == __float2int_rn(f) (nearest, ties to even);
+// f2i_rz_small(f) == (int)f (toward zero).  Both are checked against the
+// conversion instructions for every float with |f| < 2^22
+// (mcCheckSmallIntConversions).  Worth it where the conversion unit is the
+// bottleneck (the dense-tile SDDMM epilogue); elsewhere the extra issue slots
+// cost more than they save (measured slower in the softmax).
+__device__ __forceinline__ int f2i_rn_small(float f)
+{
+    return __float_as_int(__fadd_rn(f, 12582912.0f)) - 0x4B400000;
+}
+__device__ __forceinline__ int f2i_rz_small(float f)
+{
+    const int m = __float_as_int(__fadd_rz(fabsf(f), 12582912.0f)) - 0x4B400000;
+    return f < 0.f ? -m : m;
+}
+
 // Byte mask keeping the first `valid` (clamped to 0..4) bytes of a word.
 __device__ __forceinline__ uint32_t byte_mask(int valid)
 {

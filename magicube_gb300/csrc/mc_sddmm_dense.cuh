@@ -85,16 +85,6 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, uint32_t (&r)[N])
         asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
 }
 
-// f32 accumulator holding an exact integer x with |x| < 2^22 -> int32:
-// x + 1.5 * 2^23 lies in [2^23, 2^24), where the f32 spacing is 1, so the sum
-// is exact and its bit pattern is 0x4B400000 + x (one FADD and one IADD
-// instead of a quarter-rate conversion).  8-bit products over k = 64 stay
-// below 64 x 255^2 < 2^22.
-__device__ __forceinline__ int acc_to_int(uint32_t acc_bits)
-{
-    return (int)(__float_as_uint(__fadd_rn(__uint_as_float(acc_bits), 12582912.0f)) - 0x4B400000u);
-}
-
 // 16 int8 values (one 16-byte k chunk q of row `row`) -> 16 f16 in the
 // 128-byte-swizzled K-major tile: f16 chunks 2q and 2q + 1 of the row.
 template <bool SIGNED>
@@ -313,7 +303,8 @@ sddmm_dense_tc_kernel(const SddmmDenseParams dp, unsigned int* timeouts)
                             int d[V];
                             if constexpr (!HALF_OUT) {
 #pragma unroll
-                                for (int v = 0; v < V; ++v) d[v] = acc_to_int(acc[g][v]);
+                                // exact integers below 64 x 255^2 < 2^22 in magnitude
+                                for (int v = 0; v < V; ++v) d[v] = f2i_rn_small(__uint_as_float(acc[g][v]));
                             }
                             if constexpr (VECMAJOR) {
                                 const long long o = obase + (long long)slot * V;

@@ -98,6 +98,33 @@ __global__ void __launch_bounds__(256) quotient_check_kernel(float d, long long 
     }
 }
 
+// f2i_rn_small / f2i_rz_small against __float2int_rn / __float2int_rz for
+// every float whose bit pattern (sign included) is in [lo, hi); counters[0]
+// += mismatches, counters[1] = min(first mismatching pattern).
+__global__ void __launch_bounds__(256) small_int_check_kernel(unsigned long long lo, unsigned long long hi,
+                                                              unsigned long long* counters)
+{
+    unsigned long long bad = 0, first = hi;
+    const unsigned long long step = (unsigned long long)gridDim.x * blockDim.x;
+    for (unsigned long long u = lo + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; u < hi; u += step) {
+        const float f = __uint_as_float((uint32_t)u);
+        if (f2i_rn_small(f) != __float2int_rn(f) || f2i_rz_small(f) != __float2int_rz(f)) {
+            ++bad;
+            if (u < first) first = u;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bad += __shfl_xor_sync(0xffffffffu, bad, o);
+        const unsigned long long f = __shfl_xor_sync(0xffffffffu, first, o);
+        first = f < first ? f : first;
+    }
+    if ((threadIdx.x & 31) == 0 && bad) {
+        atomicAdd(counters, bad);
+        atomicMin(counters + 1, first);
+    }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(256) tensor_peak_kernel(int* out, int iters, unsigned seed)
 {
@@ -254,5 +281,18 @@ extern "C" int mcCheckQuotients(float divisor, long long lo, long long hi, void*
     if (lo == hi) return 0;
     const int blocks = mc::sm_count() * 8;
     mc::quotient_check_kernel<<<blocks, 256, 0, stream>>>(divisor, lo, hi, static_cast<unsigned long long*>(counters));
+    return (int)cudaGetLastError();
+}
+
+extern "C" int mcCheckSmallIntConversions(unsigned long long lo, unsigned long long hi, void* counters,
+                                          cudaStream_t stream)
+{
+    mc::clear_error();
+    if (!counters || reinterpret_cast<uintptr_t>(counters) % 8 || hi > 0x100000000ULL || lo > hi)
+        return mc::fail(1, "mcCheckSmallIntConversions: counters must be 8-byte aligned; [lo, hi) must lie in "
+                           "the 32-bit pattern range");
+    if (lo == hi) return 0;
+    const int blocks = mc::sm_count() * 8;
+    mc::small_int_check_kernel<<<blocks, 256, 0, stream>>>(lo, hi, static_cast<unsigned long long*>(counters));
     return (int)cudaGetLastError();
 }

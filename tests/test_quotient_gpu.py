@@ -25,3 +25,15 @@ def test_quotient_equals_ieee_division(cuda, d):
     _lib.check(_lib.lib().mcCheckQuotients(float(d), lo, hi, counters.data_ptr(), stream), "mcCheckQuotients")
     bad, first = counters.tolist()
     assert bad == 0, f"{bad} mismatches, first numerator {first}"
+
+
+@pytest.mark.parametrize("lo,hi", [(0x00000000, 0x4A800000), (0x80000000, 0xCA800000)])
+def test_small_int_conversions_equal_hardware(cuda, lo, hi):
+    """The add-and-reinterpret float-to-int of the dense-tile SDDMM epilogue
+    equals cvt.rni (and the toward-zero form cvt.rzi) for every float with
+    |f| < 2^22 (bit patterns up to 0x4A800000 = 2^22, both signs)."""
+    counters = torch.tensor([0, -1], dtype=torch.int64, device=cuda)
+    stream = torch.cuda.current_stream().cuda_stream
+    _lib.check(_lib.lib().mcCheckSmallIntConversions(lo, hi, counters.data_ptr(), stream), "mcCheckSmallIntConversions")
+    bad, first = counters.tolist()
+    assert bad == 0, f"{bad} mismatches, first pattern {first & 0xFFFFFFFFFFFFFFFF:#x}"

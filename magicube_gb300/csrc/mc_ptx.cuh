@@ -93,6 +93,19 @@ __device__ __forceinline__ void unpack4_u32(uint32_t x, uint32_t& out0, uint32_t
     if (SIGNED) { out0 = sext_nibble_bytes(out0); out1 = sext_nibble_bytes(out1); }
 }
 
+// 8 packed nibbles -> two words of bytes holding each nibble in the byte's
+// high half (nibbles 0..3, 4..7): the byte is 16 x the nibble, as a signed
+// byte exactly 16 x its sign extension.  A product of two such bytes is 256 x
+// the nibbles' product, so an int32 sum of them is 256 x the nibble sum
+// (exact while |sum| < 2^23) and an arithmetic shift by 8 recovers it; five
+// integer operations per word instead of the unpack and sign extension.
+__device__ __forceinline__ void unpack4_hi_u32(uint32_t x, uint32_t& out0, uint32_t& out1)
+{
+    const uint32_t even = (x << 4) & 0xF0F0F0F0u, odd = x & 0xF0F0F0F0u;
+    out0 = prmt(even, odd, 0x5140);
+    out1 = prmt(even, odd, 0x7362);
+}
+
 // Combine a low-nibble plane word and a high-nibble plane word (each four
 // nibbles in the low 16 bits) into four bytes (hi << 4 | lo).
 __device__ __forceinline__ uint32_t merge_nibble_planes(uint32_t lo16, uint32_t hi16)

@@ -66,6 +66,15 @@ __device__ __forceinline__ void load_kfrag(const uint8_t* row, int kb, int t, ui
     }
 }
 
+// The same 16 k elements of a 4-bit row with each nibble in its byte's high
+// half (16 x the value, see unpack4_hi_u32).
+__device__ __forceinline__ void load_kfrag_hi4(const uint8_t* row, int kb, int t, uint32_t (&pl)[2][4])
+{
+    int2 v = ldg_nc_v2(row + kb * 32 + 8 * t);
+    unpack4_hi_u32((uint32_t)v.x, pl[0][0], pl[0][1]);
+    unpack4_hi_u32((uint32_t)v.y, pl[0][2], pl[0][3]);
+}
+
 template <int BITS>
 struct BytePlanes { static constexpr int N = BITS == 16 ? 2 : 1; };
 

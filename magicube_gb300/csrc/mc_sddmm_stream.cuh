@@ -47,9 +47,16 @@ sddmm_k64_kernel(const SddmmParams p)
 
     const int* cols = p.col_indices + start;
     const uint8_t* rhs = p.rhs + (long long)b * p.rhs_stride;
+    // L4-R4 on the int8 MMA: both operands as 16 x nibble bytes, the sums 256 x
+    // the result (|result| <= 64 x 64 for k = 64: no wrap), shifted back below
+    constexpr bool HI4 = PREA == 4 && PREB == 4 && !F16;
 
     uint32_t a[2][4] = {};
-    if (g < V) load_kfrag<PREA, SIGNED>(p.lhs + (long long)b * p.lhs_stride + (long long)(row * V + g) * LHS_ROW, 0, t, a);
+    if (g < V) {
+        const uint8_t* arow = p.lhs + (long long)b * p.lhs_stride + (long long)(row * V + g) * LHS_ROW;
+        if constexpr (HI4) load_kfrag_hi4(arow, 0, t, a);
+        else load_kfrag<PREA, SIGNED>(arow, 0, t, a);
+    }
     uint32_t ah[PA][8];
     if constexpr (F16) {
 #pragma unroll
@@ -85,7 +92,10 @@ sddmm_k64_kernel(const SddmmParams p)
                 for (int q = 0; q < 2; ++q)
 #pragma unroll
                     for (int e = 0; e < 4; ++e) r[u][hf][q][e] = 0u;
-                if (c[u][hf] >= 0) load_kfrag<PREB, SIGNED>(rhs + (unsigned)c[u][hf] * RHS_ROW, 0, t, r[u][hf]);
+                if (c[u][hf] >= 0) {
+                    if constexpr (HI4) load_kfrag_hi4(rhs + (unsigned)c[u][hf] * RHS_ROW, 0, t, r[u][hf]);
+                    else load_kfrag<PREB, SIGNED>(rhs + (unsigned)c[u][hf] * RHS_ROW, 0, t, r[u][hf]);
+                }
             }
         int cn[U][2];
 #pragma unroll
@@ -147,7 +157,7 @@ sddmm_k64_kernel(const SddmmParams p)
                     for (int rb = 0; rb < PB; ++rb)
 #pragma unroll
                         for (int lb = 0; lb < PA; ++lb) s += (uint32_t)acc[rb][lb][e] << (8 * (rb + lb));
-                    d[e] = (int)s;
+                    d[e] = HI4 ? ((int)s >> 8) : (int)s;
                 }
             }
             // d[0..1]: nonzero tile*16 + g, lanes 2t, 2t+1; d[2..3]: nonzero + 8.

@@ -239,3 +239,27 @@ def test_sddmm_dp4a_rejects_16_bit(cuda):
     with pytest.raises(_lib.MagicubeError, match="dp4a"):
         ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, 16, 8, signed=True,
                   mma_kind=_lib.MMA_DP4A)
+
+
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("fill", [0x88, 0x77, 0xFF, 0x00, 0x8F, "alt"])
+@pytest.mark.parametrize("V", [2, 8])
+def test_sddmm_k64_extreme_4bit(cuda, signed, fill, V):
+    """L4-R4 at k = 64 on the pipelined kernel, whose int8 MMA takes each
+    nibble as 16 x its value and shifts the sums back: the largest products
+    (-8 x -8, 15 x 15 unsigned) and mixed signs stay exact."""
+    K, N = 64, 256
+    mask = synth.lengths_mask([256, 3, 17, 0, 64, 8, 100, 1, 255], N, V, seed=23)
+    nl, nr = mask.rows * K // 2, N * K // 2
+    if fill == "alt":
+        lhs = np.tile(np.array([0x87, 0x78], np.uint8), nl // 2 + 1)[:nl]
+        rhs = np.tile(np.array([0x7F, 0x80, 0xF8, 0x08], np.uint8), nr // 4 + 1)[:nr]
+    else:
+        lhs, rhs = np.full(nl, fill, np.uint8), np.full(nr, fill, np.uint8)
+    hm = formats.prepare_sddmm(mask)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), K, 4, 4, signed=signed,
+                    mma_kind=_lib.MMA_INT8, variant=_lib.KERNEL_STREAM)
+    ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, 4, 4,
+                            oracle.SIGNED if signed else oracle.UNSIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)

@@ -303,7 +303,8 @@ def run_gpu(args) -> None:
         # pairs and the SpMM run on mma.sync (int8 unless --mma f16)
         others = [m for m in (1, 2, 3, 4) if m != args.mma]
         sync_mma = 2 if args.mma == 2 else 1
-        cases = [(4, 4, "sddmm_L4R4", sync_mma, 0, VEC), (16, 8, "sddmm_L16R8", sync_mma, 0, VEC)]
+        cases = [(4, 4, "sddmm_L4R4", sync_mma, 0, VEC), (16, 8, "sddmm_L16R8", 0, 0, VEC),
+                 (16, 8, "sddmm_L16R8_int8mma", 1, 0, VEC)]
         cases += [(8, 8, f"sddmm_L8R8_{MMA_NAMES[m]}", m, 0, VEC) for m in others]
         cases += [(8, 8, "sddmm_L8R8_per_row_kernel", sync_mma, 1, VEC)]
         # V = 2 and 4: the int8 MMA computes 8 lanes of which V are used; dp4a

@@ -87,7 +87,10 @@ int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* row_indices, const int* 
  *              f32 accumulation flushed into int32 every 256 products (every
  *              partial sum is an integer below 2^24, so nothing rounds); on
  *              sm_103a the f16 tensor rate is several times the int8 one.
- * MC_MMA_DEFAULT selects the library default (mcSetDefaultMmaKind). */
+ * MC_MMA_DEFAULT selects the library default (mcSetDefaultMmaKind), except
+ *              for the SDDMM L16-R8 at k == 64, which it runs on the f16 path
+ *              (faster there on GB300: the 16-bit operand's two byte planes
+ *              double the int8 MMAs). */
 /* MC_MMA_TCGEN05 (SDDMM L8-R8 with k == 64 only): operands converted exactly
  *              to f16 in shared memory, tcgen05.mma kind::f16 (M = 128
  *              nonzeros, N = 16, K = 64) with the f32 accumulator in TMEM;

@@ -181,65 +181,109 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
         // Lane l visits slot pairs (2l, 2l+1), (2l+64, 2l+65), ...: one 32-bit
         // load of two half scores, one 16-bit store of two probabilities.
         // The maximum is exact in any order; the sum keeps the per-thread
-        // order and reduction tree of the separate softmax kernel.  Every
-        // lane runs the same iterations; a __syncwarp separates the scores
-        // read in an iteration from the probability bytes written over them.
+        // order and reduction tree of the separate softmax kernel.  Both
+        // vector lanes of the warp and two pair iterations go through each
+        // trip: their loads and exponentials are independent, only the adds
+        // are chained (in each lane's order; an absent slot adds +0, which
+        // leaves a sum of non-negative terms unchanged).  A __syncwarp
+        // separates the scores read in a trip from the probability bytes
+        // written over them: the bytes of iteration k overlay scores read in
+        // iteration k / 2 or earlier.
         const int npit = (nround + 63) >> 6;
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const int v = 2 * warp + e;
-            if (v >= V) break;
-            const __half* sv = S + v * SP;
-            const float mx = fmaxf(fmaxf(MAXW[v], MAXW[8 + v]), fmaxf(MAXW[16 + v], MAXW[24 + v]));
-            uint8_t* pv = P + v * PP;
-            float sum = 0.f;
+        if (2 * warp < V) {  // V is even: the warp holds lanes 2w and 2w + 1
+            const int va = 2 * warp;
+            const __half* sa = S + va * SP;
+            const __half* sb = sa + SP;
+            const float mxa = fmaxf(fmaxf(MAXW[va], MAXW[8 + va]), fmaxf(MAXW[16 + va], MAXW[24 + va]));
+            const float mxb = fmaxf(fmaxf(MAXW[va + 1], MAXW[9 + va]), fmaxf(MAXW[17 + va], MAXW[25 + va]));
+            uint8_t* pa = P + va * PP;
+            uint8_t* pb = pa + PP;
+            auto ld2 = [&](const __half* sv, int j) {
+                return j < nnz ? __half22float2(*reinterpret_cast<const __half2*>(sv + j)) : make_float2(0.f, 0.f);
+            };
+            // exponent of score x of slot jj (0 if the slot is past the row)
+            auto ex = [&](float x, float mx, int jj) {
+                return jj < nnz ? exp_flush((ROWMAX ? x : __fmul_rn(x, p.scaling)) - mx) : 0.f;
+            };
+            float suma = 0.f, sumb = 0.f;
             if constexpr (ROWMAX) {
-                for (int i = 0; i < npit; ++i) {
-                    const int j = 64 * i + 2 * lane;
-                    float e0 = 0.f, e1 = 0.f;
-                    if (j < nnz) {
-                        const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
-                        e0 = exp_flush(x.x - mx);
-                        sum += e0;
-                        if (j + 1 < nnz) {
-                            e1 = exp_flush(x.y - mx);
-                            sum += e1;
-                        }
+                for (int i = 0; i < npit; i += 2) {
+                    const int j0 = 64 * i + 2 * lane, j1 = j0 + 64;
+                    const float2 xa0 = ld2(sa, j0), xb0 = ld2(sb, j0), xa1 = ld2(sa, j1), xb1 = ld2(sb, j1);
+                    const float ea[4] = {ex(xa0.x, mxa, j0), ex(xa0.y, mxa, j0 + 1), ex(xa1.x, mxa, j1),
+                                         ex(xa1.y, mxa, j1 + 1)};
+                    const float eb[4] = {ex(xb0.x, mxb, j0), ex(xb0.y, mxb, j0 + 1), ex(xb1.x, mxb, j1),
+                                         ex(xb1.y, mxb, j1 + 1)};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        suma += ea[u];
+                        sumb += eb[u];
                     }
                     __syncwarp();
-                    if (j < nround)
-                        *reinterpret_cast<uint16_t*>(pv + j) =
-                            (uint16_t)((__float2int_rn(127.f * e0) & 0xFF) | ((__float2int_rn(127.f * e1) & 0xFF) << 8));
+                    auto q2 = [](float e0, float e1) {
+                        return (uint16_t)((__float2int_rn(127.f * e0) & 0xFF) | ((__float2int_rn(127.f * e1) & 0xFF) << 8));
+                    };
+                    if (j0 < nround) {
+                        *reinterpret_cast<uint16_t*>(pa + j0) = q2(ea[0], ea[1]);
+                        *reinterpret_cast<uint16_t*>(pb + j0) = q2(eb[0], eb[1]);
+                    }
+                    if (j1 < nround) {
+                        *reinterpret_cast<uint16_t*>(pa + j1) = q2(ea[2], ea[3]);
+                        *reinterpret_cast<uint16_t*>(pb + j1) = q2(eb[2], eb[3]);
+                    }
                 }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                for (int o = 16; o > 0; o >>= 1) {
+                    suma += __shfl_xor_sync(0xffffffffu, suma, o);
+                    sumb += __shfl_xor_sync(0xffffffffu, sumb, o);
+                }
             } else {
-                for (int i = 0; i < npit; ++i) {
-                    const int j = 64 * i + 2 * lane;
-                    if (j < nnz) {
-                        const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
-                        sum += exp_flush(__fmul_rn(x.x, p.scaling) - mx);
-                        if (j + 1 < nnz) sum += exp_flush(__fmul_rn(x.y, p.scaling) - mx);
+                for (int i = 0; i < npit; i += 2) {
+                    const int j0 = 64 * i + 2 * lane, j1 = j0 + 64;
+                    const float2 xa0 = ld2(sa, j0), xb0 = ld2(sb, j0), xa1 = ld2(sa, j1), xb1 = ld2(sb, j1);
+                    const float ea[4] = {ex(xa0.x, mxa, j0), ex(xa0.y, mxa, j0 + 1), ex(xa1.x, mxa, j1),
+                                         ex(xa1.y, mxa, j1 + 1)};
+                    const float eb[4] = {ex(xb0.x, mxb, j0), ex(xb0.y, mxb, j0 + 1), ex(xb1.x, mxb, j1),
+                                         ex(xb1.y, mxb, j1 + 1)};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        suma += ea[u];
+                        sumb += eb[u];
                     }
                 }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-                const float rs = __fdiv_rn(p.prob_scale, sum);
-                for (int i = 0; i < npit; ++i) {
-                    const int j = 64 * i + 2 * lane;
-                    // the exponents are recomputed: same inputs, same values
-                    int q0 = 0, q1 = 0;
-                    if (j < nnz) {
-                        const float2 x = __half22float2(*reinterpret_cast<const __half2*>(sv + j));
-                        q0 = (int)fminf(fmaxf(exp_flush(__fmul_rn(x.x, p.scaling) - mx) * rs, -128.f), 127.f);
-                        if (j + 1 < nnz)
-                            q1 = (int)fminf(fmaxf(exp_flush(__fmul_rn(x.y, p.scaling) - mx) * rs, -128.f), 127.f);
-                    }
+                for (int o = 16; o > 0; o >>= 1) {
+                    suma += __shfl_xor_sync(0xffffffffu, suma, o);
+                    sumb += __shfl_xor_sync(0xffffffffu, sumb, o);
+                }
+                const float rsa = __fdiv_rn(p.prob_scale, suma), rsb = __fdiv_rn(p.prob_scale, sumb);
+                // the exponents are recomputed: same inputs, same values
+                auto q = [&](float e, float rs) { return (int)fminf(fmaxf(e * rs, -128.f), 127.f); };
+                auto q2 = [&](float e0, float e1, float rs) {
+                    return (uint16_t)((q(e0, rs) & 0xFF) | ((q(e1, rs) & 0xFF) << 8));
+                };
+                for (int i = 0; i < npit; i += 2) {
+                    const int j0 = 64 * i + 2 * lane, j1 = j0 + 64;
+                    const float2 xa0 = ld2(sa, j0), xb0 = ld2(sb, j0), xa1 = ld2(sa, j1), xb1 = ld2(sb, j1);
+                    const float ea[4] = {ex(xa0.x, mxa, j0), ex(xa0.y, mxa, j0 + 1), ex(xa1.x, mxa, j1),
+                                         ex(xa1.y, mxa, j1 + 1)};
+                    const float eb[4] = {ex(xb0.x, mxb, j0), ex(xb0.y, mxb, j0 + 1), ex(xb1.x, mxb, j1),
+                                         ex(xb1.y, mxb, j1 + 1)};
                     __syncwarp();
-                    if (j < nround) *reinterpret_cast<uint16_t*>(pv + j) = (uint16_t)((q0 & 0xFF) | ((q1 & 0xFF) << 8));
+                    if (j0 < nround) {
+                        *reinterpret_cast<uint16_t*>(pa + j0) = q2(ea[0], ea[1], rsa);
+                        *reinterpret_cast<uint16_t*>(pb + j0) = q2(eb[0], eb[1], rsb);
+                    }
+                    if (j1 < nround) {
+                        *reinterpret_cast<uint16_t*>(pa + j1) = q2(ea[2], ea[3], rsa);
+                        *reinterpret_cast<uint16_t*>(pb + j1) = q2(eb[2], eb[3], rsb);
+                    }
                 }
             }
-            if (lane == 0) DEN[v] = ROWMAX ? 127.f * sum * p.out_scale : p.out_scale;
+            if (lane == 0) {
+                DEN[va] = ROWMAX ? 127.f * suma * p.out_scale : p.out_scale;
+                DEN[va + 1] = ROWMAX ? 127.f * sumb * p.out_scale : p.out_scale;
+            }
         }
         __syncthreads();
 

@@ -134,14 +134,14 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
             for (int hh = 0; hh < 2; ++hh) {
                 const int j = tile * 16 + g + 8 * hh;
                 if (j >= nnz) continue;
+                // Both modes keep the separate SDDMM's half output (fixed mode
+                // scales it on every read, row-max mode has the scaling folded
+                // into the divisor).  The maximum is taken of what the softmax
+                // reads.
+                const __half2 h2 = deq_half2(acc[2 * hh], acc[2 * hh + 1], sdiv, sdiv);
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {
-                    // Both modes keep the separate SDDMM's half output (fixed
-                    // mode scales it on every read, row-max mode has the
-                    // scaling folded into the divisor).  The maximum is
-                    // taken of what the softmax reads.
-                    const int a = acc[2 * hh + e];
-                    const __half hs = deq_half(a, sdiv);
+                    const __half hs = e ? __high2half(h2) : __low2half(h2);
                     S[(2 * t + e) * SP + j] = hs;
                     mxl[e] = fmaxf(mxl[e], ROWMAX ? __half2float(hs) : __fmul_rn(__half2float(hs), p.scaling));
                 }
@@ -338,10 +338,11 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
         if (2 * t < V) {
             __half* o = p.out + (long long)h * p.out_head_stride + (long long)(row * V + 2 * t) * 64 + 16 * warp + g;
             const Divisor d0 = make_divisor(DEN[2 * t]), d1 = make_divisor(DEN[2 * t + 1]);
-            o[0] = deq_half(tot[0], d0);
-            o[64] = deq_half(tot[1], d1);
-            o[8] = deq_half(tot[2], d0);
-            o[72] = deq_half(tot[3], d1);
+            const __half2 h01 = deq_half2(tot[0], tot[1], d0, d1), h23 = deq_half2(tot[2], tot[3], d0, d1);
+            o[0] = __low2half(h01);
+            o[64] = __high2half(h01);
+            o[8] = __low2half(h23);
+            o[72] = __high2half(h23);
         }
     }
 }

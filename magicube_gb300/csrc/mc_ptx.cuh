@@ -280,10 +280,39 @@ __device__ __forceinline__ __half deq_half(int acc, Divisor v)
 {
     return __float2half_rn(div_rn(__int2float_rn(acc), v));
 }
+// Two quotients at once, a0 / v0.d and a1 / v1.d: the steps of div_rn on
+// packed f32x2 operations (Blackwell).  Each lane rounds as the scalar
+// instruction does, and the residual is formed as q * (-d) + a, the same
+// product as (-q) * d, so both results equal div_rn's bit for bit.
+__device__ __forceinline__ float2 div_rn2(float a0, float a1, Divisor v0, Divisor v1)
+{
+    if (v0.r == 0.f || v1.r == 0.f) return make_float2(div_rn(a0, v0), div_rn(a1, v1));
+    unsigned long long A, R, ND, q, e;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(A) : "f"(a0), "f"(a1));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(R) : "f"(v0.r), "f"(v1.r));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ND) : "f"(-v0.d), "f"(-v1.d));
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(q) : "l"(A), "l"(R));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(e) : "l"(q), "l"(ND), "l"(A));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(q) : "l"(e), "l"(R), "l"(q));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(e) : "l"(q), "l"(ND), "l"(A));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(q) : "l"(e), "l"(R), "l"(q));
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(q));
+    return make_float2(lo, hi);
+}
+
+// half(a / v.d) and half(b / v.d) packed (a in the low half), as deq_half.
 __device__ __forceinline__ uint32_t pack_half2(int a, int b, Divisor v)
 {
-    __half2 h = __halves2half2(deq_half(a, v), deq_half(b, v));
+    const float2 q = div_rn2(__int2float_rn(a), __int2float_rn(b), v, v);
+    __half2 h = __floats2half2_rn(q.x, q.y);
     return *reinterpret_cast<uint32_t*>(&h);
+}
+// Two integers with their own divisors -> two halves.
+__device__ __forceinline__ __half2 deq_half2(int a, int b, Divisor va, Divisor vb)
+{
+    const float2 q = div_rn2(__int2float_rn(a), __int2float_rn(b), va, vb);
+    return __floats2half2_rn(q.x, q.y);
 }
 
 }  // namespace mc

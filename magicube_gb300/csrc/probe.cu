@@ -70,8 +70,9 @@ __global__ void __launch_bounds__(128) tc_peak_kernel(int iters, unsigned int* t
 
 // Compares div_rn (the kernels' quotient from a prepared divisor) with the
 // IEEE division __fdiv_rn for every integer numerator in [lo, hi), bit for
-// bit; counters[0] += mismatches, counters[1] = min(first mismatching
-// numerator).
+// bit, in the scalar form and in both lanes of the packed form (the second
+// lane on the numerator a ^ 0x55555555); counters[0] += mismatches,
+// counters[1] = min(first mismatching numerator).
 __global__ void __launch_bounds__(256) quotient_check_kernel(float d, long long lo, long long hi,
                                                              unsigned long long* counters)
 {
@@ -81,7 +82,12 @@ __global__ void __launch_bounds__(256) quotient_check_kernel(float d, long long 
     const long long step = (long long)gridDim.x * blockDim.x;
     for (long long a = lo + blockIdx.x * (long long)blockDim.x + threadIdx.x; a < hi; a += step) {
         const float x = __int2float_rn((int)a);
-        if (__float_as_uint(div_rn(x, v)) != __float_as_uint(__fdiv_rn(x, d))) {
+        // the packed form, its second lane on another numerator
+        const float x2 = __int2float_rn((int)((uint32_t)a ^ 0x55555555u));
+        const float2 q2 = div_rn2(x, x2, v, v);
+        const uint32_t ref = __float_as_uint(__fdiv_rn(x, d));
+        if (__float_as_uint(div_rn(x, v)) != ref || __float_as_uint(q2.x) != ref ||
+            __float_as_uint(q2.y) != __float_as_uint(__fdiv_rn(x2, d))) {
             ++bad;
             if (a < first) first = a;
         }

@@ -109,15 +109,19 @@ __global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams 
         // land while the scores and the softmax are computed.
         const int nround = (nnz + 31) & ~31;
         const int steps = nround >> 5;
+        // Copy i moves rows 16 (i & 1) .. +15 of the step, 32-byte half
+        // 2 (i >> 1) .. +1: lanes 2r and 2r + 1 take the two 16-byte chunks of
+        // one sector of row r, so each copy instruction reads 16 whole 32-byte
+        // sectors rather than 32 half sectors.
         auto issue = [&](int s, int slot) {
             if (s < steps) {
-                const int j = s * 32 + lane;
-                if (j < nnz) {
-                    const uint8_t* src = vh + (long long)C[j] * ROW;
-                    uint8_t* dst = ring + slot * 32 * ROW + lane * ROW;
-                    const int sw = (lane >> 1) & 3;
 #pragma unroll
-                    for (int c = 0; c < 4; ++c) cp_async16(dst + ((c ^ sw) << 4), src + c * 16);
+                for (int i = 0; i < 4; ++i) {
+                    const int r = 16 * (i & 1) + (lane >> 1), q = 2 * (i >> 1) + (lane & 1);
+                    const int j = s * 32 + r;
+                    if (j < nnz)
+                        cp_async16(ring + slot * 32 * ROW + r * ROW + ((q ^ ((r >> 1) & 3)) << 4),
+                                   vh + (long long)C[j] * ROW + q * 16);
                 }
             }
             cp_async_commit();

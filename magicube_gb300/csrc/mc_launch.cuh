@@ -5,6 +5,7 @@
 #include "mc_host.h"
 #include "mc_sddmm.cuh"
 #include "mc_sddmm_dp4a.cuh"
+#include "mc_spmm_n64.cuh"
 #include "mc_sddmm_stream.cuh"
 #include "mc_spmm.cuh"
 #include "mc_spmm_stream.cuh"
@@ -109,6 +110,23 @@ int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     else return spmm_launch_tma_cfg<V, PA, 8, S, H, 128, 6, 2>(d, p, s);
 }
 
+// n == 64, 8-bit x 8-bit, softmax value layout, half output (the attention's
+// P x V): persistent CTAs, k split over four warps (mc_spmm_n64.cuh).
+template <int V, bool S>
+int spmm_launch_n64(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
+{
+    const long long items = (long long)d.m_vec * d.batch;
+    if (items > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, spmm_n64_kernel<V, S>, 128, 0) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    long long grid = (long long)per_sm * sm_count();
+    if (grid > items) grid = items;
+    spmm_n64_kernel<V, S><<<(unsigned)grid, 128, 0, s>>>(p, (int)items);
+    return (int)cudaGetLastError();
+}
+
 // H (half output) is compiled only with the softmax value layout (E), the
 // combination the extension's batched SpMM uses; int32 output only with the
 // packer layout.
@@ -131,6 +149,11 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
         return (int)cudaGetLastError();
     } else {
         const bool f16 = resolve_mma_kind(d.mma_kind) == MC_MMA_F16;
+        if constexpr (PA == 8 && PB == 8 && H && E) {
+            if (d.n == 64 && !f16 && (d.kernel_variant == MC_KERNEL_AUTO || d.kernel_variant == MC_KERNEL_STREAM) &&
+                reinterpret_cast<uintptr_t>(d.values) % 16 == 0 && d.values_stride % 16 == 0)
+                return spmm_launch_n64<V, S>(d, p, s);
+        }
         const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
         if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)
             return fail(1, "mcSpmm: the streaming kernel needs 16-byte aligned values and values_stride");

@@ -62,8 +62,9 @@ __device__ __forceinline__ void ldsm_x2_trans_b8_a(uint32_t (&r)[4], const void*
                  : "r"(smem_u32(p)));
 }
 
+// 8 CTAs per SM: every variant fits 64 registers without spills.
 template <int V, bool ROWMAX>
-__global__ void __launch_bounds__(128) sparse_attention_kernel(const AttnParams p)
+__global__ void __launch_bounds__(128, 8) sparse_attention_kernel(const AttnParams p)
 {
     constexpr int STAGES = 2;   // per-warp V-row ring depth
     constexpr int ROW = 64;     // bytes of one int8 row of d = 64

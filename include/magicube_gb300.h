@@ -111,8 +111,12 @@ int mcSetDefaultMmaKind(int kind);
  *                    entry); any k.
  * MC_KERNEL_STREAM:  the pipelined kernels: SpMM -- persistent CTAs that
  *                    stream many vector-rows through one cp.async ring (needs
- *                    16-byte aligned values); SDDMM -- the k == 64 kernel with
- *                    a warp per 16-nonzero tile at full occupancy (needs k == 64).
+ *                    16-byte aligned values); for n == 64 with 8-bit operands,
+ *                    the softmax value layout and half output (the attention's
+ *                    P x V) one warp per vector-row with a private ring that
+ *                    carries the gathered rows and the probability chunks;
+ *                    SDDMM -- the k == 64 kernel with a warp per 16-nonzero
+ *                    tile at full occupancy (needs k == 64).
  * MC_KERNEL_TMA:     SpMM only, on the int8 path: persistent warp-specialised
  *                    CTAs -- one producer warp gathers B rows with TMA
  *                    (tile::gather4) into an mbarrier ring, consumer warps
@@ -131,7 +135,8 @@ int mcSetDefaultMmaKind(int kind);
  *                    dense tile costs less than per-nonzero gathers (about
  *                    sparsity <= 0.95 on GB300).
  * MC_KERNEL_AUTO:    SpMM: the TMA kernel where it applies, else the
- *                    streaming kernel, else per-row; SDDMM: the pipelined
+ *                    streaming kernel (the warp-per-row one for the n == 64
+ *                    attention shape), else per-row; SDDMM: the pipelined
  *                    kernel where it applies, else per-row. */
 enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2, MC_KERNEL_TMA = 3, MC_KERNEL_DENSE_TILE = 4 };
 

@@ -63,3 +63,38 @@ def test_null_pointers_rejected():
 def test_empty_matrix_is_a_no_op():
     d = _lib.McSpmmDesc(m_vec=0, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1)
     assert _lib.lib().mcSpmm(ctypes.byref(d), None) == 0
+
+
+@pytest.mark.parametrize("fields,msg", [
+    (dict(mma_kind=_lib.MMA_DP4A, lhs_bits=16, rhs_bits=8), b"dp4a"),
+    (dict(mma_kind=5), b"invalid mma_kind"),
+    (dict(kernel_variant=_lib.KERNEL_TMA), b"invalid kernel_variant"),
+    (dict(kernel_variant=5), b"invalid kernel_variant"),
+    (dict(kernel_variant=_lib.KERNEL_DENSE_TILE, lhs_bits=4, rhs_bits=4), b"L8-R8 with k == 64"),
+    (dict(kernel_variant=_lib.KERNEL_DENSE_TILE, k=128), b"L8-R8 with k == 64"),
+    (dict(kernel_variant=_lib.KERNEL_DENSE_TILE), b"tile bitmap"),
+])
+def test_sddmm_new_path_errors(fields, msg):
+    """The dp4a path and the dense-tile kernel reject what they cannot
+    compute, before any device work."""
+    d = _lib.McSddmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1, scale=1.0)
+    for k, v in fields.items():
+        setattr(d, k, v)
+    assert _lib.lib().mcSddmm(ctypes.byref(d), None) == 1
+    assert msg in _lib.lib().mcGetLastErrorString()
+
+
+def test_tile_mask_words_and_argument_errors():
+    lib = _lib.lib()
+    assert [lib.mcSddmmTileMaskWords(n) for n in (0, 1, 128, 129, 4096)] == [0, 4, 4, 8, 128]
+    assert lib.mcSddmmTileMask(4, 0, None, None, None, None, None, None) == 1
+    assert b"n > 0" in lib.mcGetLastErrorString()
+    assert lib.mcSddmmTileMask(4, 128, None, None, None, None, None, None) == 1
+    assert b"null status" in lib.mcGetLastErrorString()
+
+
+def test_check_entry_points_reject_bad_arguments():
+    lib = _lib.lib()
+    assert lib.mcCheckSmallIntConversions(0, 16, None, None) == 1
+    assert lib.mcCheckSmallIntConversions(16, 8, ctypes.c_void_p(8), None) == 1  # lo > hi
+    assert lib.mcCheckSmallIntConversions(0, 1 << 33, ctypes.c_void_p(8), None) == 1  # past 32-bit patterns

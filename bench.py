@@ -99,14 +99,37 @@ class ClockSampler:
 # workload construction
 # ----------------------------------------------------------------------------
 
-def sddmm_workload(pa: int, pb: int, batch: int, seed: int = 42, V: int = VEC, sparsity: float = SPARSITY):
-    from magicube_gb300 import formats, synth
+def sddmm_operands(pa: int, pb: int, batch: int, seed: int = 42, V: int = VEC, sparsity: float = SPARSITY):
+    """The headline SDDMM's mask (plain vector CSR) and `batch` instances of
+    packed A and B, numpy only (no library is loaded)."""
+    from magicube_gb300 import synth
     mask = synth.uniform_mask(SEQ // V, SEQ, V, sparsity, seed=seed)
-    hm = formats.prepare_sddmm(mask, alignment=8)
     rng = np.random.default_rng(seed + 1)
     lhs = rng.integers(0, 256, size=(batch, SEQ * HEAD_DIM * pa // 8), dtype=np.uint8)
     rhs = rng.integers(0, 256, size=(batch, SEQ * HEAD_DIM * pb // 8), dtype=np.uint8)
+    return mask, lhs, rhs
+
+
+def sddmm_workload(pa: int, pb: int, batch: int, seed: int = 42, V: int = VEC, sparsity: float = SPARSITY):
+    from magicube_gb300 import formats
+    mask, lhs, rhs = sddmm_operands(pa, pb, batch, seed, V, sparsity)
+    hm = formats.prepare_sddmm(mask, alignment=8)
     return mask, hm, lhs, rhs
+
+
+SPMM_M = SPMM_K = 1024
+SPMM_N = 256
+
+
+def spmm_operands():
+    """SpMM L8-R8 configuration: A 1024 x 1024 at V = 8, sparsity 0.9 (102
+    uniformly placed vectors per vector-row), values uniform int8; one value
+    set shared by the instances, numpy only."""
+    from magicube_gb300 import synth
+    mask = synth.uniform_mask(SPMM_M // VEC, SPMM_K, VEC, SPARSITY, seed=7)
+    rng = np.random.default_rng(8)
+    vals = rng.integers(0, 256, size=mask.nnz_vec * VEC, dtype=np.uint8)
+    return mask, vals, rng
 
 
 def measured_traffic_per_instance() -> float | None:
@@ -123,10 +146,13 @@ def measured_traffic_per_instance() -> float | None:
 
 
 def sddmm_bytes(hm, pa: int, pb: int, batch: int, V: int = VEC) -> tuple[float, float]:
-    """(algorithmic bytes per launch, ops per launch) of a batched SDDMM."""
+    """(algorithmic bytes per launch, ops per launch) of a batched SDDMM, on
+    the true nonzero vectors (the padding slots of the aligned layout are
+    not counted): A and B once per instance, one int32 per stored score, the
+    mask's column indices, offset pairs and row order once."""
     nnz = hm.mask.nnz_vec
-    per_inst = SEQ * HEAD_DIM * pa / 8 + SEQ * HEAD_DIM * pb / 8 + hm.aligned_nnz * V * 4
-    mask_bytes = hm.aligned_nnz * 4 + hm.mask.m_vec * 2 * 4 + hm.mask.m_vec * 4
+    per_inst = SEQ * HEAD_DIM * pa / 8 + SEQ * HEAD_DIM * pb / 8 + nnz * V * 4
+    mask_bytes = nnz * 4 + hm.mask.m_vec * 2 * 4 + hm.mask.m_vec * 4
     ops = 2.0 * nnz * V * HEAD_DIM * batch
     return per_inst * batch + mask_bytes, ops
 
@@ -149,75 +175,160 @@ def time_cuda(fn, steps: int, warmup: int, stream) -> list[float]:
 # CPU baseline (the oracle's restatement of the reference's host routine)
 # ----------------------------------------------------------------------------
 
-def cpu_sddmm_sample(hm, lhs0: np.ndarray, rhs0: np.ndarray, rows: int, threads: int = 1) -> tuple[float, float]:
-    """Time the host SDDMM routine over the first `rows` vector-rows of one
-    instance split across `threads` threads; returns (seconds, ops)."""
+class HostSddmmMask:
+    """The headline mask's aligned pairs and padded columns, built by the
+    oracle's numpy aligner: the CPU legs load no library of this package."""
+
+    def __init__(self, mask, alignment: int = 8):
+        import oracle
+        self.mask = mask
+        self.pairs, self.aligned_nnz = oracle.align_pairs(mask.row_offsets, alignment)
+        self.cols = oracle.pad_columns(mask.row_offsets, mask.col_indices, self.pairs, self.aligned_nnz)
+
+
+def cpu_sddmm(hmask: HostSddmmMask, lhs: np.ndarray, rhs: np.ndarray, instances: list[int], rows: int,
+              threads: int) -> tuple[float, float]:
+    """Time the host SDDMM routine (the oracle's restatement of
+    Host_sddmm_integers, SDDMM/SDDMM/sddmm_benchmark.cpp:24-60, signed lanes)
+    over the first `rows` vector-rows of each listed instance.  Instances are
+    dealt to `threads` workers; a single instance is split by vector-rows.
+    Each worker writes its own output buffer.  Returns (seconds, ops)."""
     import oracle
     L = oracle.lib()
-    out = np.zeros(hm.aligned_nnz * VEC, dtype=np.int32)
-    pairs = np.ascontiguousarray(hm.row_offsets)
-    cols = np.ascontiguousarray(hm.col_indices)
-    bounds = [int(x) for x in np.linspace(0, rows, threads + 1)]
+    m = hmask.mask
+    pairs, cols = hmask.pairs, hmask.cols
+    if len(instances) >= threads:
+        items = [[(i, 0, rows) for i in instances[w::threads]] for w in range(threads)]
+    else:
+        bounds = [int(x) for x in np.linspace(0, rows, threads + 1)]
+        items = [[(instances[0], bounds[w], bounds[w + 1])] for w in range(threads)]
+    outs = [np.zeros(hmask.aligned_nnz * VEC, dtype=np.int32) for _ in range(threads)]
 
-    def work(lo: int, hi: int) -> None:
-        if hi <= lo:
-            return
-        L.mco_sddmm_host(int(lhs0.ctypes.data) + lo * VEC * HEAD_DIM, int(rhs0.ctypes.data), int(out.ctypes.data),
-                         hi - lo, VEC, HEAD_DIM, SEQ, 8, 8, int(pairs.ctypes.data) + lo * 2 * 4,
-                         int(cols.ctypes.data), 8, 0, oracle.SIGNED)
+    def work(w: int) -> None:
+        for inst, lo, hi in items[w]:
+            if hi <= lo:
+                continue
+            L.mco_sddmm_host(int(lhs[inst].ctypes.data) + lo * VEC * HEAD_DIM, int(rhs[inst].ctypes.data),
+                             int(outs[w].ctypes.data), hi - lo, VEC, HEAD_DIM, SEQ, 8, 8,
+                             int(pairs.ctypes.data) + lo * 2 * 4, int(cols.ctypes.data), 8, 0, oracle.SIGNED)
 
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        for f in [ex.submit(work, bounds[i], bounds[i + 1]) for i in range(threads)]:
+        for f in [ex.submit(work, w) for w in range(threads)]:
             f.result()  # re-raises a worker's exception
     dt = time.perf_counter() - t0
-    nnz = int(sum(hm.row_offsets[2 * i + 1] - hm.row_offsets[2 * i] for i in range(rows)))
+    nnz = 0
+    for w in range(threads):
+        for _, lo, hi in items[w]:
+            nnz += int(m.row_offsets[hi] - m.row_offsets[lo])
     return dt, 2.0 * nnz * VEC * HEAD_DIM
 
 
-def cpu_baseline(steps_budget_s: float = 12.0) -> dict:
-    mask, hm, lhs, rhs = sddmm_workload(8, 8, 1)
+def cpu_spmm(mask, vals: np.ndarray, rhs: np.ndarray, threads: int) -> tuple[float, float]:
+    """Time the host SpMM routine (the oracle's restatement of
+    compute_ref_integers, SpMM/SpMM/spmm_benchmark.cpp:69-120, signed lanes)
+    on `threads` full instances of the SpMM L8-R8 configuration at once, one
+    per worker (rhs[w] is instance w's B).  Returns (seconds, ops)."""
+    import oracle
+    L = oracle.lib()
+    ro = np.ascontiguousarray(mask.row_offsets, dtype=np.int32)
+    ci = np.ascontiguousarray(mask.col_indices, dtype=np.int32)
+    outs = [np.empty((SPMM_M, SPMM_N), dtype=np.int32) for _ in range(threads)]
+
+    def work(w: int) -> None:
+        L.mco_spmm_host(int(vals.ctypes.data), int(rhs[w].ctypes.data), int(outs[w].ctypes.data), mask.m_vec, VEC,
+                        SPMM_K, SPMM_N, 8, 8, 8, int(ro.ctypes.data), int(ci.ctypes.data), oracle.SIGNED)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for f in [ex.submit(work, w) for w in range(threads)]:
+            f.result()
+    dt = time.perf_counter() - t0
+    return dt, 2.0 * mask.nnz_vec * VEC * SPMM_N * threads
+
+
+def _repeat_for(fn, budget_s: float, cap: int = 50) -> tuple[float, float, int]:
+    """Run fn() -> (seconds, ops) about `budget_s` seconds; totals and count."""
+    dt, ops = fn()
+    tot_t, tot_ops, n = dt, ops, 1
+    while tot_t < budget_s and n < cap:
+        dt, ops = fn()
+        tot_t, tot_ops, n = tot_t + dt, tot_ops + ops, n + 1
+    return tot_t, tot_ops, n
+
+
+def cpu_baseline(budget_s: float = 12.0) -> dict:
+    """The reference's CPU implementation of the path on one host core: the
+    host SDDMM routine on the headline workload (a bounded sample of its
+    vector-rows) and, beside it, the host SpMM routine on the SpMM L8-R8
+    configuration (whole instances)."""
+    mask, lhs, rhs = sddmm_operands(8, 8, 1)
+    hmask = HostSddmmMask(mask)
     rows = 64
-    dt, ops = cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, 1)
-    reps = max(1, int(steps_budget_s / max(dt, 1e-3)))
-    tot_t, tot_ops = 0.0, 0.0
-    for _ in range(min(reps, 50)):
-        dt, ops = cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, 1)
-        tot_t += dt
-        tot_ops += ops
-    return {"value": tot_ops / tot_t / 1e12, "unit": UNIT, "cores": 1, "kind": "port",
+    t, ops, n = _repeat_for(lambda: cpu_sddmm(hmask, lhs, rhs, [0], rows, 1), budget_s)
+    smask, vals, rng = spmm_operands()
+    srhs = rng.integers(0, 256, size=(1, SPMM_K * SPMM_N), dtype=np.uint8)
+    st, sops, sn = _repeat_for(lambda: cpu_spmm(smask, vals, srhs, 1), budget_s / 3)
+    return {"value": ops / t / 1e12, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"host SDDMM L8-R8 routine (oracle restatement of Host_sddmm_integers), {rows} of "
-                      f"{SEQ // VEC} vector-rows of one 4096x4096x64 V=8 s=0.9 instance, single thread"}
+                      f"{SEQ // VEC} vector-rows of one 4096x4096x64 V=8 s=0.9 instance, single thread, "
+                      f"{n} repetitions",
+            "spmm": {"value": sops / st / 1e12, "unit": UNIT, "cores": 1, "kind": "port",
+                     "sample": "host SpMM L8-R8 routine (oracle restatement of compute_ref_integers), one full "
+                               f"1024x1024x256 V=8 s=0.9 instance per repetition, {sn} repetitions, single thread",
+                     "ms_per_instance": st / sn * 1e3}}
 
 
 def run_reference(args) -> None:
+    """The reference arm: the reference's CPU implementation of the path (the
+    host SDDMM routine, restated by the oracle) on the headline workload, all
+    host cores.  Each step is the GPU arm's whole step (`--batch` instances,
+    each with its own A and B), the instances dealt to the threads.  The host
+    SpMM routine on the SpMM L8-R8 configuration is reported beside it.  No
+    library of this package is loaded."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     import oracle
     oracle.build()
     threads = os.cpu_count() or 1
-    mask, hm, lhs, rhs = sddmm_workload(8, 8, 1)
-    rows = SEQ // VEC  # one full instance per step
+    B = args.batch
+    mask, lhs, rhs = sddmm_operands(8, 8, B)
+    hmask = HostSddmmMask(mask)
+    rows = SEQ // VEC
+    inst = list(range(B))
     for _ in range(args.warmup):
-        cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, threads)
+        cpu_sddmm(hmask, lhs, rhs, inst[:threads], rows, threads)
     t, ops = 0.0, 0.0
     for _ in range(args.steps):
-        dt, o = cpu_sddmm_sample(hm, lhs[0], rhs[0], rows, threads)
+        dt, o = cpu_sddmm(hmask, lhs, rhs, inst, rows, threads)
         t += dt
         ops += o
     v = ops / t / 1e12
+    smask, vals, rng = spmm_operands()
+    srhs = rng.integers(0, 256, size=(threads, SPMM_K * SPMM_N), dtype=np.uint8)
+    st, sops, sn = _repeat_for(lambda: cpu_spmm(smask, vals, srhs, threads), 5.0, cap=10)
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int8", "data": "synthetic",
-        "config": {"workload": "SDDMM L8-R8 4096x4096x64 V=8 s=0.9 (one instance per step)"},
+        "config": headline_config(B, args.gpus),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "one full 4096x4096x64 V=8 s=0.9 SDDMM instance per step, host routine "
-                                   "(oracle restatement of Host_sddmm_integers) split by vector-rows over "
-                                   f"{threads} threads"},
+                         "sample": f"every step the whole headline step: {B} full 4096x4096x64 V=8 s=0.9 SDDMM "
+                                   "instances (own A and B each), host routine (oracle restatement of "
+                                   f"Host_sddmm_integers), instances dealt to {threads} threads"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "spmm": {"value": sops / st / 1e12, "unit": UNIT, "cores": threads, "kind": "port",
+                 "sample": f"host SpMM L8-R8 routine (oracle restatement of compute_ref_integers), {threads} full "
+                           f"1024x1024x256 V=8 s=0.9 instances at once (one per thread), {sn} repetitions"},
     }))
+
+
+def headline_config(batch: int, world: int) -> dict:
+    return {"workload": "SDDMM L8-R8: A,B 4096x64 int8, mask 4096x4096 V=8 sparsity 0.9 uniform, "
+                        "int32 out, signed lanes",
+            "instances_per_step": batch,
+            "l2": "inputs+outputs per step exceed 2x L2 (no flush)", "parallelism": f"replicas x{world}"}
 
 
 # ----------------------------------------------------------------------------
@@ -271,7 +382,23 @@ def run_gpu(args) -> None:
                 "bytes": byts, "ops": opc, "clocks": clocks, "mask": hm, "dm": dm, "lhs_h": lhs_h, "rhs_h": rhs_h,
                 "out": out, "lhs": lhs, "rhs": rhs}
 
+    def verify_sddmm(r, pa, pb, V, instances) -> bool:
+        """Untimed check of finished outputs against the oracle (bit for bit),
+        with the aligned layout rebuilt by the oracle's own aligner."""
+        import oracle
+        hm = r["mask"]
+        pairs, n_al = oracle.align_pairs(hm.mask.row_offsets, 8)
+        if n_al != hm.aligned_nnz or not np.array_equal(pairs, hm.row_offsets):
+            return False
+        for i in instances:
+            ref = oracle.sddmm_host(r["lhs_h"][i], r["rhs_h"][i], pairs, hm.col_indices, hm.mask.m_vec, V, HEAD_DIM,
+                                    SEQ, pa, pb, oracle.SIGNED)
+            if not np.array_equal(r["out"][i].cpu().numpy(), ref):
+                return False
+        return True
+
     head = sddmm_case(8, 8, timed_region_clock=True)
+    verified = verify_sddmm(head, 8, 8, VEC, [0, B - 1])
 
     # e2e through the C ABI with host buffers: H2D of the step's operands, the
     # launch, D2H of the step's outputs, all inside the timed region.
@@ -320,7 +447,8 @@ def run_gpu(args) -> None:
         for pa, pb, name, mma, var, v, sp in cases:
             r = sddmm_case(pa, pb, mma=mma, variant=var, V=v, sparsity=sp)
             variants[name] = {"tops": r["tops"], "ms": r["ms"], "gbs": r["gbs"],
-                              "hbm_frac": r["gbs"] / peaks["hbm_gbs"]}
+                              "hbm_frac": r["gbs"] / peaks["hbm_gbs"],
+                              "verified": verify_sddmm(r, pa, pb, v, [B - 1])}
             del r
             torch.cuda.empty_cache()
         for mma, var, tag in ((1, 0, MMA_NAMES[1]), (2, 0, MMA_NAMES[2]), (sync_mma, 1, "per_row_kernel")):
@@ -354,11 +482,7 @@ def run_gpu(args) -> None:
             "metric": METRIC, "value": head["tops"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": head["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int8", "data": "synthetic",
-            "config": {"workload": "SDDMM L8-R8: A,B 4096x64 int8, mask 4096x4096 V=8 sparsity 0.9 uniform, "
-                                   "int32 out, signed lanes",
-                       "tensor_path": MMA_NAMES[args.mma],
-                       "instances_per_step": B, "step_bytes": head["bytes"],
-                       "l2": "inputs+outputs per step exceed 2x L2 (no flush)", "parallelism": f"replicas x{world}"},
+            "config": headline_config(B, world),
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": gbs / peaks["hbm_gbs"],
                          "traffic": (measured_traffic_per_instance() * B
@@ -368,10 +492,14 @@ def run_gpu(args) -> None:
             # The contraction's tensor path and its measured peak: mma.sync int8
             # / f16 (probe), or tcgen05 kind::f16 (the measured dense bf16/f16
             # GEMM rate); sm_103a has no integer tcgen05.mma.
-            "tensor_roofline": {"achieved": head["tops"], "peak": tensor_peak, "unit": "TOP/s",
+            "tensor_roofline": {"tensor_path": MMA_NAMES[args.mma], "achieved": head["tops"], "peak": tensor_peak,
+                                "unit": "TOP/s",
                                 "frac": head["tops"] / tensor_peak, "peak_source": tensor_peak_source,
                                 "probe_tops": tpk},
             "e2e": e2e,
+            "verified": verified,
+            "verified_how": "instances 0 and last of the final timed step equal the oracle (host SDDMM routine "
+                            "restated, signed lanes) bit for bit",
             "gpu_launches": args.steps * launches_per_step,
             "clocks": head["clocks"],
             "variants": variants,
@@ -388,20 +516,22 @@ def run_gpu(args) -> None:
 
 
 def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma: int, variant: int = 0) -> dict:
-    """SpMM L8-R8: A 1024x1024 V=8 sparsity 0.9, B 1024x256, batched instances > 2x L2."""
+    """SpMM L8-R8: A 1024x1024 V=8 sparsity 0.9, B 1024x256, 256 instances per
+    launch (own B and C each, one value set) so a step exceeds 2x L2.
+    Algorithmic bytes on the true nonzeros: values nnz V, B K N and C M N 4 per
+    instance, column indices, offset pairs and row order once.  The first and
+    last instances are checked against the oracle after the timed loop."""
     import torch
 
-    from magicube_gb300 import formats, ops, synth
-    M = K = 1024
-    N = 256
-    B = 256
-    mask = synth.uniform_mask(M // VEC, K, VEC, SPARSITY, seed=7)
-    rng = np.random.default_rng(8)
-    vals = rng.integers(0, 256, size=mask.nnz_vec * VEC, dtype=np.uint8)
+    import oracle
+    from magicube_gb300 import formats, ops
+    M, K, N, B = SPMM_M, SPMM_K, SPMM_N, 256
+    mask, vals, rng = spmm_operands()
     h = formats.prepare_spmm(mask, vals, 8, 8)
     d = ops.DeviceSpmmLhs.from_host(h, dev)
     d.values = d.values.repeat(B)  # one value set per instance
-    rhs = torch.from_numpy(rng.integers(0, 256, size=(B, K * N), dtype=np.uint8)).to(dev)
+    rhs_h = rng.integers(0, 256, size=(B, K * N), dtype=np.uint8)
+    rhs = torch.from_numpy(rhs_h).to(dev)
     out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
     fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size, mma_kind=mma,
                           variant=variant)
@@ -410,9 +540,12 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
     sync_all()
     t = max_over_ranks(sum(ms) / 1e3) / args.steps
     opc = 2.0 * mask.nnz_vec * VEC * N * B
-    byts = B * (h.values.size + K * N + M * N * 4) + h.aligned_nnz * 4 + mask.m_vec * 12
+    byts = B * (mask.nnz_vec * VEC + K * N + M * N * 4) + mask.nnz_vec * 4 + mask.m_vec * 12
+    verified = all(np.array_equal(out[i].cpu().numpy(),
+                                  oracle.spmm_host(vals, rhs_h[i], mask.row_offsets, mask.col_indices, mask.m_vec, VEC,
+                                                   K, N, 8, 8, oracle.SIGNED)) for i in (0, B - 1))
     return {"tops": opc * world / t / 1e12, "ms": t * 1e3, "gbs": byts / t / 1e9,
-            "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"], "instances_per_step": B}
+            "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"], "instances_per_step": B, "verified": verified}
 
 
 def attention_suite(args, dev) -> dict:

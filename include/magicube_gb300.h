@@ -384,15 +384,24 @@ int mcIdentityRowSwizzle(int m_vec, int* row_indices);
 
 /* Aligned pairs (8-byte aligned device array of 2*m_vec ints) and the aligned
  * slot count (*aligned_nnz, a device int; -1 when the offsets are not
- * monotone or the count overflows int).  Scratch of 8 * ceil(m_vec / 4096) +
- * 256 bytes comes from the stream-ordered allocator and is released on the
- * stream. */
+ * monotone or the count overflows int).  Scratch of 8 * ceil(m_vec / 1024) +
+ * 256 bytes (one 8-byte sum per 1,024-row scan tile, then the flag word) comes
+ * from the stream-ordered allocator and is released on the stream. */
 int mcDeviceAlignRowOffsets(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs,
                             int* aligned_nnz, cudaStream_t stream);
 /* mcDeviceAlignRowOffsets without any allocation (no counterpart in the
- * reference): the scratch is a 128 KB file-scope device array, so at most
- * 16,744,448 vector-rows (larger m_vec is rejected with status 1).  Calls that
- * overlap on the device (concurrent streams) share that scratch and race. */
+ * reference).  For callers that may not allocate device memory at all: a
+ * serving process that reserved its whole HBM budget up front, or a host
+ * framework whose own allocator owns the device and forbids cudaMalloc and
+ * the stream-ordered pool.  The caller still passes row_offsets,
+ * aligned_pairs and aligned_nnz.  The scratch is a 128 KB file-scope device
+ * array that every GPU loading the library holds until exit, so at most
+ * 16,744,448 vector-rows (larger m_vec is rejected with status 1 before any
+ * launch).  The first call on each device looks up that array's device
+ * address (cudaGetSymbolAddress) with the device current; make that first
+ * call before any stream capture.  Every call shares the array and the flag
+ * word is cleared on each call; calls that overlap on the device (concurrent
+ * streams) race. */
 int mcDeviceAlignRowOffsetsNoAlloc(int m_vec, const int* row_offsets, int alignment, int* aligned_pairs,
                                    int* aligned_nnz, cudaStream_t stream);
 /* Column indices into the aligned slots, -1 padded, 8-shuffled if shuffle8

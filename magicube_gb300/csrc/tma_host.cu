@@ -41,11 +41,16 @@ bool encode_row_gather_u8(CUtensorMap* map, const void* base, long long rows, lo
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Device address of g_async_timeouts on the current device, looked up once
+// per device under a lock (the library assumes the primary context of a
+// device is never reset while it is loaded).
 unsigned int* async_timeout_counter()
 {
+    static std::mutex mu;
     static unsigned int* cache[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
     if (!cache[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_async_timeouts) != cudaSuccess) return nullptr;

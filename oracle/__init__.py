@@ -78,6 +78,39 @@ def sddmm_host(lhs: np.ndarray, rhs: np.ndarray, pairs: np.ndarray, cols: np.nda
     return out
 
 
+def align_pairs(row_offsets: np.ndarray, alignment: int) -> tuple[np.ndarray, int]:
+    """Aligned [start, end) pairs of a plain vector CSR, numpy only.
+
+    Restates the reference's host conversion (SpMM/SpMM/spmm_benchmark.cpp:196-206):
+    each vector-row starts at the running total of the previous rows' lengths
+    rounded up to a multiple of `alignment`; its end is start + true length.
+    Returns (pairs int32[2 m_vec], aligned slot count)."""
+    ro = np.asarray(row_offsets, dtype=np.int64)
+    lengths = np.diff(ro)
+    padded = (lengths + alignment - 1) // alignment * alignment
+    starts = np.zeros(lengths.size, dtype=np.int64)
+    if lengths.size > 1:
+        np.cumsum(padded[:-1], out=starts[1:])
+    pairs = np.empty(2 * lengths.size, dtype=np.int32)
+    pairs[0::2] = starts
+    pairs[1::2] = starts + lengths
+    return pairs, int(padded.sum())
+
+
+def pad_columns(row_offsets: np.ndarray, col_indices: np.ndarray, pairs: np.ndarray, aligned_nnz: int) -> np.ndarray:
+    """Column indices in the aligned slots, -1 in the padding slots (numpy
+    restatement of SpMM/SpMM/spmm_benchmark.cpp:209-216, without the 4-bit
+    8-shuffle)."""
+    ro = np.asarray(row_offsets, dtype=np.int64)
+    ci = np.asarray(col_indices, dtype=np.int32)
+    out = np.full(aligned_nnz, -1, dtype=np.int32)
+    lengths = np.diff(ro)
+    # destination slot of source nonzero j of row i: pairs[2 i] + (j - ro[i])
+    dst = np.repeat(np.asarray(pairs[0::2], dtype=np.int64) - ro[:-1], lengths) + np.arange(int(ro[-1]))
+    out[dst] = ci[:int(ro[-1])]
+    return out
+
+
 def spmm_device(pairs: np.ndarray, cols: np.ndarray, dev_values: np.ndarray, rhs: np.ndarray, m_vec: int,
                 V: int, K: int, N: int, preA: int, preB: int, mode: int, layout: int = 0) -> np.ndarray:
     """C (M x N int32) decoded from the SpMM device operand layout."""

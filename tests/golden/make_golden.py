@@ -1,6 +1,6 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Needs the reference checkout (default /root/reference) and builds
+Needs the reference checkout (--ref, or MAGICUBE_REFERENCE) and builds
 oracle/_ref (``make -C oracle ref``): the reference's own host benchmark
 programs and verification routines compiled from its source files against a
 host-memory fake of the CUDA runtime.  Two kinds of fixture are written:
@@ -18,7 +18,7 @@ host-memory fake of the CUDA runtime.  Two kinds of fixture are written:
   top-lane sign extension of the reference routines matters), with inputs
   and outputs.
 
-Run:  python tests/golden/make_golden.py [--ref /root/reference]
+Run:  python tests/golden/make_golden.py --ref <reference checkout>
 """
 from __future__ import annotations
 
@@ -153,8 +153,10 @@ def routine_sddmm(lib: ctypes.CDLL, bits: int, V: int, seed: int) -> dict:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("MAGICUBE_REFERENCE"))
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give --ref <reference checkout> or set MAGICUBE_REFERENCE")
     subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "all", "ref", f"REF={args.ref}"], check=True)
     rdir = ROOT / "oracle" / "_ref"
     for i, (pa, pb, V) in enumerate(SPMM_CASES):

@@ -76,3 +76,32 @@ def test_oracle_against_reference_sddmm_program(name):
     got = oracle.sddmm_host(d["lhs"], d["rhs"], pairs, d["col_indices"], mask.m_vec, V, K, N, bits, bits,
                             oracle.LITERAL)
     np.testing.assert_array_equal(got, d["out"])
+
+
+@pytest.mark.parametrize("name", names("ref_sddmm_") + [n for n in names("ref_spmm_") if "R4" not in n
+                                                        and "L4" not in n])
+def test_oracle_aligner_equals_reference_packer(name):
+    """The oracle's numpy aligner (used by the CPU baselines, which load no
+    library of this package) reproduces the reference packer's aligned pairs
+    and -1 padded columns (alignment 8 for SDDMM, 16 for 8/16-bit SpMM)."""
+    d = load(name)
+    align = 8 if name.startswith("ref_sddmm_") else 16
+    pairs, n = oracle.align_pairs(d["csr_row_offsets"], align)
+    np.testing.assert_array_equal(pairs, d["row_offsets"])
+    np.testing.assert_array_equal(oracle.pad_columns(d["csr_row_offsets"], d["csr_col_indices"], pairs, n),
+                                  d["col_indices"])
+
+
+def test_oracle_aligner_edge_rows():
+    """Empty rows, rows of exactly the alignment and an empty matrix."""
+    ro = np.array([0, 0, 8, 9, 9, 25], np.int32)
+    ci = np.arange(25, dtype=np.int32)
+    pairs, n = oracle.align_pairs(ro, 8)
+    np.testing.assert_array_equal(pairs, [0, 0, 0, 8, 8, 9, 16, 16, 16, 32])
+    assert n == 32
+    cols = oracle.pad_columns(ro, ci, pairs, n)
+    np.testing.assert_array_equal(cols[:9], np.arange(9))
+    assert (cols[9:16] == -1).all()
+    np.testing.assert_array_equal(cols[16:], np.arange(9, 25))
+    pairs0, n0 = oracle.align_pairs(np.zeros(1, np.int32), 16)
+    assert pairs0.size == 0 and n0 == 0

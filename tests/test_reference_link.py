@@ -2,8 +2,8 @@
 (SpMM/SpMM/spmm_benchmark.cpp, SDDMM/SDDMM/sddmm_benchmark.cpp), compiled from
 their unmodified sources, link against libmagicube_gb300.so in place of the
 reference's kernel sources (every spmm:: / sddmm:: symbol they call resolves
-to this library).  CPU only; skipped where the reference checkout is absent."""
-import os
+to this library).  CPU only; skipped where no reference checkout is known
+(MAGICUBE_REFERENCE, or the one recorded by the build of oracle/_ref)."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -12,7 +12,9 @@ import pytest
 
 from magicube_gb300 import build
 
-REF = Path(os.environ.get("MAGICUBE_REFERENCE", "/root/reference"))
+from oracle.reference import location
+
+REF = location() or Path("/nonexistent")
 PROGRAMS = ["SpMM/SpMM/spmm_benchmark.cpp", "SDDMM/SDDMM/sddmm_benchmark.cpp"]
 
 

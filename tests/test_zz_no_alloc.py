@@ -1,6 +1,10 @@
-"""mcDeviceAlignRowOffsetsNoAlloc (static device scratch, no allocation)
-against the allocating mcDeviceAlignRowOffsets.  The file name puts it last
-in collection order: it runs after every other test of a full run, and alone."""
+"""mcDeviceAlignRowOffsetsNoAlloc against the allocating mcDeviceAlignRowOffsets.
+
+The no-allocation entry point serves callers that may not allocate device
+memory (a server that reserved its HBM up front, a host framework whose
+allocator owns the device): its scratch is a fixed file-scope device array.
+The file name puts it last in collection order: it runs after every other
+test of a full run, and alone."""
 import ctypes
 
 import numpy as np
@@ -62,3 +66,20 @@ def test_no_alloc_align_rejects_oversize(cuda):
                                                    n.data_ptr(), None)
     assert rc == 1
     assert b"static scratch" in _lib.lib().mcGetLastErrorString()
+
+
+def test_no_alloc_align_at_the_largest_accepted_size(cuda):
+    """m_vec at the limit fills the static scratch to its last tile sum and
+    the flag word right after it; all-zero offsets give no slots.  A second
+    call of a small size right after it is still correct."""
+    ro = torch.zeros(MAX_ROWS + 1, dtype=torch.int32, device=cuda)
+    p, n = _no_alloc(ro, 16)
+    p_ref, n_ref = dfm.align_row_offsets(ro, 16)
+    torch.cuda.synchronize()
+    assert int(n.item()) == int(n_ref.item()) == 0
+    assert torch.equal(p, p_ref)
+    del ro, p, p_ref
+    ro = torch.tensor([0, 3, 3, 20], dtype=torch.int32, device=cuda)
+    p, n = _no_alloc(ro, 8)
+    p_ref, n_ref = dfm.align_row_offsets(ro, 8)
+    assert torch.equal(p, p_ref) and int(n.item()) == int(n_ref.item()) == 32

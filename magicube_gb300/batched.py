@@ -119,6 +119,7 @@ class _AttentionCore:
         self.score_div = float(np.float32(np.float32(scale_qkv ** 2) / np.float32(self.scaling)))
         self.sddmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO, "row_split": 0}
         self.spmm_cfg = {"mma_kind": _lib.MMA_INT8, "variant": _lib.KERNEL_AUTO}
+        self.fused_cfg: dict = {}
         self._tune = tune
 
     # -- the four steps -----------------------------------------------------
@@ -256,7 +257,10 @@ class BatchedSparseAttention:
 
 
 class PerInstanceSparseAttention:
-    """The plain baseline: the same steps launched separately per instance."""
+    """The plain baseline: the same steps launched separately per instance,
+    either from the host (`__call__`) or replayed from one CUDA graph that
+    holds every instance's launches (`capture` / `replay`: the same kernels
+    without the host's per-launch cost)."""
 
     def __init__(self, masks: list[VectorSparse], heads: int, head_dim: int = 64, lhs_bits: int = 8,
                  rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 32.0, device="cuda",
@@ -268,3 +272,21 @@ class PerInstanceSparseAttention:
 
     def __call__(self, qkvs: list[torch.Tensor]) -> list[torch.Tensor]:
         return [c.run(x) for c, x in zip(self.cores, qkvs)]
+
+    def capture(self, qkvs: list[torch.Tensor]) -> "PerInstanceSparseAttention":
+        """Capture every instance's launches on these inputs in one CUDA graph."""
+        self(qkvs)  # warm up outside the capture
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self(qkvs)
+        torch.cuda.current_stream().wait_stream(s)
+        self._graph = g
+        return self
+
+    def replay(self) -> list[torch.Tensor]:
+        self._graph.replay()
+        return [c.out for c in self.cores]

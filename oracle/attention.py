@@ -115,3 +115,26 @@ def sparse_attention_fp64(q: np.ndarray, k: np.ndarray, v: np.ndarray, mask: np.
     den = p.sum(axis=-1, keepdims=True)
     p = np.where(den > 0, p / np.where(den > 0, den, 1.0), 0.0)
     return np.einsum("hlm,hmd->hld", p, v)
+
+
+def sparse_attention_fp64_rows(q: np.ndarray, k: np.ndarray, v: np.ndarray, row_offsets: np.ndarray,
+                               col_indices: np.ndarray, V: int, scaling: float) -> np.ndarray:
+    """The same unquantized attention as sparse_attention_fp64, computed
+    vector-row by vector-row on the gathered K and V rows of the row's
+    columns (no dense L x L scores).  q, k, v: [H, L, d]; row_offsets /
+    col_indices: the plain vector CSR (m_vec + 1 offsets).  Rows without
+    nonzeros give 0."""
+    q, k, v = (np.asarray(a, dtype=np.float64) for a in (q, k, v))
+    H, L, d = q.shape
+    out = np.zeros((H, L, d), dtype=np.float64)
+    m_vec = len(row_offsets) - 1
+    for i in range(m_vec):
+        c = col_indices[int(row_offsets[i]):int(row_offsets[i + 1])]
+        if c.size == 0:
+            continue
+        s = np.matmul(q[:, i * V:(i + 1) * V, :], k[:, c, :].transpose(0, 2, 1)) * scaling  # [H, V, n]
+        s -= s.max(axis=-1, keepdims=True)
+        p = np.exp(s)
+        p /= p.sum(axis=-1, keepdims=True)
+        out[:, i * V:(i + 1) * V, :] = np.matmul(p, v[:, c, :])
+    return out

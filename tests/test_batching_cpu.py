@@ -50,3 +50,22 @@ def test_footprint_grows_with_batch():
     f1 = serving.footprint_bytes(reqs[:1], 64, 4, 2, 8)
     f3 = serving.footprint_bytes(reqs, 64, 4, 2, 8)
     assert 0 < f1 < f3
+
+
+def test_rowwise_fp64_attention_equals_dense_fp64():
+    """The vector-row-wise float64 attention oracle (gathered K and V rows)
+    equals the dense-mask form, including a row without nonzeros."""
+    import oracle
+    from oracle import attention as oa
+    m = synth.band_random_mask(256, 8, 64, 0.8, seed=3)
+    ro = m.row_offsets.copy()
+    ro[5:] -= ro[5] - ro[4]  # vector-row 4 left empty
+    cols = np.concatenate([m.col_indices[:ro[4]], m.col_indices[m.row_offsets[5]:]])
+    rng = np.random.default_rng(0)
+    q, k, v = (rng.standard_normal((2, 256, 64)) for _ in range(3))
+    pairs, n = oracle.align_pairs(ro, 16)
+    mk = oa.dense_mask(pairs, oracle.pad_columns(ro, cols, pairs, n), m.m_vec, 8, 256)
+    a = oa.sparse_attention_fp64(q, k, v, mk, 0.125)
+    b = oa.sparse_attention_fp64_rows(q, k, v, ro, cols, 8, 0.125)
+    np.testing.assert_allclose(b, a, rtol=0, atol=1e-12)
+    assert not b[:, 32:40].any()

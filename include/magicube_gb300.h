@@ -290,9 +290,13 @@ int mcCheckSmallIntConversions(unsigned long long lo, unsigned long long hi, voi
 
 /* mcSparseAttention: the quantized sparse attention of every vector-row and
  * head in one persistent kernel (SDDMM, softmax + requantization, SpMM with
- * scores and probabilities kept on chip).  q, k, v: int8 [heads][tokens][64]
- * (mcQuantize output), out: half [heads][tokens][64]; the mask in the
- * attention layout (rows aligned to 16, columns unshuffled).
+ * scores and probabilities kept on chip); the reference composes it from
+ * batched_deq_sddmm, csrSoftmaxKernel_ and batched_deq_spmm launches
+ * (spattention.py:189-216).  Precision pairs (lhs_bits = probabilities,
+ * rhs_bits = Q / K / V): L8-R8, L16-R8 (fixed requantization only) and L8-R4.
+ * q, k, v: [heads][tokens][64] packed int8 or int4 (mcQuantize output), out:
+ * half [heads][tokens][64]; the mask in the attention layout (columns
+ * unshuffled).
  *   MC_REQUANT_FIXED:  s = half(acc / score_scale) * scaling,
  *                      q = trunc(clamp(exp(s - max) * (prob_scale / sum))),
  *                      out = half(acc / out_scale) -- bit-identical to
@@ -320,6 +324,10 @@ typedef struct mcAttnDesc {
     void* out;
     long long out_head_stride;  /* halves between heads of out */
     int* status;                /* optional device int */
+    /* launch configuration (0 = default; every choice gives the same bits):
+     * warps per CTA 4 or 8 (the k-split of P x V), cp.async ring stages per
+     * warp 2 or 3, at most ctas_per_sm resident CTAs per SM */
+    int warps, stages, ctas_per_sm;
 } mcAttnDesc;
 int mcSparseAttention(const mcAttnDesc* desc, cudaStream_t stream);
 

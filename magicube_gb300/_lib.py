@@ -62,6 +62,7 @@ class McAttnDesc(ctypes.Structure):
         ("row_indices", _c_vp), ("row_offsets", _c_vp), ("column_indices", _c_vp),
         ("q", _c_vp), ("k", _c_vp), ("v", _c_vp), ("head_stride", _c_ll),
         ("out", _c_vp), ("out_head_stride", _c_ll), ("status", _c_vp),
+        ("warps", _c_int), ("stages", _c_int), ("ctas_per_sm", _c_int),
     ]
 
 

@@ -4,8 +4,9 @@ For a problem signature (operation, precision pair, V, dense width, row-length
 and row-count buckets, batch bucket) it times every candidate configuration on
 the caller's own buffers -- tensor path (int8 or exact f16), kernel variant
 (per-row, pipelined/streaming, or for SpMM the TMA-gather kernel where it
-applies), and for SDDMM the number of CTAs per
-vector-row -- and keeps the fastest.  Results persist in a JSON cache
+applies), for SDDMM the number of CTAs per vector-row, and for the fused
+attention kernel the warps per CTA, ring stages and CTAs per SM -- and keeps
+the fastest.  Results persist in a JSON cache
 (``$MC_AUTOTUNE_CACHE``, default ``~/.cache/magicube_gb300/autotune.json``) so
 a shape bucket is tuned once per machine.  Every candidate computes the same
 integers; the choice only affects speed.
@@ -80,6 +81,13 @@ def sddmm_candidates(k: int, bits: int = 8) -> list[dict]:
             if k == 64:
                 out.append({"mma_kind": m, "variant": _lib.KERNEL_STREAM, "row_split": split})
     return out
+
+
+def fused_attention_candidates() -> list[dict]:
+    """Launch configurations of the fused attention kernel: warps per CTA
+    (the k-split of P x V across warps), cp.async ring stages per warp, and a
+    cap on resident CTAs per SM (0: as many as fit)."""
+    return [{"warps": w, "stages": st, "ctas_per_sm": c} for w in (4, 8) for st in (2, 3) for c in (0, 2, 4)]
 
 
 def _time(fn: Callable[[], None], reps: int) -> float:

@@ -30,6 +30,10 @@ from . import _lib, autotune, formats
 from .formats import VectorSparse
 
 
+# (probability bits, Q/K/V bits) of the fused attention kernel
+FUSED_PAIRS = ((8, 8), (16, 8), (8, 4))
+
+
 @dataclass
 class AttentionMaskDev:
     m_vec: int
@@ -90,8 +94,8 @@ class _AttentionCore:
                  requant: str = "fixed"):
         self.fused = fused
         self.requant = _lib.REQUANT_ROWMAX if requant == "rowmax" else _lib.REQUANT_FIXED
-        if fused and (lhs_bits, rhs_bits, head_dim) != (8, 8, 64):
-            raise ValueError("the fused attention kernel computes L8-R8 with head_dim 64")
+        if fused and ((lhs_bits, rhs_bits) not in FUSED_PAIRS or head_dim != 64):
+            raise ValueError("the fused attention kernel computes L8-R8, L16-R8 and L8-R4 with head_dim 64")
         if requant not in ("fixed", "rowmax"):
             raise ValueError("requant must be 'fixed' or 'rowmax'")
         if requant == "rowmax" and lhs_bits != 8:
@@ -180,8 +184,20 @@ class _AttentionCore:
         sig = autotune.signature("spmm_attn", self.lb, self.rb, m.vec_length, self.d, m.m_vec, avg, self.H)
         self.spmm_cfg = autotune.tune(sig, autotune.spmm_candidates(), lambda c: self._spmm(c, stream))
 
-    def _fused(self, stream) -> None:
+    def tune_fused(self, qkv: torch.Tensor) -> None:
+        """Pick the fused kernel's launch configuration (warps per CTA = the
+        k-split of P x V, ring stages, CTAs per SM) with the autotuner."""
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         m = self.m
+        avg = m.aligned_nnz / max(1, m.m_vec)
+        self._quantize(qkv, stream)
+        sig = autotune.signature(f"attn_fused_{'rowmax' if self.requant else 'fixed'}", self.lb, self.rb,
+                                 m.vec_length, self.d, m.m_vec, avg, self.H)
+        self.fused_cfg = autotune.tune(sig, autotune.fused_attention_candidates(), lambda c: self._fused(stream, c))
+
+    def _fused(self, stream, cfg: dict | None = None) -> None:
+        m = self.m
+        cfg = self.fused_cfg if cfg is None else cfg
         d = _lib.McAttnDesc(
             m_vec=m.m_vec, vec_length=m.vec_length, heads=self.H, head_dim=self.d, max_row_nnz=m.max_row_nnz,
             lhs_bits=self.lb, rhs_bits=self.rb, requant=self.requant, score_scale=float(self.scale_qkv ** 2),
@@ -191,13 +207,17 @@ class _AttentionCore:
             row_indices=m.row_indices.data_ptr(), row_offsets=m.row_offsets.data_ptr(),
             column_indices=m.col_indices.data_ptr(), q=self.qkv_q[0].data_ptr(), k=self.qkv_q[1].data_ptr(),
             v=self.qkv_q[2].data_ptr(), head_stride=self.q_words * 4, out=self.out.data_ptr(),
-            out_head_stride=m.seq_len * self.d, status=self.status.data_ptr())
+            out_head_stride=m.seq_len * self.d, status=self.status.data_ptr(), warps=cfg.get("warps", 0),
+            stages=cfg.get("stages", 0), ctas_per_sm=cfg.get("ctas_per_sm", 0))
         _lib.check(_lib.lib().mcSparseAttention(ctypes.byref(d), stream), "mcSparseAttention")
 
     def run(self, qkv: torch.Tensor) -> torch.Tensor:
         """qkv: [3, H, L, d] half (contiguous) -> [H, L, d] half."""
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         if self.fused:
+            if self._tune:
+                self.tune_fused(qkv)
+                self._tune = False
             self._quantize(qkv, stream)
             self._fused(stream)
             return self.out

@@ -18,7 +18,7 @@ import torch.nn as nn
 import torch.nn.functional as F
 
 from . import _lib
-from .batched import AttentionMaskDev
+from .batched import FUSED_PAIRS, AttentionMaskDev
 from .projection import qkv_project_quantize
 
 
@@ -91,22 +91,27 @@ def attention_core_quantized(qkv_q: torch.Tensor, T: int, mask: AttentionMaskDev
 
 
 def attention_fused_quantized(qkv_q: torch.Tensor, T: int, mask: AttentionMaskDev, scale_qkv: float,
-                              scale_sfmx: float, requant: str = "fixed") -> torch.Tensor:
-    """qkv_q: [3, H, T*64/4] int32 (int8 Q, K, V, head_dim 64) -> [H, T, 64]
-    half through the fused attention kernel (mcSparseAttention): the same
-    bits as attention_core_quantized with the same requant mode."""
+                              scale_sfmx: float, requant: str = "fixed", lhs_bits: int = 8, rhs_bits: int = 8,
+                              fused_cfg: dict | None = None) -> torch.Tensor:
+    """qkv_q: [3, H, T*64*rhs_bits/32] int32 (int8 or int4 Q, K, V, head_dim
+    64) -> [H, T, 64] half through the fused attention kernel
+    (mcSparseAttention; pairs L8-R8, L16-R8, L8-R4): the same bits as
+    attention_core_quantized with the same requant mode."""
     H, d = qkv_q.shape[1], 64
-    q_words = T * d // 4
+    q_words = T * d * rhs_bits // 32
+    fc = fused_cfg or {}
     out = torch.empty((H, T, d), dtype=torch.float16, device=qkv_q.device)
     rowmax = requant == "rowmax"
     desc = _lib.McAttnDesc(
-        m_vec=mask.m_vec, vec_length=mask.vec_length, heads=H, head_dim=d, max_row_nnz=mask.max_row_nnz, lhs_bits=8,
-        rhs_bits=8, requant=_lib.REQUANT_ROWMAX if rowmax else _lib.REQUANT_FIXED, score_scale=float(scale_qkv ** 2),
+        m_vec=mask.m_vec, vec_length=mask.vec_length, heads=H, head_dim=d, max_row_nnz=mask.max_row_nnz,
+        lhs_bits=lhs_bits, rhs_bits=rhs_bits, requant=_lib.REQUANT_ROWMAX if rowmax else _lib.REQUANT_FIXED,
+        score_scale=float(scale_qkv ** 2),
         scaling=float(d ** -0.5), prob_scale=float(scale_sfmx),
         out_scale=float(scale_qkv) if rowmax else float(scale_qkv * scale_sfmx),
         row_indices=mask.row_indices.data_ptr(), row_offsets=mask.row_offsets.data_ptr(),
         column_indices=mask.col_indices.data_ptr(), q=qkv_q[0].data_ptr(), k=qkv_q[1].data_ptr(),
-        v=qkv_q[2].data_ptr(), head_stride=q_words * 4, out=out.data_ptr(), out_head_stride=T * d, status=None)
+        v=qkv_q[2].data_ptr(), head_stride=q_words * 4, out=out.data_ptr(), out_head_stride=T * d, status=None,
+        warps=fc.get("warps", 0), stages=fc.get("stages", 0), ctas_per_sm=fc.get("ctas_per_sm", 0))
     _lib.check(_lib.lib().mcSparseAttention(ctypes.byref(desc), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                "mcSparseAttention")
     return out
@@ -131,9 +136,11 @@ class SparseEncoderLayer(nn.Module):
         self.linear2 = nn.Linear(ffn, hidden)
         self.sddmm_cfg: dict | None = None
         self.spmm_cfg: dict | None = None
+        self.fused_cfg: dict | None = None  # launch configuration of the fused kernel (autotuner's choice)
         # attention kernels: "separate" (SDDMM, softmax, SpMM launches) or
-        # "fused" (mcSparseAttention, int8 with head_dim 64 and rows of at
-        # most 4096 nonzero vectors; otherwise the separate launches run);
+        # "fused" (mcSparseAttention: L8-R8, L16-R8 or L8-R4 with head_dim 64
+        # and rows of at most 4096 nonzero vectors; otherwise the separate
+        # launches run);
         # requant "fixed" (the reference's scales) or "rowmax"
         self.attention = "separate"
         self.requant = "fixed"
@@ -142,8 +149,8 @@ class SparseEncoderLayer(nn.Module):
         self.fused_projection = hidden % 64 == 0 and 64 <= hidden <= 256 and self.head_dim % 64 == 0
 
     def _fused_ok(self, mask: AttentionMaskDev) -> bool:
-        return (self.attention == "fused" and self.lhs_bits == 8 and self.rhs_bits == 8 and self.head_dim == 64
-                and 0 < mask.max_row_nnz <= 4096)
+        return (self.attention == "fused" and (self.lhs_bits, self.rhs_bits) in FUSED_PAIRS and self.head_dim == 64
+                and (self.requant == "fixed" or self.lhs_bits == 8) and 0 < mask.max_row_nnz <= 4096)
 
     def forward(self, x: torch.Tensor, mask: AttentionMaskDev) -> torch.Tensor:
         """x: [T, hidden] half (sequences back to back) -> [T, hidden]."""
@@ -153,7 +160,8 @@ class SparseEncoderLayer(nn.Module):
             qkv_q = qkv_project_quantize(h, self.in_proj.weight, self.in_proj.bias, self.heads, self.rhs_bits,
                                          self.scale_qkv)
             if self._fused_ok(mask):
-                att = attention_fused_quantized(qkv_q, T, mask, self.scale_qkv, self.scale_sfmx, self.requant)
+                att = attention_fused_quantized(qkv_q, T, mask, self.scale_qkv, self.scale_sfmx, self.requant,
+                                                self.lhs_bits, self.rhs_bits, self.fused_cfg)
             else:
                 att = attention_core_quantized(qkv_q, T, mask, self.head_dim, self.lhs_bits, self.rhs_bits,
                                                self.scale_qkv, self.scale_sfmx, self.sddmm_cfg, self.spmm_cfg,

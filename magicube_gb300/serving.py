@@ -40,6 +40,7 @@ class Request:
     t_admit: float = float("nan")
     t_done: float = float("nan")
     dev: dict = field(default_factory=dict)
+    error: str | None = None         # set when the request was rejected at admission
 
     @property
     def latency(self) -> float:
@@ -187,6 +188,9 @@ class ContinuousBatchingServer:
         self.device = torch.device(device)
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
         self.batches: list[list[int]] = []
+        self.peak_inflight = 0        # most batches on the device at once
+        self.held_back = 0            # admissions deferred because the batch did not fit the free HBM
+        self.rejected: list[int] = []  # requests that cannot fit even alone on an idle device
 
     def _fits(self, reqs: list[Request]) -> bool:
         free, _ = torch.cuda.mem_get_info(self.device)
@@ -196,6 +200,7 @@ class ContinuousBatchingServer:
         pending = deque(sorted(requests, key=lambda r: r.arrival))
         queue: deque[Request] = deque()
         inflight: list[tuple[torch.cuda.Event, list[Request], int]] = []
+        self.inflight = inflight
         free_streams = list(range(self.max_inflight))
         done = 0
         t0 = time.perf_counter()
@@ -217,10 +222,12 @@ class ContinuousBatchingServer:
                         free_streams.append(si)
                     else:
                         still.append((ev, batch, si))
-                inflight = still
+                inflight[:] = still
                 # admission of a new batch: as many queued requests as the
-                # token budget and the free HBM allow (the first one always,
-                # when nothing else is on the device)
+                # token budget and the free HBM allow.  A request that does
+                # not fit even alone on an idle device is rejected instead of
+                # launched; one that does not fit next to the batches in
+                # flight waits for them.
                 queued_tokens = sum(r.seq_len for r in queue)
                 if queue and free_streams and (not inflight or queued_tokens >= self.overlap_tokens):
                     batch, tokens = [], 0
@@ -228,7 +235,15 @@ class ContinuousBatchingServer:
                         r = queue[0]
                         if batch and tokens + r.seq_len > self.max_batch_tokens:
                             break
-                        if (batch or inflight) and not self._fits(batch + [r]):
+                        if not self._fits(batch + [r]):
+                            if not batch and not inflight:
+                                queue.popleft()
+                                r.error = "does not fit the free device memory"
+                                r.t_done = time.perf_counter() - t0
+                                self.rejected.append(r.rid)
+                                done += 1
+                                continue
+                            self.held_back += 1
                             break
                         batch.append(queue.popleft())
                         tokens += r.seq_len
@@ -249,6 +264,7 @@ class ContinuousBatchingServer:
                             ev = torch.cuda.Event()
                             ev.record(s)
                         inflight.append((ev, batch, si))
+                        self.peak_inflight = max(self.peak_inflight, len(inflight))
                         self.batches.append([r.rid for r in batch])
                         continue
                 if not inflight and not queue and pending:
@@ -278,7 +294,11 @@ def serve_sequential(model, requests: list[Request], V: int = 8, rhs_bits: int =
 
 
 def summarize(requests: list[Request], makespan: float) -> dict:
-    lat = np.array([r.latency for r in requests]) * 1e3
-    return {"requests": len(requests), "makespan_s": makespan, "req_per_s": len(requests) / makespan,
+    """Throughput and latency percentiles over the served requests (rejected
+    ones are counted apart)."""
+    served = [r for r in requests if r.error is None]
+    lat = np.array([r.latency for r in served]) * 1e3 if served else np.zeros(1)
+    return {"requests": len(served), "rejected": len(requests) - len(served), "makespan_s": makespan,
+            "req_per_s": len(served) / makespan,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_ms": float(lat.mean()), "tokens": int(sum(r.seq_len for r in requests))}
+            "mean_ms": float(lat.mean()), "tokens": int(sum(r.seq_len for r in served))}

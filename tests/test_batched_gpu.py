@@ -240,3 +240,96 @@ def test_device_packed_request_masks_equal_host_packed(cuda):
         b = enc(x, host_masks)
     torch.cuda.synchronize()
     assert torch.equal(a, b)
+
+
+FUSED_CFGS = [{"warps": w, "stages": st, "ctas_per_sm": c} for w in (4, 8) for st in (2, 3) for c in (0, 3)]
+PAIR_SCALES = {(8, 8): (60.0, 100.0), (16, 8): (60.0, 32767.0), (8, 4): (3.0, 100.0)}
+
+
+@pytest.mark.parametrize("pair", [(8, 8), (16, 8), (8, 4)])
+@pytest.mark.parametrize("V", [2, 4, 8])
+def test_fused_fixed_every_pair_and_config_equals_separate(cuda, pair, V):
+    """Every precision pair of the fused kernel, in every launch
+    configuration the autotuner chooses from (warps per CTA = k-split,
+    ring stages, CTAs per SM), reproduces the separate SDDMM -> softmax ->
+    SpMM launches of the same pair bit for bit."""
+    lb, rb = pair
+    sq, ss = PAIR_SCALES[pair]
+    lens = [64, 512, 128, 1024, 192]
+    masks = [synth.band_random_mask(L, V, 64, 0.8, seed=70 + i) for i, L in enumerate(lens)]
+    H, d = 2, 64
+    qkv = (torch.randn(3, H, sum(lens), d, generator=torch.Generator().manual_seed(7)) * 0.5).half().to(cuda)
+    sep = batched.BatchedSparseAttention(masks, H, d, lb, rb, scale_qkv=sq, scale_sfmx=ss, device=cuda, tune=False)
+    a = sep(qkv).clone()
+    fus = batched.BatchedSparseAttention(masks, H, d, lb, rb, scale_qkv=sq, scale_sfmx=ss, device=cuda, fused=True,
+                                         tune=False)
+    for cfg in FUSED_CFGS:
+        fus.core.fused_cfg = cfg
+        fus.core.out.fill_(1000.0)
+        b = fus(qkv).clone()
+        torch.cuda.synchronize()
+        assert int(fus.core.status.item()) == 0
+        assert torch.equal(a, b), cfg
+
+
+@pytest.mark.parametrize("pair", [(8, 8), (8, 4)])
+@pytest.mark.parametrize("V", [2, 8])
+def test_fused_rowmax_every_config_equals_separate(cuda, pair, V):
+    lb, rb = pair
+    lens = [64, 512, 128, 1024, 192]
+    masks = [synth.band_random_mask(L, V, 64, 0.8, seed=90 + i) for i, L in enumerate(lens)]
+    H, d = 2, 64
+    qkv = (torch.randn(3, H, sum(lens), d, generator=torch.Generator().manual_seed(9)) * 0.5).half().to(cuda)
+    kw = dict(scale_qkv=PAIR_SCALES[pair][0], scale_sfmx=127.0, device=cuda, requant="rowmax", tune=False)
+    sep = batched.BatchedSparseAttention(masks, H, d, lb, rb, **kw)
+    a = sep(qkv).clone()
+    fus = batched.BatchedSparseAttention(masks, H, d, lb, rb, fused=True, **kw)
+    assert torch.isfinite(a).all()
+    for cfg in FUSED_CFGS:
+        fus.core.fused_cfg = cfg
+        fus.core.out.fill_(1000.0)
+        b = fus(qkv).clone()
+        torch.cuda.synchronize()
+        assert torch.equal(a, b), cfg
+
+
+def test_fused_autotuned_configuration_is_used(cuda, tmp_path, monkeypatch):
+    """With tuning on, the fused kernel's configuration comes from the
+    autotuner's candidates, is cached, and the tuned launch keeps the bits."""
+    from magicube_gb300 import autotune
+    monkeypatch.setenv("MC_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_cache", None)
+    lens = [256, 768]
+    masks = [synth.band_random_mask(L, 8, 64, 0.8, seed=80 + i) for i, L in enumerate(lens)]
+    qkv = (torch.randn(3, 2, sum(lens), 64, generator=torch.Generator().manual_seed(8)) * 0.5).half().to(cuda)
+    sep = batched.BatchedSparseAttention(masks, 2, 64, 16, 8, scale_qkv=60.0, scale_sfmx=32767.0, device=cuda,
+                                         tune=False)
+    fus = batched.BatchedSparseAttention(masks, 2, 64, 16, 8, scale_qkv=60.0, scale_sfmx=32767.0, device=cuda,
+                                         fused=True, tune=True)
+    a = sep(qkv).clone()
+    b = fus(qkv).clone()
+    assert fus.core.fused_cfg in autotune.fused_attention_candidates()
+    assert torch.equal(a, b)
+    assert any(k.split("|")[1].startswith("attn_fused") for k in autotune._load())
+
+
+def test_fused_L16R8_error_vs_fp64(cuda):
+    """16-bit probabilities at the full output range: the attention error
+    against the float64 unquantized attention."""
+    import oracle.attention as oatt
+    lens = [256, 512]
+    masks = [synth.band_random_mask(L, 8, 128, 0.8, seed=40 + i) for i, L in enumerate(lens)]
+    H, d = 2, 64
+    qkv_h = (torch.randn(3, H, sum(lens), d, generator=torch.Generator().manual_seed(4)) * 0.5).half()
+    sq = 127.0 / float(qkv_h.abs().max())
+    fus = batched.BatchedSparseAttention(masks, H, d, 16, 8, scale_qkv=sq, scale_sfmx=32767.0, device=cuda,
+                                         fused=True, tune=False)
+    fus(qkv_h.to(cuda))
+    torch.cuda.synchronize()
+    for i, m in enumerate(masks):
+        a, z = int(fus.token_offsets[i]), int(fus.token_offsets[i + 1])
+        q, k, v = (qkv_h[j, :, a:z].double().numpy() for j in range(3))
+        ref = oatt.sparse_attention_fp64_rows(q, k, v, m.row_offsets, m.col_indices, 8, d ** -0.5)
+        got = fus.instance_output(i).double().cpu().numpy()
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err < 0.05, err

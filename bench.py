@@ -454,6 +454,14 @@ def run_gpu(args) -> None:
         for mma, var, tag in ((1, 0, MMA_NAMES[1]), (2, 0, MMA_NAMES[2]), (sync_mma, 1, "per_row_kernel")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
+        # small vectors: an int8 MMA computes 8 vector lanes of which V are
+        # used; the dp4a consumers compute only the V lanes
+        for v in (2, 4):
+            for pa, pb in ((8, 8), (8, 4), (4, 4)):
+                for mma in (1, 4):
+                    variants[f"spmm_L{pa}R{pb}_4096x4096x256_V{v}_s0.9_{MMA_NAMES[mma]}"] = spmm_point(
+                        args, dev, stream, peaks, 4096, 4096, 256, v, pa, pb, mma)
+                    torch.cuda.empty_cache()
     attention = serving_res = packer = projection = competitors = None
     if not args.headline_only and rank == 0:
         torch.cuda.empty_cache()
@@ -546,6 +554,38 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
                                                    K, N, 8, 8, oracle.SIGNED)) for i in (0, B - 1))
     return {"tops": opc * world / t / 1e12, "ms": t * 1e3, "gbs": byts / t / 1e9,
             "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"], "instances_per_step": B, "verified": verified}
+
+
+def spmm_point(args, dev, stream, peaks, M: int, K: int, N: int, V: int, pa: int, pb: int, mma: int,
+               sparsity: float = SPARSITY, seed: int = 17) -> dict:
+    """One SpMM point of the precision/shape sweep (row lengths normal, cv
+    0.3): enough instances per launch that a step moves more than 2.5x L2,
+    median of `--steps` CUDA-event timings; the last instance is checked
+    against the oracle.  Algorithmic bytes as in the sweep."""
+    import torch
+
+    import oracle
+    from magicube_gb300 import formats, ops, synth
+    mask = synth.normal_mask(M // V, K, V, sparsity, cv=0.3, seed=seed)
+    vals = synth.random_bytes(mask.nnz_vec * V * pa // 8, seed + 1)
+    h = formats.prepare_spmm(mask, vals, pa, pb)
+    l2 = int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0)) or 129 * 2 ** 20
+    per_inst = h.values.size + K * N * pb // 8 + M * N * 4
+    B = max(1, min(1024, -(-int(2.5 * l2) // per_inst)))
+    d = ops.DeviceSpmmLhs.from_host(h, dev)
+    d.values = d.values.repeat(B)
+    rhs_h = synth.random_bytes(B * K * N * pb // 8, seed + 2).reshape(B, -1)
+    rhs = torch.from_numpy(rhs_h).to(dev)
+    out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
+    fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size,  # noqa: E731
+                          mma_kind=mma)
+    t = statistics.median(time_cuda(fn, args.steps, args.warmup, stream)) / 1e3
+    opc = 2.0 * mask.nnz_vec * V * N * B
+    byts = B * (mask.nnz_vec * V * pa / 8 + K * N * pb / 8 + M * N * 4) + 4 * mask.nnz_vec + 4 * (mask.m_vec + 1)
+    ref = oracle.spmm_host(vals, rhs_h[B - 1], mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
+                           oracle.SIGNED)
+    return {"tops": opc / t / 1e12, "ms": t * 1e3, "gbs": byts / t / 1e9, "hbm_frac": byts / t / 1e9 / peaks["hbm_gbs"],
+            "instances_per_step": B, "verified": bool(np.array_equal(out[B - 1].cpu().numpy(), ref))}
 
 
 def attention_suite(args, dev) -> dict:

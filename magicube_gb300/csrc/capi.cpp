@@ -51,8 +51,10 @@ static int check_spmm(const mcSpmmDesc& d)
     if (d.row_div && !d.out_half) return fail(1, "mcSpmm: row divisors apply to half output only");
     if (d.row_div && (reinterpret_cast<uintptr_t>(d.row_div) % 4 || (d.batch > 1 && d.row_div_stride < 0)))
         return fail(1, "mcSpmm: row_div must be 4-byte aligned with a non-negative stride");
-    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_F16)
-        return fail(1, "mcSpmm: invalid mma_kind (the SpMM runs on MC_MMA_INT8 or MC_MMA_F16)");
+    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_DP4A || d.mma_kind == MC_MMA_TCGEN05)
+        return fail(1, "mcSpmm: invalid mma_kind (the SpMM runs on MC_MMA_INT8, MC_MMA_F16 or MC_MMA_DP4A)");
+    if (d.mma_kind == MC_MMA_DP4A && (d.lhs_bits > 8 || d.rhs_bits > 8 || d.vec_length > 4))
+        return fail(1, "mcSpmm: the dp4a SpMM computes V = 2 and 4 with 8-bit or 4-bit operands");
     if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_TMA)
         return fail(1, "mcSpmm: invalid kernel_variant");
     if (d.m_vec == 0) return 0;

@@ -50,7 +50,8 @@ int spmm_launch_stream(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 // of B a whole number of rows apart.
 inline bool spmm_tma_eligible(const mcSpmmDesc& d)
 {
-    if (resolve_mma_kind(d.mma_kind) != MC_MMA_INT8) return false;
+    const int kind = resolve_mma_kind(d.mma_kind);
+    if (kind != MC_MMA_INT8 && kind != MC_MMA_DP4A) return false;
     if (!((d.rhs_bits == 8 && d.n % 128 == 0) || (d.rhs_bits == 4 && d.n % 256 == 0))) return false;
     if (reinterpret_cast<uintptr_t>(d.values) % 16 || d.values_stride % 16) return false;
     if (reinterpret_cast<uintptr_t>(d.rhs) % 16) return false;
@@ -60,7 +61,7 @@ inline bool spmm_tma_eligible(const mcSpmmDesc& d)
     return per_entry * (d.batch - 1) + d.k <= 0x7fffffffLL;
 }
 
-template <int V, int PA, int PB, bool S, bool H, int NT, int STAGES = 4, int CW = 4>
+template <int V, int PA, int PB, bool S, bool H, int NT, int STAGES = 4, int CW = 4, bool DP4A = false>
 int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
     using G = SpmmTmaGeom<V, PA, PB, NT, STAGES, CW>;
@@ -73,7 +74,7 @@ int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s
         return fail(1, "mcSpmm: TMA tensor map encoding failed");
     unsigned int* timeouts = async_timeout_counter();
     if (!timeouts) return fail(1, "mcSpmm: timeout counter unavailable");
-    auto kern = spmm_tma_kernel<V, PA, PB, S, H, H, NT, STAGES, CW>;
+    auto kern = spmm_tma_kernel<V, PA, PB, S, H, H, NT, STAGES, CW, DP4A>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
         return (int)cudaGetLastError();
     // resident CTAs per SM from registers, shared memory and warps
@@ -102,12 +103,12 @@ int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s
 // over 6 stages.  Deeper rings cost resident CTAs, which matter more.  4-bit
 // B: 256-column tiles (128-byte rows, half the stage of 8-bit B) over 6
 // stages.
-template <int V, int PA, int PB, bool S, bool H, int NT>
+template <int V, int PA, int PB, bool S, bool H, int NT, bool DP4A = false>
 int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
-    if constexpr (PB == 4) return spmm_launch_tma_cfg<V, PA, 4, S, H, 256, 6, 4>(d, p, s);
-    else if constexpr (NT == 256) return spmm_launch_tma_cfg<V, PA, 8, S, H, 256, 4, 4>(d, p, s);
-    else return spmm_launch_tma_cfg<V, PA, 8, S, H, 128, 6, 2>(d, p, s);
+    if constexpr (PB == 4) return spmm_launch_tma_cfg<V, PA, 4, S, H, 256, 6, 4, DP4A>(d, p, s);
+    else if constexpr (NT == 256) return spmm_launch_tma_cfg<V, PA, 8, S, H, 256, 4, 4, DP4A>(d, p, s);
+    else return spmm_launch_tma_cfg<V, PA, 8, S, H, 128, 6, 2, DP4A>(d, p, s);
 }
 
 // n == 64, 8-bit x 8-bit, softmax value layout, half output (the attention's
@@ -153,6 +154,20 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
             if (d.n == 64 && !f16 && (d.kernel_variant == MC_KERNEL_AUTO || d.kernel_variant == MC_KERNEL_STREAM) &&
                 reinterpret_cast<uintptr_t>(d.values) % 16 == 0 && d.values_stride % 16 == 0)
                 return spmm_launch_n64<V, S>(d, p, s);
+        }
+        if (resolve_mma_kind(d.mma_kind) == MC_MMA_DP4A) {
+            // CUDA-core dp4a consumers in the TMA kernel: V = 2 and 4 compute
+            // no padding lanes (an int8 MMA always computes 8)
+            if constexpr (V <= 4 && PA <= 8) {
+                if (!spmm_tma_eligible(d))
+                    return fail(1, "mcSpmm: the dp4a SpMM runs on the TMA kernel: n % 128 == 0 (8-bit B) or "
+                                   "n % 256 == 0 (4-bit B), 16-byte aligned values, values_stride and rhs, and "
+                                   "rhs_stride a multiple of the B row bytes");
+                return d.n % 256 == 0 ? spmm_launch_tma<V, PA, PB, S, H, 256, true>(d, p, s)
+                                      : spmm_launch_tma<V, PA, PB, S, H, 128, true>(d, p, s);
+            } else {
+                return fail(1, "mcSpmm: the dp4a SpMM computes V = 2 and 4 with 8-bit or 4-bit values");
+            }
         }
         const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);
         if (d.kernel_variant == MC_KERNEL_STREAM && !stream_ok)

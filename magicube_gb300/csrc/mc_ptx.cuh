@@ -40,6 +40,17 @@ __device__ __forceinline__ void mma_k32(int (&d)[4], uint32_t a0, uint32_t a1, u
     }
 }
 
+// c + the dot product of the four bytes of a and b (both signed or both
+// unsigned), modulo 2^32.
+template <bool SIGNED>
+__device__ __forceinline__ int dp4a(uint32_t a, uint32_t b, int c)
+{
+    int d;
+    if constexpr (SIGNED) asm("dp4a.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    else asm("dp4a.u32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 // D += A * B with A 16x16 (row), B 16x8 (col), f16 operands, f32 accumulators.
 __device__ __forceinline__ void mma_f16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                         uint32_t b0, uint32_t b1)

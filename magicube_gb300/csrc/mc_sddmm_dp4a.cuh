@@ -31,15 +31,6 @@
 
 namespace mc {
 
-template <bool SIGNED>
-__device__ __forceinline__ int dp4a(uint32_t a, uint32_t b, int c)
-{
-    int d;
-    if constexpr (SIGNED) asm("dp4a.s32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    else asm("dp4a.u32.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
-    return d;
-}
-
 // K64: k == 64, one k block, the A chunks stay in registers for the whole
 // vector-row; otherwise they are reloaded per k block.
 template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool K64>

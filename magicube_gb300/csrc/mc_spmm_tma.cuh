@@ -46,7 +46,8 @@ struct SpmmTmaGeom {
     static constexpr size_t SMEM = 1024 + (size_t)STAGES * (RHS_BYTES + AUX_BYTES) + 2 * STAGES * 8;
 };
 
-template <int V, int PREA, int PREB, bool SIGNED, bool HALF_OUT, bool EXT, int NT, int STAGES, int CWARPS = 4>
+template <int V, int PREA, int PREB, bool SIGNED, bool HALF_OUT, bool EXT, int NT, int STAGES, int CWARPS = 4,
+          bool DP4A = false>
 __global__ void __launch_bounds__((CWARPS + 1) * 32)
 spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, const int ntasks,
                 const int rows_per_entry, unsigned int* timeouts)
@@ -62,6 +63,7 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
     static_assert(RB == 128 || RB == 256, "one or two 128-byte TMA boxes per gathered row");
     static_assert(PREB == 8 || MT % 2 == 0, "4-bit B: two MMA tiles per 16-byte chunk");
     static_assert(HDR % 16 == 0, "header alignment");
+    static_assert(!DP4A || (V <= 4 && BP == 1), "the dp4a consumer computes V = 2 and 4 with 8-bit or 4-bit A");
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
@@ -184,6 +186,17 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
         for (int m = 0; m < MT; ++m)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[bp][m][e] = 0;
+    // dp4a consumer: partial sums over this lane's slots (4t..4t+3, 16+4t..)
+    // of output columns g (hh = 0) and g + 8 (hh = 1) of every tile, for
+    // every vector lane; summed over the four t lanes when a row ends
+    constexpr int DM = DP4A ? MT : 1, DV = DP4A ? V : 1;
+    int pacc[DM][2][DV];
+#pragma unroll
+    for (int m = 0; m < DM; ++m)
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+            for (int v = 0; v < DV; ++v) pacc[m][hh][v] = 0;
 
 #pragma unroll 1
     for (int it = 0;; ++it) {
@@ -201,10 +214,31 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
         const int nnz = hdr.z;
         if (!empty_row) {
             // value fragments: vals[bp][h] for vector lane v = g, slots 16h+4t..+3
+            // (dp4a: vv[v][h] for every vector lane v)
             uint32_t vals[BP][2];
+            uint32_t vv[DV][2];
 #pragma unroll
             for (int bp = 0; bp < BP; ++bp) { vals[bp][0] = 0u; vals[bp][1] = 0u; }
-            if (g < V) {
+            if constexpr (DP4A) {
+                const bool whole = step * 32 + 32 <= nnz;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const uint32_t keep = whole ? 0xffffffffu : byte_mask(nnz - (step * 32 + 16 * h + 4 * t));
+#pragma unroll
+                    for (int v = 0; v < DV; ++v) {
+                        if constexpr (L::VCHUNK == 16) {
+                            vv[v][h] = lds32(aux + h * 16 * SLOT_BYTES + vword16<V, PREA, PREB, EXT>(v, t, 0)) & keep;
+                        } else {
+                            constexpr int PLANE_BYTES = V * 32 * L::PLANE_BITS / 8;
+                            const int o = v * 16 + 8 * h + 2 * t;
+                            if constexpr (PREA == 4)
+                                vv[v][h] = unpack4_u16<SIGNED>(lds16(aux + o)) & keep;
+                            else
+                                vv[v][h] = merge_nibble_planes(lds16(aux + o), lds16(aux + PLANE_BYTES + o)) & keep;
+                        }
+                    }
+                }
+            } else if (g < V) {
                 const bool whole = step * 32 + 32 <= nnz;  // no slot of this step past the row end
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
@@ -255,8 +289,19 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
                     }
                 }
             }
+            if constexpr (DP4A) {
 #pragma unroll
-            for (int bp = 0; bp < BP; ++bp) {
+                for (int m = 0; m < MT; ++m)
+#pragma unroll
+                    for (int v = 0; v < DV; ++v) {
+                        pacc[m][0][v] = dp4a<SIGNED>(af[m][0], vv[v][0], pacc[m][0][v]);
+                        pacc[m][0][v] = dp4a<SIGNED>(af[m][2], vv[v][1], pacc[m][0][v]);
+                        pacc[m][1][v] = dp4a<SIGNED>(af[m][1], vv[v][0], pacc[m][1][v]);
+                        pacc[m][1][v] = dp4a<SIGNED>(af[m][3], vv[v][1], pacc[m][1][v]);
+                    }
+            }
+#pragma unroll
+            for (int bp = 0; bp < (DP4A ? 0 : BP); ++bp) {
                 const bool top = (bp == BP - 1);
 #pragma unroll
                 for (int m = 0; m < MT; ++m) {
@@ -272,6 +317,31 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
         __syncwarp();  // every lane has read the stage
         if (lane == 0) mbar_arrive(empty + slot);
         if (last) {
+            if constexpr (DP4A) {
+                // sum the four t lanes' partial sums; lane t then holds vector
+                // lanes 2t, 2t + 1 in the MMA accumulator layout below
+#pragma unroll
+                for (int m = 0; m < MT; ++m)
+#pragma unroll
+                    for (int hh = 0; hh < 2; ++hh)
+#pragma unroll
+                        for (int v = 0; v < DV; ++v) {
+                            int x = pacc[m][hh][v];
+                            x += __shfl_xor_sync(0xffffffffu, x, 1);
+                            x += __shfl_xor_sync(0xffffffffu, x, 2);
+                            pacc[m][hh][v] = x;
+                        }
+#pragma unroll
+                for (int m = 0; m < MT; ++m)
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int hh = e >> 1, vo = e & 1;
+                        if constexpr (DV == 4) acc[0][m][e] = t ? pacc[m][hh][2 + vo] : pacc[m][hh][vo];
+                        else acc[0][m][e] = pacc[m][hh][vo < DV ? vo : 0];
+                        pacc[m][hh][vo] = 0;
+                        if constexpr (DV == 4) pacc[m][hh][2 + vo] = 0;
+                    }
+            }
             // acc[.][m][e]: vector lane 2t + (e & 1), column of the warp's slice
             // 8-bit B: 16m + 8(e>>1) + g;  4-bit B: 32(m>>1) + 2g + (m&1) + 16(e>>1)
             const int row = hdr.x, b = hdr.y;

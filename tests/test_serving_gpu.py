@@ -32,6 +32,23 @@ def _same_as_alone(enc, reqs, cuda, kw=KW):
         assert (got - ref).abs().max() <= 2e-2 * ref.abs().max(), a.rid
 
 
+class _SlowBatches(torch.nn.Module):
+    """The encoder followed by a fixed spin of about a millisecond on the
+    batch's stream (torch.cuda._sleep: a bounded busy loop), so a batch
+    stays on the device while the host admits the next ones -- at these
+    small sizes the host would otherwise launch slower than the device
+    finishes."""
+
+    def __init__(self, enc):
+        super().__init__()
+        self.enc, self.layers = enc, enc.layers
+
+    def forward(self, x, masks):
+        y = self.enc(x, masks)
+        torch.cuda._sleep(2_000_000)
+        return y
+
+
 @pytest.mark.parametrize("attention", ["fused", "separate"])
 def test_batches_overlap_and_each_result_equals_served_alone(cuda, attention):
     """Staggered arrivals with a small overlap threshold: several batches are
@@ -39,8 +56,8 @@ def test_batches_overlap_and_each_result_equals_served_alone(cuda, attention):
     its served-alone output within the stated tolerance."""
     enc = _encoder(cuda, attention)
     reqs = serving.make_requests(12, rate=20000.0, **KW)
-    srv = serving.ContinuousBatchingServer(enc, hidden=256, heads=4, max_inflight=3, max_batch_tokens=2048,
-                                           overlap_tokens=1, device=cuda)
+    srv = serving.ContinuousBatchingServer(_SlowBatches(enc), hidden=256, heads=4, max_inflight=3,
+                                           max_batch_tokens=2048, overlap_tokens=1, device=cuda)
     stats = srv.serve(reqs)
     assert stats["requests"] == 12 and stats["rejected"] == 0
     assert srv.peak_inflight >= 2, srv.batches
@@ -67,8 +84,8 @@ def test_admission_holds_requests_back_while_memory_is_taken(cuda, monkeypatch):
     reqs = serving.make_requests(6, rate=0.0, **kw)
     srv = serving.ContinuousBatchingServer(enc, hidden=256, heads=4, max_inflight=3, max_batch_tokens=1 << 20,
                                            overlap_tokens=1, hbm_reserve=0, device=cuda)
-    one = max(serving.footprint_bytes([r], 256, 4, 2, 8) for r in reqs)
-    two = min(serving.footprint_bytes([a, b], 256, 4, 2, 8) for a in reqs for b in reqs if a is not b)
+    one = max(srv.footprint([r]) for r in reqs)
+    two = min(srv.footprint([a, b]) for a in reqs for b in reqs if a is not b)
     assert two > one
     _fake_free_memory(monkeypatch, srv, budget=(one + two) // 2, per_batch=one)
     stats = srv.serve(reqs)
@@ -87,10 +104,37 @@ def test_oversize_request_is_rejected_not_launched(cuda, monkeypatch):
     big = max(reqs, key=lambda r: r.seq_len)
     srv = serving.ContinuousBatchingServer(enc, hidden=256, heads=4, max_inflight=2, max_batch_tokens=1 << 20,
                                            hbm_reserve=0, device=cuda)
-    fit = max(serving.footprint_bytes([r], 256, 4, 2, 8) for r in reqs if r is not big)
-    assert serving.footprint_bytes([big], 256, 4, 2, 8) > fit
+    fit = max(srv.footprint([r]) for r in reqs if r is not big)
+    assert srv.footprint([big]) > fit
     _fake_free_memory(monkeypatch, srv, budget=fit, per_batch=fit)
     stats = srv.serve(reqs)
     assert srv.rejected == [big.rid] and big.error is not None and big.out is None
     assert stats["requests"] == 3 and stats["rejected"] == 1
     assert all(r.out is not None for r in reqs if r is not big)
+
+
+@pytest.mark.parametrize("attention", ["fused", "separate"])
+def test_footprint_bounds_the_measured_peak(cuda, attention):
+    """The admission estimate is an upper bound of the measured peak device
+    memory of a batch (torch.cuda.max_memory_allocated) and within 2x of it,
+    on encoder-request lengths from 512 to 8192 tokens."""
+    enc = _encoder(cuda, attention)
+    srv = serving.ContinuousBatchingServer(enc, hidden=256, heads=4, device=cuda)
+    for lens in ([512], [2048], [8192], [2048] * 4, [1024, 4096, 8192]):
+        reqs = [serving.make_requests(1, 0.0, hidden=256, layers=2, median=L, clip=(L, L), seed=60 + i)[0]
+                for i, L in enumerate(lens)]
+        for r in reqs:
+            serving._upload_csr(r, cuda)
+        with torch.no_grad():
+            for warm in (True, False):  # the first pass creates library handles outside the measurement
+                torch.cuda.synchronize()
+                base = torch.cuda.memory_allocated()
+                torch.cuda.reset_peak_memory_stats()
+                masks = serving.pack_batch_masks(reqs, 2, 8, 16, cuda)
+                x = torch.cat([r.dev["x"] for r in reqs], 0)
+                y = enc(x, masks)
+                torch.cuda.synchronize()
+                peak = torch.cuda.max_memory_allocated() - base
+                del y, x, masks
+        est = srv.footprint(reqs)
+        assert peak <= est <= 2 * peak, (lens, peak, est)

@@ -167,3 +167,76 @@ def test_tma_rejects_ineligible(cuda):
 def test_tma_no_timeouts(cuda):
     torch.cuda.synchronize()
     assert _lib.lib().mcTensorCoreTimeouts() == 0
+
+
+DP4A_PAIRS = [(8, 8), (8, 4), (4, 4)]
+
+
+@pytest.mark.parametrize("pa,pb", DP4A_PAIRS)
+@pytest.mark.parametrize("V", [2, 4])
+@pytest.mark.parametrize("signed", [False, True])
+@pytest.mark.parametrize("N", [128, 256, 512])
+def test_dp4a_spmm_ragged(cuda, pa, pb, V, signed, N):
+    """The dp4a consumers of the TMA kernel (MC_MMA_DP4A, V = 2 and 4): row
+    lengths around every group-of-4, 16-slot and 32-slot boundary, empty
+    rows, bit-exact against the oracle."""
+    if pb == 4 and N == 128:
+        N = 256
+    K = 256
+    mask = synth.lengths_mask(RAGGED, K, V, seed=pa * 10 + V + 7)
+    vals = _vals(mask, V, pa, 40 + V)
+    rhs = synth.random_bytes(K * N * pb // 8, 41 + V)
+    out = _run(cuda, mask, vals, rhs, pa, pb, N, signed, variant=_lib.KERNEL_AUTO, mma_kind=_lib.MMA_DP4A)
+    ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
+                           oracle.SIGNED if signed else oracle.UNSIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", DP4A_PAIRS)
+@pytest.mark.parametrize("V", [2, 4])
+@pytest.mark.parametrize("fill", [0x80, 0x7F, 0xFF])
+def test_dp4a_spmm_extreme_values_long_rows(cuda, pa, pb, V, fill):
+    """Extreme lanes over rows of up to K = 2048 nonzero vectors."""
+    K, N = 2048, 256
+    mask = synth.lengths_mask([2048, 1, 0, 999, 33, 2047, 64, 16], K, V, seed=V + pa)
+    vals = np.full(mask.nnz_vec * V * pa // 8, fill, np.uint8)
+    rhs = np.full(K * N * pb // 8, fill, np.uint8)
+    out = _run(cuda, mask, vals, rhs, pa, pb, N, True, variant=_lib.KERNEL_AUTO, mma_kind=_lib.MMA_DP4A)
+    ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
+                           oracle.SIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("pa,pb", DP4A_PAIRS)
+@pytest.mark.parametrize("V", [2, 4])
+def test_dp4a_spmm_batched_many_tasks_equals_int8(cuda, pa, pb, V):
+    """Many tasks per CTA, per-entry values and B: dp4a and int8 MMA give the
+    same integers."""
+    K, N, B = 1024, 256, 3
+    mask = synth.normal_mask(700, K, V, 0.9, seed=V * 3 + pa)
+    h = formats.prepare_spmm(mask, _vals(mask, V, pa, 50), pa, pb)
+    d = ops.DeviceSpmmLhs.from_host(h, cuda)
+    d.values = torch.cat([d.values, torch.randint(0, 256, (2 * d.values.numel(),), dtype=torch.uint8,
+                                                  device=cuda)])
+    rhs = torch.randint(0, 256, (B, K * N * pb // 8), dtype=torch.uint8, device=cuda)
+    kw = dict(signed=True, batch=B, values_stride=h.values.size)
+    a = ops.spmm(d, rhs, N, mma_kind=_lib.MMA_DP4A, **kw)
+    b = ops.spmm(d, rhs, N, mma_kind=_lib.MMA_INT8, variant=_lib.KERNEL_TMA, **kw)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    i = B - 1
+    vals_i = d.values[i * h.values.size:(i + 1) * h.values.size].cpu().numpy()
+    ref = oracle.spmm_device(h.row_offsets, h.col_indices, vals_i, rhs[i].cpu().numpy(), mask.m_vec, V, K, N, pa, pb,
+                             oracle.SIGNED)
+    np.testing.assert_array_equal(a[i].cpu().numpy(), ref)
+
+
+def test_dp4a_spmm_rejects_unsupported(cuda):
+    mask = synth.lengths_mask([5, 9], 64, 8, seed=1)
+    with pytest.raises(_lib.MagicubeError):
+        _run(cuda, mask, _vals(mask, 8, 8, 1), synth.random_bytes(64 * 128, 2), 8, 8, 128, True,
+             variant=_lib.KERNEL_AUTO, mma_kind=_lib.MMA_DP4A)
+    mask = synth.lengths_mask([5, 9], 64, 4, seed=1)
+    with pytest.raises(_lib.MagicubeError):
+        _run(cuda, mask, _vals(mask, 4, 16, 1), synth.random_bytes(64 * 128, 2), 16, 8, 128, True,
+             variant=_lib.KERNEL_AUTO, mma_kind=_lib.MMA_DP4A)

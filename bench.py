@@ -873,14 +873,18 @@ def serving_suite(args, dev) -> dict:
     lognormal (median 2048, clipped to [256, 8192]).  The server runs the
     fused attention kernel; the baseline serves the same requests one at a
     time on the plain separate SDDMM / softmax / SpMM launches (same bits,
-    fixed requantization)."""
+    row-max requantization).  The attention output's error against the
+    float64 oracle is stated for a few requests of this workload."""
     import torch
 
     from magicube_gb300 import model, serving
     torch.manual_seed(0)
     enc = model.SparseEncoder(2, 256, 4, 1024).to(dev).half().eval()
-    fused = lambda: enc.set_attention("fused")  # noqa: E731
-    plain = lambda: enc.set_attention("separate")  # noqa: E731
+    # row-max requantization (probabilities relative to each row's maximum):
+    # the accurate 8-bit mode; the fused and the separate launches give the
+    # same bits in it
+    fused = lambda: enc.set_attention("fused", "rowmax")  # noqa: E731
+    plain = lambda: enc.set_attention("separate", "rowmax")  # noqa: E731
     warm = serving.make_requests(4, 0.0, seed=99)
     serving.ContinuousBatchingServer(fused(), device=dev).serve(warm)
     serving.serve_sequential(plain(), serving.make_requests(2, 0.0, seed=98), device=dev)
@@ -908,7 +912,54 @@ def serving_suite(args, dev) -> dict:
     return {"config": "2-layer sparse encoder, hidden 256, 4x64 heads, FFN 1024, sparsity 0.95, "
                       "lengths lognormal(median 2048) in [256, 8192]",
             "kernels": {"continuous": "fused attention kernel", "sequential": "separate SDDMM/softmax/SpMM"},
-            "runs": out}
+            "runs": out,
+            "requant": "rowmax",
+            "attention_rel_error_vs_fp64": encoder_attention_error(fused(), dev)}
+
+
+def encoder_attention_error(enc, dev, n_requests: int = 4) -> dict:
+    """The served encoder's attention output against the float64 oracle of
+    the unquantized attention, per layer, for a few requests of the serving
+    workload (lengths lognormal, median 2048): the layer's own input (the
+    model's fp16 hidden state), its LayerNorm and projection weights; the
+    oracle projects in float64 without quantization and applies the softmax
+    over the request's mask of that layer.  Relative Frobenius error of the
+    [heads, tokens, 64] output (median and maximum)."""
+    import torch
+
+    import oracle.attention as oatt
+    from magicube_gb300 import serving
+    from magicube_gb300.model import attention_fused_quantized
+    from magicube_gb300.projection import qkv_project_quantize
+    reqs = serving.make_requests(n_requests, 0.0, seed=5)
+    errs = []
+    with torch.no_grad():
+        for r in reqs:
+            serving._upload_csr(r, dev)
+            masks = serving.pack_batch_masks([r], len(enc.layers), 8, 16, dev)
+            x = r.dev["x"]
+            for li, (layer, m) in enumerate(zip(enc.layers, masks)):
+                h = layer.ln1(x)
+                qkv_q = qkv_project_quantize(h, layer.in_proj.weight, layer.in_proj.bias, layer.heads,
+                                             layer.rhs_bits, layer.scale_qkv)
+                att = attention_fused_quantized(qkv_q, r.seq_len, m, layer.scale_qkv, layer.scale_sfmx,
+                                                layer.requant, layer.lhs_bits, layer.rhs_bits, layer.fused_cfg)
+                w = layer.in_proj.weight.double().cpu().numpy()
+                bias = layer.in_proj.bias.double().cpu().numpy()
+                qkv = h.double().cpu().numpy() @ w.T + bias  # [T, 3E]
+                T, E, H = r.seq_len, layer.hidden, layer.heads
+                qkv = qkv.reshape(T, 3, H, E // H).transpose(1, 2, 0, 3)  # [3, H, T, d]
+                mk = r.masks[li]
+                ref = oatt.sparse_attention_fp64_rows(qkv[0], qkv[1], qkv[2], mk.row_offsets, mk.col_indices, 8,
+                                                      (E // H) ** -0.5)
+                got = att.double().cpu().numpy()
+                errs.append({"request_tokens": T, "layer": li,
+                             "rel_error": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))})
+                x = layer(x, m)
+            r.dev.clear()
+    e = [x["rel_error"] for x in errs]
+    return {"requant": enc.layers[0].requant, "pair": f"L{enc.layers[0].lhs_bits}-R{enc.layers[0].rhs_bits}",
+            "median": statistics.median(e), "max": max(e), "per_request_layer": errs}
 
 
 def tensor_peaks(dev) -> dict:

@@ -21,8 +21,8 @@ def _encoder(cuda, attention="fused"):
     return model.SparseEncoder(layers=2, hidden=256, heads=4, ffn=512).to(cuda).half().eval().set_attention(attention)
 
 
-def _same_as_alone(enc, reqs, cuda, kw=KW):
-    alone = serving.make_requests(len(reqs), rate=0.0, **kw)
+def _same_as_alone(enc, reqs, cuda, kw=KW, rate=0.0):
+    alone = serving.make_requests(len(reqs), rate=rate, **kw)  # the same requests (same draws)
     serving.serve_sequential(enc, alone, device=cuda)
     for a, m in zip(alone, reqs):
         ref, got = a.out.float().cpu(), m.out.float().cpu()
@@ -62,7 +62,7 @@ def test_batches_overlap_and_each_result_equals_served_alone(cuda, attention):
     assert stats["requests"] == 12 and stats["rejected"] == 0
     assert srv.peak_inflight >= 2, srv.batches
     assert sorted(r for b in srv.batches for r in b) == list(range(12))
-    _same_as_alone(enc, reqs, cuda)
+    _same_as_alone(enc, reqs, cuda, rate=20000.0)
 
 
 def _fake_free_memory(monkeypatch, srv, budget: int, per_batch: int):

@@ -455,25 +455,13 @@ def run_gpu(args) -> None:
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
         # small vectors: an int8 MMA computes 8 vector lanes of which V are
-        # used; the dp4a consumers compute only the V lanes.  The TMA
-        # kernel's gather split: groups = 4-row groups per step copied by
-        # the cp.async copier warp instead of TMA (0: all TMA).
-        from magicube_gb300 import _lib
-        prev = _lib.lib().mcSetSpmmCopyGroups(0)
-        for groups in (0, 2, 4):
-            _lib.lib().mcSetSpmmCopyGroups(groups)
-            tag = f"_copy{groups}"
-            variants[f"spmm_L8R8_1024x1024x256_int8mma{tag}"] = spmm_variant(
-                args, dev, stream, peaks, world, sync_all, max_over_ranks, 1, 3)
-            for v in (2, 4):
-                for pa, pb in ((8, 8), (8, 4), (4, 4)):
-                    for mma in (1, 4):
-                        variants[f"spmm_L{pa}R{pb}_4096x4096x256_V{v}_s0.9_{MMA_NAMES[mma]}{tag}"] = spmm_point(
-                            args, dev, stream, peaks, 4096, 4096, 256, v, pa, pb, mma)
-                        torch.cuda.empty_cache()
-            variants[f"spmm_L8R8_4096x4096x256_V8_s0.9_int8mma{tag}"] = spmm_point(
-                args, dev, stream, peaks, 4096, 4096, 256, 8, 8, 8, 1)
-        _lib.lib().mcSetSpmmCopyGroups(prev)
+        # used; the dp4a consumers compute only the V lanes
+        for v in (2, 4):
+            for pa, pb in ((8, 8), (8, 4), (4, 4)):
+                for mma in (1, 4):
+                    variants[f"spmm_L{pa}R{pb}_4096x4096x256_V{v}_s0.9_{MMA_NAMES[mma]}"] = spmm_point(
+                        args, dev, stream, peaks, 4096, 4096, 256, v, pa, pb, mma)
+                    torch.cuda.empty_cache()
     attention = serving_res = packer = projection = competitors = None
     if not args.headline_only and rank == 0:
         torch.cuda.empty_cache()

@@ -105,12 +105,6 @@ enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2, MC_MMA_TCGEN05 = 3, 
 unsigned mcTensorCoreTimeouts(void);
 /* Sets the default tensor path; returns the previous one (or -1 if invalid). */
 int mcSetDefaultMmaKind(int kind);
-/* The TMA SpMM gathers each 32-slot step's B rows with tile::gather4; with
- * groups = 2 or 4, the last 8 or 16 rows of every step go through a copier
- * warp's cp.async copies instead, so the load/store path and the tensor
- * memory accelerator share the gather.  Same results for every setting.
- * Returns the previous setting (or -1 if invalid). */
-int mcSetSpmmCopyGroups(int groups);
 
 /* ---- Kernel variant ---------------------------------------------------------
  * MC_KERNEL_PER_ROW: one CTA per (vector-row, column tile / row split, batch

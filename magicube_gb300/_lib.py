@@ -95,7 +95,6 @@ _SIGNATURES = {
     "mcGetLastErrorString": (ctypes.c_char_p, []),
     "mcVersion": (ctypes.c_char_p, []),
     "mcSetDefaultMmaKind": (_c_int, [_c_int]),
-    "mcSetSpmmCopyGroups": (_c_int, [_c_int]),
     "mcTensorCoreTimeouts": (ctypes.c_uint, []),
     "mcSpmm": (_c_int, [ctypes.POINTER(McSpmmDesc), _c_vp]),
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),

@@ -10,10 +10,8 @@ namespace mc {
 
 static thread_local std::string g_last_error;
 static std::atomic<int> g_default_mma{MC_MMA_INT8};
-static std::atomic<int> g_spmm_copy_groups{0};
 
 int default_mma_kind() { return g_default_mma.load(std::memory_order_relaxed); }
-int spmm_copy_groups() { return g_spmm_copy_groups.load(std::memory_order_relaxed); }
 
 int fail(int code, const char* msg)
 {
@@ -123,12 +121,6 @@ int mcSetDefaultMmaKind(int kind)
 {
     if (kind != MC_MMA_INT8 && kind != MC_MMA_F16) return -1;
     return mc::g_default_mma.exchange(kind);
-}
-
-int mcSetSpmmCopyGroups(int groups)
-{
-    if (groups != 0 && groups != 2 && groups != 4) return -1;
-    return mc::g_spmm_copy_groups.exchange(groups);
 }
 
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream)

@@ -9,8 +9,6 @@ namespace mc {
 // Tensor path used by a call whose descriptor asks for MC_MMA_DEFAULT.
 int default_mma_kind();
 inline int resolve_mma_kind(int k) { return k == MC_MMA_DEFAULT ? default_mma_kind() : k; }
-// 4-row groups per 32-slot step the TMA SpMM copies with cp.async (0, 2, 4).
-int spmm_copy_groups();
 
 // Number of SMs of the current device (cached per device).
 inline int sm_count()

@@ -61,16 +61,10 @@ inline bool spmm_tma_eligible(const mcSpmmDesc& d)
     return per_entry * (d.batch - 1) + d.k <= 0x7fffffffLL;
 }
 
-template <int V, int PA, int PB, bool S, bool H, int NT, int STAGES = 4, int CW = 4, bool DP4A = false, int CPG = 0>
+template <int V, int PA, int PB, bool S, bool H, int NT, int STAGES = 4, int CW = 4, bool DP4A = false>
 int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
 {
-    if constexpr (CPG == 0) {
-        // the copy split is a runtime setting: dispatch to its instantiation
-        const int cpg = spmm_copy_groups();
-        if (cpg == 2) return spmm_launch_tma_cfg<V, PA, PB, S, H, NT, STAGES, CW, DP4A, 2>(d, p, s);
-        if (cpg == 4) return spmm_launch_tma_cfg<V, PA, PB, S, H, NT, STAGES, CW, DP4A, 4>(d, p, s);
-    }
-    using G = SpmmTmaGeom<V, PA, PB, NT, STAGES, CW, CPG>;
+    using G = SpmmTmaGeom<V, PA, PB, NT, STAGES, CW>;
     const long long ntasks = (long long)d.m_vec * d.batch;
     if (ntasks > 0x7fffffffLL) return fail(1, "mcSpmm: m_vec * batch too large");
     const long long row_bytes = (long long)d.n * PB / 8;
@@ -80,7 +74,7 @@ int spmm_launch_tma_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s
         return fail(1, "mcSpmm: TMA tensor map encoding failed");
     unsigned int* timeouts = async_timeout_counter();
     if (!timeouts) return fail(1, "mcSpmm: timeout counter unavailable");
-    auto kern = spmm_tma_kernel<V, PA, PB, S, H, H, NT, STAGES, CW, DP4A, CPG>;
+    auto kern = spmm_tma_kernel<V, PA, PB, S, H, H, NT, STAGES, CW, DP4A>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM) != cudaSuccess)
         return (int)cudaGetLastError();
     // resident CTAs per SM from registers, shared memory and warps

@@ -33,10 +33,10 @@
 
 namespace mc {
 
-template <int V, int PREA, int PREB, int NT, int STAGES, int CWARPS = 4, int CPG = 0>
+template <int V, int PREA, int PREB, int NT, int STAGES, int CWARPS = 4>
 struct SpmmTmaGeom {
     static constexpr int CW = CWARPS;                 // consumer warps
-    static constexpr int THREADS = (CW + 1 + (CPG > 0 ? 1 : 0)) * 32;  // + producer (+ copier)
+    static constexpr int THREADS = (CW + 1) * 32;
     static constexpr int MT = NT / (16 * CW);         // 16-column MMA tiles per consumer warp
     static constexpr int SLOT_BYTES = V * PREA / 8;   // value bytes per vector slot
     static constexpr int RB = NT * PREB / 8;          // bytes of one gathered row slice
@@ -47,14 +47,14 @@ struct SpmmTmaGeom {
 };
 
 template <int V, int PREA, int PREB, bool SIGNED, bool HALF_OUT, bool EXT, int NT, int STAGES, int CWARPS = 4,
-          bool DP4A = false, int CPG = 0>
-__global__ void __launch_bounds__((CWARPS + 1 + (CPG > 0 ? 1 : 0)) * 32)
+          bool DP4A = false>
+__global__ void __launch_bounds__((CWARPS + 1) * 32)
 spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, const int ntasks,
                 const int rows_per_entry, unsigned int* timeouts)
 {
     using namespace sm100;
     using L = SpmmLayout<PREA, PREB, EXT>;
-    using G = SpmmTmaGeom<V, PREA, PREB, NT, STAGES, CWARPS, CPG>;
+    using G = SpmmTmaGeom<V, PREA, PREB, NT, STAGES, CWARPS>;
     constexpr int CW = G::CW, MT = G::MT, BP = L::BYTE_PLANES;
     constexpr int SLOT_BYTES = G::SLOT_BYTES, RB = G::RB, RHS_BYTES = G::RHS_BYTES, AUX_BYTES = G::AUX_BYTES;
     constexpr int HDR = 32 * SLOT_BYTES;              // header offset inside a stage's aux block
@@ -64,8 +64,6 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
     static_assert(PREB == 8 || MT % 2 == 0, "4-bit B: two MMA tiles per 16-byte chunk");
     static_assert(HDR % 16 == 0, "header alignment");
     static_assert(!DP4A || (V <= 4 && BP == 1), "the dp4a consumer computes V = 2 and 4 with 8-bit or 4-bit A");
-    static_assert(CPG >= 0 && CPG < 8 && (CPG & (CPG - 1)) == 0, "cp.async copies 0, 1, 2 or 4 row groups");
-    constexpr int TG = 8 - CPG;                       // 4-row groups per step gathered by TMA
 
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
@@ -78,7 +76,7 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
     if (tid == 0) {
 #pragma unroll
         for (int s = 0; s < STAGES; ++s) {
-            mbar_init(full + s, 1 + (CPG > 0 ? 32 : 0));  // producer (+ the copier's 32 lanes)
+            mbar_init(full + s, 1);
             mbar_init(empty + s, CW);
         }
         fence_mbar_init();
@@ -150,10 +148,10 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
                 const int last = (c.steps == 0) || (c.step == c.steps - 1);
                 h.w = c.step | (last << 30) | ((c.steps == 0) << 29);
                 *reinterpret_cast<int4*>(aux + HDR) = h;
-                mbar_arrive_expect_tx(full + slot, (uint32_t)(min(ngroups, TG) * 4 * RB + vbytes));
+                mbar_arrive_expect_tx(full + slot, (uint32_t)(ngroups * 4 * RB + vbytes));
             }
             __syncwarp();
-            if (lane < ngroups && lane < TG) {
+            if (lane < ngroups) {
                 uint8_t* dst = rhs_s + slot * RHS_BYTES + lane * 512;  // box rows 4 lane .. 4 lane + 3
 #pragma unroll
                 for (int hf = 0; hf < G::BOXES; ++hf)
@@ -176,78 +174,6 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
             for (int j = (it > STAGES ? it - STAGES : 0); j < it; ++j)
                 mbar_wait(full + j % STAGES, (j / STAGES) & 1, WAIT);
         }
-        return;
-    }
-    if (CPG > 0 && warp == CW + 1) {
-        // -------------------------------- copier --------------------------------
-        // The last 4 CPG rows of every step through the load/store path
-        // (cp.async, 16 bytes per copy) beside the TMA gathers, into the same
-        // 128-byte-swizzled layout; every lane arrives on the stage's "full"
-        // barrier once its copies have landed.  Slots past the row's end are
-        // not copied (their value bytes are zeroed by the consumers).
-        constexpr int CG = CPG > 0 ? CPG : 1;      // (only instantiated with CPG > 0)
-        constexpr int R0 = 32 - 4 * CG;            // first row of the step copied here
-        constexpr int CPR = RB / 16;               // 16-byte chunks per row slice
-        constexpr int LPR = 32 / (4 * CG);         // lanes per row
-        constexpr int PER = CPR / LPR;             // copies per lane
-        static_assert(PER >= 1 && CPR % LPR == 0, "copier geometry");
-        const int r = R0 + lane / LPR, q0 = lane % LPR;
-        auto load_task = [&](StreamTask& x, int task) {
-            x.task = task;
-            x.step = 0;
-            x.steps = 0;
-            if (task < ntasks) {
-                x.b = task / p.m_vec;
-                x.row = __ldg(p.row_indices + (task - x.b * p.m_vec));
-                x.start = __ldg(p.row_offsets + 2 * x.row);
-                x.nnz = __ldg(p.row_offsets + 2 * x.row + 1) - x.start;
-                x.steps = (x.nnz + 31) >> 5;
-            }
-        };
-        auto fetch_col = [&](const StreamTask& x) {
-            const int j = 32 * x.step + r;
-            return (x.task < ntasks && j < x.nnz) ? __ldg(p.col_indices + x.start + col_slot<L::SHUFFLED_COLS>(j))
-                                                  : -1;
-        };
-        auto next_of = [&](int task) {
-            const long long n = (long long)task + gridDim.x;
-            return n < ntasks ? (int)n : ntasks;
-        };
-        StreamTask c, nx;
-        load_task(c, blockIdx.x);
-        load_task(nx, next_of(blockIdx.x));
-        int col = fetch_col(c);
-        const long long row_bytes = (long long)p.n * PREB / 8;
-        for (int it = 0;; ++it) {
-            const int slot = it % STAGES;
-            if (it >= STAGES && !mbar_wait(empty + slot, ((it / STAGES) - 1) & 1, WAIT)) {
-                if (lane == 0) atomicAdd(timeouts, 1u);
-                cp_async_commit();
-                cp_async_wait<0>();
-                return;
-            }
-            if (c.task >= ntasks) {  // end of the stream: the producer's empty stage
-                mbar_arrive(full + slot);
-                break;
-            }
-            if (col >= 0) {
-                const uint8_t* src = p.rhs + (long long)c.b * p.rhs_stride + (long long)col * row_bytes + n0 * PREB / 8;
-                uint8_t* dst = rhs_s + slot * RHS_BYTES + r * 128;
-#pragma unroll
-                for (int i = 0; i < PER; ++i) {
-                    const int q = q0 + LPR * i;  // chunk of the row slice: box q / 8, chunk q % 8 of the box
-                    cp_async16(dst + (q >> 3) * 4096 + (((q & 7) ^ (r & 7)) << 4), src + 16 * q);
-                }
-            }
-            cp_async_mbar_arrive(full + slot);
-            if (++c.step >= (c.steps > 0 ? c.steps : 1)) {
-                c = nx;
-                load_task(nx, c.task < ntasks ? next_of(c.task) : ntasks);
-            }
-            col = fetch_col(c);
-        }
-        cp_async_commit();
-        cp_async_wait<0>();
         return;
     }
 

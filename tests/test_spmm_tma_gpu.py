@@ -240,65 +240,3 @@ def test_dp4a_spmm_rejects_unsupported(cuda):
     with pytest.raises(_lib.MagicubeError):
         _run(cuda, mask, _vals(mask, 4, 16, 1), synth.random_bytes(64 * 128, 2), 16, 8, 128, True,
              variant=_lib.KERNEL_AUTO, mma_kind=_lib.MMA_DP4A)
-
-
-@pytest.fixture
-def copy_groups():
-    """Sets mcSetSpmmCopyGroups for one test and restores the previous value."""
-    prev = []
-
-    def set_(groups):
-        old = _lib.lib().mcSetSpmmCopyGroups(groups)
-        assert old >= 0
-        if not prev:
-            prev.append(old)
-
-    yield set_
-    if prev:
-        _lib.lib().mcSetSpmmCopyGroups(prev[0])
-
-
-@pytest.mark.parametrize("groups", [2, 4])
-@pytest.mark.parametrize("pa,pb", [(8, 8), (16, 8), (4, 4), (8, 4)])
-@pytest.mark.parametrize("V", [2, 8])
-@pytest.mark.parametrize("mma", [_lib.MMA_INT8, _lib.MMA_DP4A])
-def test_tma_with_cp_async_copier_ragged(cuda, copy_groups, groups, pa, pb, V, mma):
-    """The last 8 or 16 rows of every step gathered by the copier warp's
-    cp.async copies beside the TMA gathers: bit-exact on ragged rows, with
-    the int8 MMA and the dp4a consumers."""
-    if mma == _lib.MMA_DP4A and (pa == 16 or V == 8):
-        pytest.skip("dp4a: V = 2 and 4, 8-bit or 4-bit values")
-    copy_groups(groups)
-    K = 256
-    N = 256 if pb == 4 else 384
-    mask = synth.lengths_mask(RAGGED, K, V, seed=pa * 10 + V + groups)
-    vals = _vals(mask, V, pa, 60 + V)
-    rhs = synth.random_bytes(K * N * pb // 8, 61 + V)
-    out = _run(cuda, mask, vals, rhs, pa, pb, N, True, variant=_lib.KERNEL_TMA if mma == _lib.MMA_INT8 else 0,
-               mma_kind=mma)
-    ref = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb,
-                           oracle.SIGNED)
-    np.testing.assert_array_equal(out.cpu().numpy(), ref)
-    assert _lib.lib().mcTensorCoreTimeouts() == 0
-
-
-@pytest.mark.parametrize("groups", [2, 4])
-@pytest.mark.parametrize("N", [128, 256])
-def test_tma_with_cp_async_copier_many_tasks_batched(cuda, copy_groups, groups, N):
-    """Far more tasks than resident CTAs, per-entry values and B: the same
-    integers with and without the copier."""
-    V, K, B = 8, 512, 4
-    lengths = np.random.default_rng(N + groups).integers(0, 90, size=700)
-    lengths[::29] = 0
-    mask = synth.lengths_mask(lengths, K, V, seed=3)
-    h = formats.prepare_spmm(mask, _vals(mask, V, 8, 70), 8, 8)
-    d = ops.DeviceSpmmLhs.from_host(h, cuda)
-    d.values = torch.cat([d.values, torch.randint(0, 256, (3 * d.values.numel(),), dtype=torch.uint8, device=cuda)])
-    rhs = torch.randint(0, 256, (B, K * N), dtype=torch.uint8, device=cuda)
-    kw = dict(signed=True, batch=B, values_stride=h.values.size, variant=_lib.KERNEL_TMA)
-    a = ops.spmm(d, rhs, N, **kw).clone()
-    copy_groups(groups)
-    b = ops.spmm(d, rhs, N, **kw)
-    torch.cuda.synchronize()
-    assert torch.equal(a, b)
-    assert _lib.lib().mcTensorCoreTimeouts() == 0

@@ -978,14 +978,14 @@ def tensor_peaks(dev) -> dict:
     for kind, name in ((0, "int8_mma_sync"), (1, "int4_mma_sync"), (2, "f16_mma_sync"), (3, "int8_k16_mma_sync"),
                        (4, "int8_dp4a"), (5, "int8_mma_plus_dp4a")):
         ms, ops = ctypes.c_float(), ctypes.c_double()
-        _lib.check(_lib.lib().mcProbeTensorPeak(kind, sink.data_ptr(), sink.numel(), 2048, ctypes.byref(ms),
+        _lib.check(_lib.probe_lib().mcProbeTensorPeak(kind, sink.data_ptr(), sink.numel(), 2048, ctypes.byref(ms),
                                                 ctypes.byref(ops), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                    "mcProbeTensorPeak")
         out[name] = ops.value / (ms.value * 1e-3) / 1e12
     timeouts = torch.zeros(1, dtype=torch.int32, device=dev)
     for n in (16, 64, 256):  # tcgen05.mma kind::f16, M = 128, K = 16 (padding included)
         ms, ops = ctypes.c_float(), ctypes.c_double()
-        _lib.check(_lib.lib().mcProbeTensorCorePeak(n, 8000, ctypes.byref(ms), ctypes.byref(ops),
+        _lib.check(_lib.probe_lib().mcProbeTensorCorePeak(n, 8000, ctypes.byref(ms), ctypes.byref(ops),
                                                     timeouts.data_ptr(),
                                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                    "mcProbeTensorCorePeak")

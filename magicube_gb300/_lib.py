@@ -103,12 +103,6 @@ _SIGNATURES = {
     "mcQuantize": (_c_int, [_c_vp, _c_vp, _c_ll, _c_int, _c_float, _c_vp]),
     "mcQuantSoftmax": (_c_int, [ctypes.POINTER(McSoftmaxDesc), _c_vp]),
     "mcSparseAttention": (_c_int, [ctypes.POINTER(McAttnDesc), _c_vp]),
-    "mcProbeTensorPeak": (_c_int, [_c_int, _c_vp, _c_ll, _c_int, ctypes.POINTER(ctypes.c_float),
-                                   ctypes.POINTER(ctypes.c_double), _c_vp]),
-    "mcCheckQuotients": (_c_int, [_c_float, _c_ll, _c_ll, _c_vp, _c_vp]),
-    "mcCheckSmallIntConversions": (_c_int, [ctypes.c_ulonglong, ctypes.c_ulonglong, _c_vp, _c_vp]),
-    "mcProbeTensorCorePeak": (_c_int, [_c_int, _c_int, ctypes.POINTER(ctypes.c_float),
-                                       ctypes.POINTER(ctypes.c_double), _c_vp, _c_vp]),
     "mcAlignRowOffsets": (_c_int, [_c_int, _c_vp, _c_int, _c_vp]),
     "mcPadColumnIndices": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_vp]),
     "mcPackSpmmValues": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_int, _c_vp, _c_vp]),
@@ -123,6 +117,15 @@ _SIGNATURES = {
     "mcDeviceSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp]),
     "mcDevicePack": (_c_int, [ctypes.POINTER(McDevicePackDesc), _c_vp]),
     "mcQkvProjectQuantize": (_c_int, [ctypes.POINTER(McQkvProjDesc), _c_vp]),
+}
+# the diagnostics library (include/magicube_gb300_probe.h)
+_PROBE_SIGNATURES = {
+    "mcProbeTensorPeak": (_c_int, [_c_int, _c_vp, _c_ll, _c_int, ctypes.POINTER(ctypes.c_float),
+                                   ctypes.POINTER(ctypes.c_double), _c_vp]),
+    "mcCheckQuotients": (_c_int, [_c_float, _c_ll, _c_ll, _c_vp, _c_vp]),
+    "mcCheckSmallIntConversions": (_c_int, [ctypes.c_ulonglong, ctypes.c_ulonglong, _c_vp, _c_vp]),
+    "mcProbeTensorCorePeak": (_c_int, [_c_int, _c_int, ctypes.POINTER(ctypes.c_float),
+                                       ctypes.POINTER(ctypes.c_double), _c_vp, _c_vp]),
 }
 for _p in ("4b", "8b4b", "12b4b", "16b4b", "8b", "12b8b", "16b8b", "16b"):
     _SIGNATURES[f"mcWmmaSpmm_{_p}"] = (_c_int, [_c_int, _c_int, _c_int, _c_int] + [_c_vp] * 6)
@@ -154,6 +157,29 @@ def lib() -> ctypes.CDLL:
                     fn.argtypes = args
                 _handle = h
     return _handle
+
+
+_probe: ctypes.CDLL | None = None
+PROBE_PATH = LIB_PATH.with_name("libmagicube_gb300_probe.so")
+
+
+def probe_lib() -> ctypes.CDLL:
+    """The diagnostics library (tensor-peak probes, arithmetic checks); it
+    reports errors through the main library's mcGetLastErrorString."""
+    global _probe
+    if _probe is None:
+        with _lock:
+            if _probe is None:
+                lib()
+                if not PROBE_PATH.exists():
+                    raise ImportError(f"{PROBE_PATH} is missing: build it with `python -m magicube_gb300.build`")
+                h = ctypes.CDLL(str(PROBE_PATH))
+                for name, (res, args) in _PROBE_SIGNATURES.items():
+                    fn = getattr(h, name)
+                    fn.restype = res
+                    fn.argtypes = args
+                _probe = h
+    return _probe
 
 
 def check(rc: int, what: str) -> None:

@@ -22,6 +22,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libmagicube_gb300.so"
+PROBE_LIB = PKG / "libmagicube_gb300_probe.so"  # diagnostics (probe.cu), linked against LIB
+PROBE_SRCS = ("probe.cu",)
 CLI = PKG / "cli"
 BIN = PKG / "bin"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -99,10 +101,17 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     jobs = jobs or max(1, min(len(srcs), os.cpu_count() or 4))
     with ThreadPoolExecutor(max_workers=jobs) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
+    lib_objs = [o for o, src in zip(objs, srcs) if src.name not in PROBE_SRCS]
+    probe_objs = [o for o, src in zip(objs, srcs) if src.name in PROBE_SRCS]
+    if not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in lib_objs):
         tmp = LIB.with_suffix(".so.tmp")
-        _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs)])
+        _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, lib_objs)])
         os.replace(tmp, LIB)
+    if not PROBE_LIB.exists() or any(o.stat().st_mtime > PROBE_LIB.stat().st_mtime for o in [*probe_objs, LIB]):
+        tmp = PROBE_LIB.with_suffix(".so.tmp")
+        _run([_nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, probe_objs), "-L", str(PKG), "-lmagicube_gb300",
+              "-Xlinker", "-rpath,$ORIGIN"])
+        os.replace(tmp, PROBE_LIB)
     build_cli()
     return LIB
 

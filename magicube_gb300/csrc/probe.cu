@@ -4,6 +4,7 @@
 #include <cstdint>
 
 #include "mc_host.h"
+#include "../../include/magicube_gb300_probe.h"
 #include "mc_ptx.cuh"
 #include "mc_sm100.cuh"
 

@@ -9,10 +9,11 @@ import pytest
 from magicube_gb300 import _lib
 
 HEADER = Path(__file__).resolve().parent.parent / "include" / "magicube_gb300.h"
+PROBE_HEADER = HEADER.with_name("magicube_gb300_probe.h")
 
 
-def declared_functions() -> list[str]:
-    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+def declared_functions(header: Path = HEADER) -> list[str]:
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
     return sorted(set(re.findall(r"\b(mc[A-Z]\w*)\s*\(", text)))
 
 
@@ -26,6 +27,18 @@ def test_library_exports_every_declared_symbol():
 
 def test_binding_covers_header():
     assert set(declared_functions()) <= set(_lib.exported_symbols())
+
+
+def test_probe_library_exports_its_header_and_product_library_does_not():
+    """The diagnostics live in their own library: it exports every function
+    its header declares, and the product library none of them."""
+    names = declared_functions(PROBE_HEADER)
+    assert len(names) == 4
+    probe = _lib.probe_lib()
+    assert all(hasattr(probe, n) for n in names)
+    import ctypes as _ct
+    product = _ct.CDLL(str(_lib.LIB_PATH))
+    assert not any(hasattr(product, n) for n in names)
 
 
 def test_version():
@@ -98,7 +111,7 @@ def test_tile_mask_words_and_argument_errors():
 
 
 def test_check_entry_points_reject_bad_arguments():
-    lib = _lib.lib()
+    lib = _lib.probe_lib()
     assert lib.mcCheckSmallIntConversions(0, 16, None, None) == 1
     assert lib.mcCheckSmallIntConversions(16, 8, ctypes.c_void_p(8), None) == 1  # lo > hi
     assert lib.mcCheckSmallIntConversions(0, 1 << 33, ctypes.c_void_p(8), None) == 1  # past 32-bit patterns

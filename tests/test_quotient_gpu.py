@@ -22,7 +22,7 @@ def test_quotient_equals_ieee_division(cuda, d):
     lo, hi = -(2 ** 31), 2 ** 31
     counters = torch.tensor([0, hi], dtype=torch.int64, device=cuda)
     stream = torch.cuda.current_stream().cuda_stream
-    _lib.check(_lib.lib().mcCheckQuotients(float(d), lo, hi, counters.data_ptr(), stream), "mcCheckQuotients")
+    _lib.check(_lib.probe_lib().mcCheckQuotients(float(d), lo, hi, counters.data_ptr(), stream), "mcCheckQuotients")
     bad, first = counters.tolist()
     assert bad == 0, f"{bad} mismatches, first numerator {first}"
 
@@ -34,6 +34,6 @@ def test_small_int_conversions_equal_hardware(cuda, lo, hi):
     |f| < 2^22 (bit patterns up to 0x4A800000 = 2^22, both signs)."""
     counters = torch.tensor([0, -1], dtype=torch.int64, device=cuda)
     stream = torch.cuda.current_stream().cuda_stream
-    _lib.check(_lib.lib().mcCheckSmallIntConversions(lo, hi, counters.data_ptr(), stream), "mcCheckSmallIntConversions")
+    _lib.check(_lib.probe_lib().mcCheckSmallIntConversions(lo, hi, counters.data_ptr(), stream), "mcCheckSmallIntConversions")
     bad, first = counters.tolist()
     assert bad == 0, f"{bad} mismatches, first pattern {first & 0xFFFFFFFFFFFFFFFF:#x}"

@@ -109,7 +109,7 @@ def test_tcgen05_throughput_probe(cuda, n):
     import ctypes
     timeouts = torch.zeros(1, dtype=torch.int32, device=cuda)
     ms, ops = ctypes.c_float(), ctypes.c_double()
-    _lib.check(_lib.lib().mcProbeTensorCorePeak(n, 200, ctypes.byref(ms), ctypes.byref(ops), timeouts.data_ptr(),
+    _lib.check(_lib.probe_lib().mcProbeTensorCorePeak(n, 200, ctypes.byref(ms), ctypes.byref(ops), timeouts.data_ptr(),
                                                 ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                "mcProbeTensorCorePeak")
     torch.cuda.synchronize()

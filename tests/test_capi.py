@@ -80,11 +80,7 @@ def test_empty_matrix_is_a_no_op():
 
 @pytest.mark.parametrize("fields,msg", [
     (dict(mma_kind=_lib.MMA_DP4A, lhs_bits=16, rhs_bits=8), b"dp4a"),
-    (dict(mma_kind=6), b"invalid mma_kind"),
-    (dict(mma_kind=_lib.MMA_MIXED, lhs_bits=4, rhs_bits=4), b"mixed"),
-    (dict(mma_kind=_lib.MMA_MIXED, k=128), b"mixed"),
-    (dict(mma_kind=_lib.MMA_MIXED, mix_period=5), b"mix_period"),
-    (dict(mma_kind=_lib.MMA_MIXED, kernel_variant=_lib.KERNEL_PER_ROW), b"mixed"),
+    (dict(mma_kind=5), b"invalid mma_kind"),
     (dict(kernel_variant=_lib.KERNEL_TMA), b"invalid kernel_variant"),
     (dict(kernel_variant=5), b"invalid kernel_variant"),
     (dict(kernel_variant=_lib.KERNEL_DENSE_TILE, lhs_bits=4, rhs_bits=4), b"L8-R8 with k == 64"),

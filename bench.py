@@ -30,7 +30,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-MMA_NAMES = {1: "int8mma", 2: "f16mma", 3: "tcgen05", 4: "dp4a", 5: "int8mma+dp4a"}
+MMA_NAMES = {1: "int8mma", 2: "f16mma", 3: "tcgen05", 4: "dp4a"}
 METRIC = "quantized SpMM/SDDMM TOP/s vs roofline; sparse-attn req/s + p50/p99 latency"
 UNIT = "TOP/s"
 SEQ, HEAD_DIM, VEC, SPARSITY = 4096, 64, 8, 0.9
@@ -359,15 +359,14 @@ def run_gpu(args) -> None:
     results = {}
     launches_per_step = 1
 
-    def sddmm_case(pa, pb, timed_region_clock=False, mma=args.mma, variant=0, V=VEC, sparsity=SPARSITY,
-                   mix_period=args.mix_period):
+    def sddmm_case(pa, pb, timed_region_clock=False, mma=args.mma, variant=0, V=VEC, sparsity=SPARSITY):
         mask, hm, lhs_h, rhs_h = sddmm_workload(pa, pb, B, V=V, sparsity=sparsity)
         dm = ops.DeviceSddmmMask.from_host(hm, dev)
         lhs = torch.from_numpy(lhs_h).to(dev)
         rhs = torch.from_numpy(rhs_h).to(dev)
         out = torch.empty((B, hm.aligned_nnz * V), dtype=torch.int32, device=dev)
         fn = lambda: ops.sddmm(dm, lhs, rhs, HEAD_DIM, pa, pb, signed=True, out=out, batch=B, mma_kind=mma,
-                                    variant=variant, mix_period=mix_period)
+                                    variant=variant)
         sync_all()
         if timed_region_clock:
             with ClockSampler(local) as cs:
@@ -412,7 +411,7 @@ def run_gpu(args) -> None:
         head["lhs"].copy_(lhs_pin, non_blocking=True)
         head["rhs"].copy_(rhs_pin, non_blocking=True)
         ops.sddmm(dm, head["lhs"], head["rhs"], HEAD_DIM, 8, 8, signed=True, out=head["out"], batch=B,
-                  mma_kind=args.mma, mix_period=args.mix_period)
+                  mma_kind=args.mma)
         out_pin.copy_(head["out"], non_blocking=True)
 
     e2e_steps = max(3, args.steps // 4)
@@ -435,21 +434,18 @@ def run_gpu(args) -> None:
                  (16, 8, "sddmm_L16R8_int8mma", 1, 0, VEC)]
         cases += [(8, 8, f"sddmm_L8R8_{MMA_NAMES[m]}", m, 0, VEC) for m in others]
         cases += [(8, 8, "sddmm_L8R8_per_row_kernel", sync_mma, 1, VEC)]
-        # the int8 MMA and dp4a together: every mix_period-th unit on dp4a
-        mixed = [(8, 8, f"sddmm_L8R8_mixed_period{r}", 5, 0, VEC, SPARSITY, r) for r in (2, 3, 4, 6)]
         # V = 2 and 4: the int8 MMA computes 8 lanes of which V are used; dp4a
         # computes only the V lanes
         cases += [(8, 8, f"sddmm_L8R8_V{v}_{MMA_NAMES[m]}", m, 0, v) for v in (2, 4) for m in (1, 4)]
         cases += [(4, 4, f"sddmm_L4R4_V{v}_{MMA_NAMES[m]}", m, 0, v) for v in (2, 4) for m in (1, 4)]
         cases += [(4, 4, "sddmm_L4R4_dp4a", 4, 0, VEC)]
-        cases = [c + (SPARSITY, 0) for c in cases] + mixed
+        cases = [c + (SPARSITY,) for c in cases]
         # every score of 128 x 256 tiles on the tcgen05 f16 tensor cores with a
         # masked epilogue, against the per-nonzero int8 kernel across sparsity
         for sp in (0.5, 0.7, 0.9):
-            cases += [(8, 8, f"sddmm_L8R8_s{sp}_{tag}", 1, var, VEC, sp, 0)
-                      for var, tag in ((0, "k64"), (4, "dense_tile"))]
-        for pa, pb, name, mma, var, v, sp, mp in cases:
-            r = sddmm_case(pa, pb, mma=mma, variant=var, V=v, sparsity=sp, mix_period=mp)
+            cases += [(8, 8, f"sddmm_L8R8_s{sp}_{tag}", 1, var, VEC, sp) for var, tag in ((0, "k64"), (4, "dense_tile"))]
+        for pa, pb, name, mma, var, v, sp in cases:
+            r = sddmm_case(pa, pb, mma=mma, variant=var, V=v, sparsity=sp)
             variants[name] = {"tops": r["tops"], "ms": r["ms"], "gbs": r["gbs"],
                               "hbm_frac": r["gbs"] / peaks["hbm_gbs"],
                               "verified": verify_sddmm(r, pa, pb, v, [B - 1])}
@@ -1154,7 +1150,7 @@ def run_profile_case(args) -> None:
         out = torch.empty((args.batch, hm.aligned_nnz * VEC), dtype=torch.int32, device=dev)
         for _ in range(args.reps):
             ops.sddmm(dm, lhs, rhs, HEAD_DIM, 8, 8, signed=True, out=out, batch=args.batch, mma_kind=args.mma,
-                      variant=args.sddmm_kernel, mix_period=args.mix_period)
+                      variant=args.sddmm_kernel)
     else:
         M = K = 1024
         N = 256
@@ -1192,9 +1188,7 @@ def main() -> None:
     ap.add_argument("--serving-requests", type=int, default=96, help="requests per serving run (0 skips it)")
     ap.add_argument("--serving-overlap-tokens", type=int, default=8192,
                     help="queued tokens at which the server overlaps a new batch with running ones")
-    ap.add_argument("--mix-period", type=int, default=0,
-                    help="--mma mixed: every N-th unit of 32 nonzeros on dp4a (2, 3, 4, 6; 0 = 3)")
-    ap.add_argument("--mma", choices=["int8", "f16", "tc", "dp4a", "mixed"], default="int8",
+    ap.add_argument("--mma", choices=["int8", "f16", "tc", "dp4a"], default="int8",
                     help="arithmetic path of the headline SDDMM: int8 / f16 mma.sync, tcgen05 or CUDA-core dp4a "
                          "(all bit-exact; see include/magicube_gb300.h)")
     ap.add_argument("--sddmm-kernel", choices=["auto", "per_row", "stream", "dense"], default="auto",
@@ -1206,7 +1200,7 @@ def main() -> None:
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    args.mma = {"int8": 1, "f16": 2, "tc": 3, "dp4a": 4, "mixed": 5}[args.mma]
+    args.mma = {"int8": 1, "f16": 2, "tc": 3, "dp4a": 4}[args.mma]
     args.sddmm_kernel = {"auto": 0, "per_row": 1, "stream": 2, "dense": 4}[args.sddmm_kernel]
     if args.sweep:
         run_sweep(args)

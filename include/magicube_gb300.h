@@ -98,12 +98,7 @@ int mcWmmaSddmm_16b(int m_vec, int k, int n, const int* row_indices, const int* 
 /* MC_MMA_DP4A (SDDMM with 8-bit or 4-bit operands): no tensor core; each
  *              vector lane is a chain of CUDA-core dp4a, so V = 2 and V = 4
  *              compute no padding lanes (an int8 MMA always computes 8). */
-/* MC_MMA_MIXED (SDDMM L8-R8 with k == 64): the int8 MMA and dp4a at once --
- *              units of 32 nonzeros alternate between the tensor pipe (two
- *              16-nonzero MMA tiles) and the CUDA cores (one nonzero per
- *              lane, all V dot products), so warps of an SM keep both pipes
- *              busy; mix_period sets the share. */
-enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2, MC_MMA_TCGEN05 = 3, MC_MMA_DP4A = 4, MC_MMA_MIXED = 5 };
+enum { MC_MMA_DEFAULT = 0, MC_MMA_INT8 = 1, MC_MMA_F16 = 2, MC_MMA_TCGEN05 = 3, MC_MMA_DP4A = 4 };
 /* Number of bounded mbarrier waits that ran out in the tcgen05 SDDMM and the
  * TMA SpMM (0 unless the device stalled; an affected launch's results are
  * incomplete).  Synchronous. */
@@ -211,9 +206,6 @@ typedef struct mcSddmmDesc {
      * (mcSddmmTileMask), m_vec x mcSddmmTileMaskWords(n) entries each. */
     const unsigned* tile_bitmap;
     const int* tile_prefix;
-    /* MC_MMA_MIXED only: every mix_period-th unit of 32 nonzeros runs on
-     * dp4a, the others on the int8 MMA (2, 3, 4 or 6; 0 = 3) */
-    int mix_period;
 } mcSddmmDesc;
 int mcSddmm(const mcSddmmDesc* desc, cudaStream_t stream);
 /* Tile bitmap of an SDDMM mask for MC_KERNEL_DENSE_TILE: per vector-row,

@@ -39,7 +39,7 @@ class McSddmmDesc(ctypes.Structure):
         ("rhs", _c_vp), ("rhs_stride", _c_ll),
         ("out", _c_vp), ("out_stride", _c_ll),
         ("mma_kind", _c_int), ("kernel_variant", _c_int),
-        ("tile_bitmap", _c_vp), ("tile_prefix", _c_vp), ("mix_period", _c_int),
+        ("tile_bitmap", _c_vp), ("tile_prefix", _c_vp),
     ]
 
 
@@ -85,7 +85,7 @@ class McDevicePackDesc(ctypes.Structure):
 
 
 REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
-MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05, MMA_DP4A, MMA_MIXED = 0, 1, 2, 3, 4, 5
+MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05, MMA_DP4A = 0, 1, 2, 3, 4
 KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA, KERNEL_DENSE_TILE = 0, 1, 2, 3, 4
 VALUES_PACKED, VALUES_SOFTMAX = 0, 1
 

@@ -87,14 +87,7 @@ static int check_sddmm(const mcSddmmDesc& d)
     if (d.out_half && (!d.is_signed || !d.out_vecmajor))
         return fail(1, "mcSddmm: half output requires is_signed = 1 and out_vecmajor = 1");
     if (d.out_half && !(d.scale != 0.0f)) return fail(1, "mcSddmm: half output requires a nonzero scale");
-    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_MIXED) return fail(1, "mcSddmm: invalid mma_kind");
-    if (d.mma_kind == MC_MMA_MIXED) {
-        if (d.lhs_bits != 8 || d.rhs_bits != 8 || d.k != 64 || d.kernel_variant == MC_KERNEL_PER_ROW ||
-            d.kernel_variant == MC_KERNEL_DENSE_TILE)
-            return fail(1, "mcSddmm: the mixed MMA + dp4a path computes L8-R8 with k == 64 on the pipelined kernel");
-        if (!(d.mix_period == 0 || d.mix_period == 2 || d.mix_period == 3 || d.mix_period == 4 || d.mix_period == 6))
-            return fail(1, "mcSddmm: mix_period must be 0, 2, 3, 4 or 6");
-    }
+    if (d.mma_kind < MC_MMA_DEFAULT || d.mma_kind > MC_MMA_DP4A) return fail(1, "mcSddmm: invalid mma_kind");
     if (d.mma_kind == MC_MMA_DP4A && (d.lhs_bits > 8 || d.rhs_bits > 8))
         return fail(1, "mcSddmm: the dp4a path computes 8-bit and 4-bit operands");
     if (d.mma_kind == MC_MMA_TCGEN05 && (d.lhs_bits != 8 || d.rhs_bits != 8 || d.k != 64))

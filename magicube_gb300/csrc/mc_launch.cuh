@@ -5,7 +5,6 @@
 #include "mc_host.h"
 #include "mc_sddmm.cuh"
 #include "mc_sddmm_dp4a.cuh"
-#include "mc_sddmm_mixed.cuh"
 #include "mc_spmm_n64.cuh"
 #include "mc_sddmm_stream.cuh"
 #include "mc_spmm.cuh"
@@ -251,19 +250,6 @@ int sddmm_launch_dp4a(const mcSddmmDesc& d, const SddmmParams& p, int split, cud
     }
 }
 
-template <int V, bool S, bool VM, bool H>
-int sddmm_launch_mixed(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaStream_t s)
-{
-    dim3 grid((unsigned)d.m_vec, (unsigned)split, (unsigned)d.batch);
-    switch (d.mix_period) {
-        case 2: sddmm_k64_mixed_kernel<V, S, VM, H, 4, 2><<<grid, 128, 0, s>>>(p); break;
-        case 4: sddmm_k64_mixed_kernel<V, S, VM, H, 4, 4><<<grid, 128, 0, s>>>(p); break;
-        case 6: sddmm_k64_mixed_kernel<V, S, VM, H, 4, 6><<<grid, 128, 0, s>>>(p); break;
-        default: sddmm_k64_mixed_kernel<V, S, VM, H, 4, 3><<<grid, 128, 0, s>>>(p); break;
-    }
-    return (int)cudaGetLastError();
-}
-
 // The tcgen05 SDDMM (sddmm_tc.cu).
 int sddmm_tc_launch(const mcSddmmDesc& d, const SddmmParams& p, cudaStream_t s);
 
@@ -272,10 +258,6 @@ int sddmm_launch_v(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaSt
 {
     if (resolve_mma_kind(d.mma_kind) == MC_MMA_TCGEN05) return sddmm_tc_launch(d, p, s);
     if (resolve_mma_kind(d.mma_kind) == MC_MMA_DP4A) return sddmm_launch_dp4a<V, PA, PB, S, VM, H>(d, p, split, s);
-    if (resolve_mma_kind(d.mma_kind) == MC_MMA_MIXED) {
-        if constexpr (PA == 8 && PB == 8) return sddmm_launch_mixed<V, S, VM, H>(d, p, split, s);
-        else return fail(1, "mcSddmm: the mixed MMA + dp4a path computes L8-R8");
-    }
     // MC_MMA_DEFAULT takes the f16 path for L16-R8 on the k == 64 kernel: its
     // two byte planes double the int8 MMAs, and the f16 rate absorbs them
     // (measured 83 vs 70 TOP/s on GB300; the integers are the same)

@@ -120,7 +120,7 @@ def sddmm(mask: DeviceSddmmMask, lhs: torch.Tensor, rhs: torch.Tensor, k: int, l
           signed: bool = True, vecmajor: bool = False, out: torch.Tensor | None = None, out_half: bool = False,
           scale: float = 1.0, batch: int = 1, lhs_stride: int | None = None, rhs_stride: int | None = None,
           out_stride: int | None = None, row_split: int = 0, mma_kind: int = 0, variant: int = 0,
-          mix_period: int = 0, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+          stream: torch.cuda.Stream | None = None) -> torch.Tensor:
     """out = (A * B^T) on the mask's stored nonzero vectors.
 
     lhs: packed A (M rows of k*lhs_bits/8 bytes), rhs: packed B (n rows of
@@ -143,7 +143,7 @@ def sddmm(mask: DeviceSddmmMask, lhs: torch.Tensor, rhs: torch.Tensor, k: int, l
         row_split=row_split, row_indices=mask.row_indices.data_ptr(), row_offsets=mask.row_offsets.data_ptr(),
         column_indices=mask.col_indices.data_ptr(), lhs=lhs.data_ptr(), lhs_stride=lhs_stride,
         rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride, mma_kind=mma_kind,
-        kernel_variant=variant, mix_period=mix_period)
+        kernel_variant=variant)
     if variant == _lib.KERNEL_DENSE_TILE:
         bitmap, prefix = mask.tile_mask(stream)
         d.tile_bitmap, d.tile_prefix = bitmap.data_ptr(), prefix.data_ptr()

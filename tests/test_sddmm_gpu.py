@@ -263,47 +263,3 @@ def test_sddmm_k64_extreme_4bit(cuda, signed, fill, V):
     ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, 4, 4,
                             oracle.SIGNED if signed else oracle.UNSIGNED)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
-
-
-@pytest.mark.parametrize("V", [2, 4, 8])
-@pytest.mark.parametrize("period", [2, 3, 4, 6])
-@pytest.mark.parametrize("layout", ["blocked", "vecmajor", "half"])
-def test_sddmm_mixed_mma_dp4a(cuda, V, period, layout):
-    """MC_MMA_MIXED: units of 32 nonzeros split between the int8 MMA and
-    dp4a, bit-exact against the oracle (ragged rows, many tasks, batch)."""
-    K, N, B = 64, 1024, 2
-    lengths = np.random.default_rng(V + period).integers(0, 120, size=300)
-    lengths[::17] = 0
-    lengths[5] = 1024
-    lengths[6] = 31
-    lengths[7] = 33
-    mask = synth.lengths_mask(lengths, N, V, seed=V * 7 + period)
-    vecmajor = layout != "blocked"
-    hm = formats.prepare_sddmm(mask, alignment=16 if vecmajor else 8)
-    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
-    lhs = np.stack([synth.random_bytes(mask.rows * K, 90 + b) for b in range(B)])
-    rhs = np.stack([synth.random_bytes(N * K, 95 + b) for b in range(B)])
-    kw = dict(signed=True, vecmajor=vecmajor, batch=B, out_half=layout == "half", scale=300.0)
-    lt, rt = torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda)
-    out = ops.sddmm(dm, lt, rt, K, 8, 8, mma_kind=_lib.MMA_MIXED, mix_period=period, **kw)
-    ref_dev = ops.sddmm(dm, lt, rt, K, 8, 8, mma_kind=_lib.MMA_INT8, **kw)
-    torch.cuda.synchronize()
-    assert torch.equal(out, ref_dev)
-    if layout != "half":
-        for b in range(B):
-            ref = oracle.sddmm_host(lhs[b], rhs[b], hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, 8, 8,
-                                    oracle.SIGNED, alignment=8,
-                                    layout=oracle.OUT_VECMAJOR if vecmajor else oracle.OUT_BLOCKED)
-            np.testing.assert_array_equal(out[b].cpu().numpy(), ref)
-
-
-def test_sddmm_mixed_headline_shape(cuda):
-    """The headline SDDMM shape on the mixed path against the oracle."""
-    mask = synth.uniform_mask(512, 4096, 8, 0.9, seed=42)
-    hm = formats.prepare_sddmm(mask)
-    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
-    lhs, rhs = synth.random_bytes(4096 * 64, 1), synth.random_bytes(4096 * 64, 2)
-    out = ops.sddmm(dm, torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda), 64, 8, 8, signed=True,
-                    mma_kind=_lib.MMA_MIXED)
-    ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, 512, 8, 64, 4096, 8, 8, oracle.SIGNED)
-    np.testing.assert_array_equal(out.cpu().numpy(), ref)

@@ -87,9 +87,8 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
     if (warp == CW) {
         // ------------------------------- producer -------------------------------
         if (lane == 0) prefetch_tmap(&tmap);
-        // The next task's metadata is requested one task ahead and each
-        // step's column indices two steps ahead, so no step waits on the
-        // latency of its own index loads.
+        // The next task's metadata and the next step's column indices are
+        // requested one step ahead, so their latency overlaps the ring waits.
         auto load_task = [&](StreamTask& x, int task) {
             x.task = task;
             x.step = 0;
@@ -102,8 +101,8 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
                 x.steps = (x.nnz + 31) >> 5;
             }
         };
-        auto fetch_col = [&](const StreamTask& x, int step) {
-            const int j = 32 * step + lane;
+        auto fetch_col = [&](const StreamTask& x) {
+            const int j = 32 * x.step + lane;
             return (x.task < ntasks && j < x.nnz) ? __ldg(p.col_indices + x.start + col_slot<L::SHUFFLED_COLS>(j))
                                                   : -1;
         };
@@ -114,11 +113,7 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
         StreamTask c, nx;
         load_task(c, blockIdx.x);
         load_task(nx, next_of(blockIdx.x));
-        // the indices of the step after c's current one: c's next step, or
-        // the next task's first (an empty row takes one step)
-        auto fetch_after = [&]() { return c.step + 1 < c.steps ? fetch_col(c, c.step + 1) : fetch_col(nx, 0); };
-        int col = fetch_col(c, 0);
-        int col_next = fetch_after();
+        int col = fetch_col(c);
         int it = 0;
         bool ok = true;
         for (;; ++it) {
@@ -171,8 +166,7 @@ spmm_tma_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams p, co
                 c = nx;
                 load_task(nx, c.task < ntasks ? next_of(c.task) : ntasks);
             }
-            col = col_next;
-            col_next = fetch_after();
+            col = fetch_col(c);
         }
         if (!ok) {
             if (lane == 0) atomicAdd(timeouts, 1u);

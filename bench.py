@@ -1143,6 +1143,24 @@ def run_profile_case(args) -> None:
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "packer", "reps": args.reps}))
         return
+    if args.profile == "spmm-v2":
+        # SpMM L8-R8, M = K = 4096, N = 256, V = 2, sparsity 0.9 (normal row
+        # lengths): about 6 MB per instance
+        M = K = 4096
+        N, V = 256, 2
+        mask = synth.normal_mask(M // V, K, V, SPARSITY, cv=0.3, seed=17)
+        vals = synth.random_bytes(mask.nnz_vec * V, 18)
+        h = formats.prepare_spmm(mask, vals, 8, 8)
+        d = ops.DeviceSpmmLhs.from_host(h, dev)
+        d.values = d.values.repeat(args.batch)
+        rhs = torch.randint(0, 256, (args.batch, K * N), dtype=torch.uint8, device=dev)
+        out = torch.empty((args.batch, M, N), dtype=torch.int32, device=dev)
+        for _ in range(args.reps):
+            ops.spmm(d, rhs, N, signed=True, out=out, batch=args.batch, values_stride=h.values.size,
+                     mma_kind=args.mma)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": args.profile, "batch": args.batch, "reps": args.reps}))
+        return
     if args.profile == "sddmm":
         mask, hm, lhs_h, rhs_h = sddmm_workload(8, 8, args.batch)
         dm = ops.DeviceSddmmMask.from_host(hm, dev)
@@ -1178,7 +1196,8 @@ def main() -> None:
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--requant", choices=["fixed", "rowmax"], default="rowmax",
                     help="requantization of the --profile attention case")
-    ap.add_argument("--profile", choices=["sddmm", "spmm", "attention", "attention-steps", "packer", "projection"],
+    ap.add_argument("--profile", choices=["sddmm", "spmm", "spmm-v2", "attention", "attention-steps", "packer",
+                                          "projection"],
                     default=None,
                     help="run only a small case of one kernel (for ncu captures)")
     ap.add_argument("--reps", type=int, default=3, help="launches of the --profile case")

@@ -100,8 +100,10 @@ def test_oversize_request_is_rejected_not_launched(cuda, monkeypatch):
     """A request whose working set exceeds the free memory of an idle device
     is rejected at admission (never launched); the others are served."""
     enc = _encoder(cuda)
-    reqs = serving.make_requests(4, rate=0.0, **KW)
-    big = max(reqs, key=lambda r: r.seq_len)
+    reqs = serving.make_requests(3, rate=0.0, **dict(KW, clip=(512, 1536)))
+    big = serving.make_requests(1, rate=0.0, **dict(KW, clip=(2048, 2048), seed=99))[0]
+    big.rid = 3
+    reqs.insert(1, big)  # arrives between the others
     srv = serving.ContinuousBatchingServer(enc, hidden=256, heads=4, max_inflight=2, max_batch_tokens=1 << 20,
                                            hbm_reserve=0, device=cuda)
     fit = max(srv.footprint([r]) for r in reqs if r is not big)

@@ -654,11 +654,31 @@ def attention_suite(args, dev) -> dict:
         fused[mode]["_out"] = f.core.out.clone()
         del f
         torch.cuda.empty_cache()
+    # the other precision pairs of the fused kernel (tuned), each against the
+    # separate batched launches of the same pair: L16-R8 (16-bit
+    # probabilities at the full range, fixed requantization) and L8-R4 (4-bit
+    # Q / K / V, row-max requantization)
+    pairs = {}
+    for (lb, rb, mode, s_q, s_p) in ((16, 8, "fixed", sq, 32767.0), (8, 4, "rowmax", 7.0 / amax, 127.0)):
+        key = f"L{lb}R{rb}_{mode}"
+        kw = dict(scale_qkv=s_q, scale_sfmx=s_p, device=dev, requant=mode)
+        f = batched.BatchedSparseAttention(masks, H, d, lb, rb, fused=True, tune=True, **kw)
+        f.qkv.copy_(b.qkv)
+        f.capture()
+        t_f = med(time_cuda(lambda: f.replay(), args.steps, args.warmup, stream))
+        sep = batched.BatchedSparseAttention(masks, H, d, lb, rb, tune=False, **kw)
+        same_bits = bool(torch.equal(sep(b.qkv), f.core.out))
+        pairs[key] = {"ms": t_f, "req_per_s": n_inst / (t_f / 1e3), "tuned": f.core.fused_cfg,
+                      "identical_to_separate_launches": same_bits, "scales": {"qkv": s_q, "softmax": s_p},
+                      "_out": f.core.out.clone()}
+        del f, sep
+        torch.cuda.empty_cache()
     nnz = sum(m.nnz_vec for m in masks)
     ops = 4.0 * nnz * V * d * H
     # accuracy: every instance against the float64 oracle (row-wise form)
-    errs = {"batched_fixed": [], "fused_fixed": [], "fused_rowmax": []}
     outs = {"batched_fixed": b.core.out, "fused_fixed": fused["fixed"]["_out"], "fused_rowmax": fused["rowmax"]["_out"]}
+    outs.update({f"fused_{k}": v["_out"] for k, v in pairs.items()})
+    errs = {k: [] for k in outs}
     for i in range(n_inst):
         a, z = int(b.token_offsets[i]), int(b.token_offsets[i + 1])
         q, k, v = (qkv_host[j, :, a:z].double().numpy() for j in range(3))
@@ -667,7 +687,7 @@ def attention_suite(args, dev) -> dict:
         for key, o in outs.items():
             got = o[:, a:z].double().cpu().numpy()
             errs[key].append(float(np.linalg.norm(got - ref) / nref))
-    for m in fused.values():
+    for m in list(fused.values()) + list(pairs.values()):
         del m["_out"]
     err_summary = {k: {"median": statistics.median(v), "max": max(v), "instances": len(v)} for k, v in errs.items()}
     return {"config": "64 instances x 4 heads, d=64, L ~ U[512,4096], band 256 + random V=8, sparsity 0.9, "
@@ -682,6 +702,7 @@ def attention_suite(args, dev) -> dict:
             "launches": {"batched": 4, "per_instance": 4 * n_inst, "batched_is_cuda_graph": True},
             "results_identical": bool(same), "scales": {"qkv": sq, "softmax": ss},
             "fused": fused,
+            "fused_other_pairs": pairs,
             "rel_error_vs_fp64_all_instances": err_summary,
             "autotuned": {"sddmm": b.core.sddmm_cfg, "spmm": b.core.spmm_cfg}}
 

@@ -232,24 +232,6 @@ int spmm_launch(const mcSpmmDesc& d, cudaStream_t s)
 template <int V, int PA, int PB, bool S, bool VM, bool H, bool F>
 int sddmm_launch_k64(const mcSddmmDesc& d, const SddmmParams& p, int split, cudaStream_t s)
 {
-    if constexpr (!F) {
-        // MC_KERNEL_STREAM with one CTA per vector-row's tiles: the
-        // persistent form (resident CTAs loop over the rows)
-        if (d.kernel_variant == MC_KERNEL_STREAM && split == 1) {
-            const long long ntasks = (long long)d.m_vec * d.batch;
-            if (ntasks > 0x7fffffffLL) return fail(1, "mcSddmm: m_vec * batch too large");
-            if (d.row_split == 1) {
-                auto kern = sddmm_k64_persistent_kernel<V, PA, PB, S, VM, H, 4, 12>;
-                const long long grid = persistent_ctas(kern, 128, ntasks);
-                kern<<<(unsigned)(grid < 1 ? 1 : grid), 128, 0, s>>>(p, (int)ntasks);
-            } else {
-                auto kern = sddmm_k64_persistent_kernel<V, PA, PB, S, VM, H, 4, 16>;
-                const long long grid = persistent_ctas(kern, 128, ntasks);
-                kern<<<(unsigned)(grid < 1 ? 1 : grid), 128, 0, s>>>(p, (int)ntasks);
-            }
-            return (int)cudaGetLastError();
-        }
-    }
     dim3 grid((unsigned)d.m_vec, (unsigned)split, (unsigned)d.batch);
     sddmm_k64_kernel<V, PA, PB, S, VM, H, 4, F><<<grid, 128, 0, s>>>(p);
     return (int)cudaGetLastError();

@@ -26,18 +26,23 @@
 
 namespace mc {
 
-// One warp's share of one vector-row: tiles ti, ti + stride, ... of row
-// `row` of batch entry b (its nonzeros [start, start + nnz)).
-template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, bool F16, int U>
-__device__ __forceinline__ void k64_row(const SddmmParams& p, const Divisor& dq, const int b, const int row,
-                                        const int start, const int nnz, int ti, const int stride)
+template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool F16, int U = 1>
+__global__ void __launch_bounds__(WARPS * 32)
+sddmm_k64_kernel(const SddmmParams p)
 {
+    const Divisor dq = make_divisor(p.scale);  // half output: acc / scale
     constexpr int PA = BytePlanes<PREA>::N, PB = BytePlanes<PREB>::N;
     constexpr int RHS_ROW = 64 * PREB / 8, LHS_ROW = 64 * PREA / 8;
-    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, t = lane & 3;
+    const int row = __ldg(p.row_indices + blockIdx.x);
+    const int b = blockIdx.z;
+    const int start = __ldg(p.row_offsets + 2 * row);
+    const int nnz = __ldg(p.row_offsets + 2 * row + 1) - start;
     const int nnz8 = (nnz + 7) & ~7;
     const int ntiles = (nnz8 + 15) >> 4;
+    const int stride = gridDim.y * WARPS;  // tile stride between this warp's tiles
+    int ti = blockIdx.y * WARPS + warp;
     if (ti >= ntiles) return;
 
     const int* cols = p.col_indices + start;
@@ -184,61 +189,6 @@ __device__ __forceinline__ void k64_row(const SddmmParams& p, const Divisor& dq,
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) { c[u][0] = cn[u][0]; c[u][1] = cn[u][1]; }
-    }
-}
-
-template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, bool F16, int U = 1>
-__global__ void __launch_bounds__(WARPS * 32)
-sddmm_k64_kernel(const SddmmParams p)
-{
-    const Divisor dq = make_divisor(p.scale);  // half output: acc / scale
-    const int warp = threadIdx.x >> 5;
-    const int row = __ldg(p.row_indices + blockIdx.x);
-    const int start = __ldg(p.row_offsets + 2 * row);
-    const int nnz = __ldg(p.row_offsets + 2 * row + 1) - start;
-    k64_row<V, PREA, PREB, SIGNED, VECMAJOR, HALF_OUT, F16, U>(p, dq, blockIdx.z, row, start, nnz,
-                                                                blockIdx.y * WARPS + warp, gridDim.y * WARPS);
-}
-
-// Persistent form of sddmm_k64_kernel: CTA c takes tasks c, c + G, ... (a
-// task is one vector-row of one batch entry, the batch entry varying
-// slowest) and its warps split each task's tiles as one CTA per row does.
-// The next task's offsets are requested while the current task runs and
-// the row index of the task after it one task earlier, so a warp starts a
-// row with one dependent load (the A rows and the first column indices)
-// instead of the four of a fresh CTA.
-template <int V, int PREA, int PREB, bool SIGNED, bool VECMAJOR, bool HALF_OUT, int WARPS, int MINB>
-__global__ void __launch_bounds__(WARPS * 32, MINB)
-sddmm_k64_persistent_kernel(const SddmmParams p, const int ntasks)
-{
-    const Divisor dq = make_divisor(p.scale);
-    const int warp = threadIdx.x >> 5;
-    const int G = gridDim.x;
-    auto row_of = [&](int task) { return __ldg(p.row_indices + (task - (task / p.m_vec) * p.m_vec)); };
-    int task = blockIdx.x;
-    if (task >= ntasks) return;
-    int row = row_of(task);
-    int start = __ldg(p.row_offsets + 2 * row);
-    int end = __ldg(p.row_offsets + 2 * row + 1);
-    int nrow = task + G < ntasks ? row_of(task + G) : 0;
-    int nnrow = task + 2 * G < ntasks ? row_of(task + 2 * G) : 0;
-#pragma unroll 1
-    for (;;) {
-        const int nt = task + G;
-        int nstart = 0, nend = 0;
-        if (nt < ntasks) {
-            nstart = __ldg(p.row_offsets + 2 * nrow);
-            nend = __ldg(p.row_offsets + 2 * nrow + 1);
-        }
-        k64_row<V, PREA, PREB, SIGNED, VECMAJOR, HALF_OUT, false, 1>(p, dq, task / p.m_vec, row, start, end - start,
-                                                                     warp, WARPS);
-        if (nt >= ntasks) break;
-        task = nt;
-        row = nrow;
-        start = nstart;
-        end = nend;
-        nrow = nnrow;
-        nnrow = task + 2 * G < ntasks ? row_of(task + 2 * G) : 0;
     }
 }
 

@@ -263,36 +263,3 @@ def test_sddmm_k64_extreme_4bit(cuda, signed, fill, V):
     ref = oracle.sddmm_host(lhs, rhs, hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, 4, 4,
                             oracle.SIGNED if signed else oracle.UNSIGNED)
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
-
-
-@pytest.mark.parametrize("pa,pb", [(8, 8), (4, 4), (16, 8)])
-@pytest.mark.parametrize("V", [2, 8])
-@pytest.mark.parametrize("split", [0, 1])
-@pytest.mark.parametrize("layout", ["blocked", "vecmajor", "half"])
-def test_sddmm_persistent_k64(cuda, pa, pb, V, split, layout):
-    """The persistent k = 64 kernel (MC_KERNEL_STREAM with one CTA per row's
-    tiles): resident CTAs loop over (batch entry, vector-row) tasks with the
-    next rows' offsets requested ahead; bit-exact against the oracle on
-    ragged rows and many tasks per CTA."""
-    K, N, B = 64, 1024, 3
-    lengths = np.random.default_rng(V + pa + split).integers(0, 120, size=3000)
-    lengths[::17] = 0
-    lengths[5] = 1024
-    mask = synth.lengths_mask(lengths, N, V, seed=V * 7 + pa)
-    vecmajor = layout != "blocked"
-    hm = formats.prepare_sddmm(mask, alignment=16 if vecmajor else 8)
-    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
-    lhs = np.stack([synth.random_bytes(mask.rows * K * pa // 8, 90 + b) for b in range(B)])
-    rhs = np.stack([synth.random_bytes(N * K * pb // 8, 95 + b) for b in range(B)])
-    lt, rt = torch.from_numpy(lhs).to(cuda), torch.from_numpy(rhs).to(cuda)
-    kw = dict(signed=True, vecmajor=vecmajor, batch=B, out_half=layout == "half", scale=300.0, mma_kind=_lib.MMA_INT8)
-    out = ops.sddmm(dm, lt, rt, K, pa, pb, variant=_lib.KERNEL_STREAM, row_split=split, **kw)
-    ref_dev = ops.sddmm(dm, lt, rt, K, pa, pb, variant=_lib.KERNEL_PER_ROW, **kw)
-    torch.cuda.synchronize()
-    assert torch.equal(out, ref_dev)
-    if layout != "half":
-        for b in range(B):
-            ref = oracle.sddmm_host(lhs[b], rhs[b], hm.row_offsets, hm.col_indices, mask.m_vec, V, K, N, pa, pb,
-                                    oracle.SIGNED, alignment=8,
-                                    layout=oracle.OUT_VECMAJOR if vecmajor else oracle.OUT_BLOCKED)
-            np.testing.assert_array_equal(out[b].cpu().numpy(), ref)

@@ -654,6 +654,21 @@ def attention_suite(args, dev) -> dict:
         fused[mode]["_out"] = f.core.out.clone()
         del f
         torch.cuda.empty_cache()
+    # the same row-max attention through the library's C++ engine
+    # (mcAttnBatch*: mask builder, quantize + fused launch, its own tuner and
+    # CUDA graph; no PyTorch on the path)
+    eng = batched.NativeBatchedSparseAttention(masks, H, d, 8, 8, scale_qkv=sq, scale_sfmx=ss, device=dev,
+                                               requant="rowmax")
+    eng.qkv.copy_(b.qkv)
+    eng.tune()
+    eng.capture()
+    t_e = med(time_cuda(lambda: eng.replay(), args.steps, args.warmup, stream))
+    native = {"ms": t_e, "req_per_s": n_inst / (t_e / 1e3), "tuned": eng.config,
+              "speedup_vs_per_instance_graph": base["rowmax"]["graph_ms"] / t_e,
+              "identical_to_python_fused": bool(torch.equal(eng.out, fused["rowmax"]["_out"])),
+              "launches": 2, "status": eng.status()}
+    del eng
+    torch.cuda.empty_cache()
     # the other precision pairs of the fused kernel (tuned), each against the
     # separate batched launches of the same pair: L16-R8 (16-bit
     # probabilities at the full range, fixed requantization) and L8-R4 (4-bit
@@ -703,6 +718,7 @@ def attention_suite(args, dev) -> dict:
             "results_identical": bool(same), "scales": {"qkv": sq, "softmax": ss},
             "fused": fused,
             "fused_other_pairs": pairs,
+            "native_engine_rowmax": native,
             "rel_error_vs_fp64_all_instances": err_summary,
             "autotuned": {"sddmm": b.core.sddmm_cfg, "spmm": b.core.spmm_cfg}}
 

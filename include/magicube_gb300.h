@@ -318,6 +318,48 @@ typedef struct mcQkvProjDesc {
 } mcQkvProjDesc;
 int mcQkvProjectQuantize(const mcQkvProjDesc* desc, cudaStream_t stream);
 
+/* ---- Batched attention engine (host C++, no PyTorch) -------------------------
+ * The reference runs its sparse attention one sequence at a time, four
+ * launches each, from Python (spattention.py:189-216).  mcAttnBatch holds the
+ * attention of `n_instances` sequences of different lengths and masks, all
+ * heads, as one problem: mcAttnBatchCreate stacks the instances' masks into
+ * one block-diagonal vector-sparse mask (rows stacked, each instance's
+ * columns offset by its first token), packs it (aligned pairs, padded
+ * columns, longest-first row order) and keeps it and the quantized operands
+ * on the device; mcAttnBatchRun is then two launches (mcQuantize, then the
+ * fused mcSparseAttention) for every instance and head.  Results equal the
+ * separate launches of the same pair and requantization mode, bit for bit.
+ *   qkv: device half [3][heads][T][head_dim], the instances' tokens back to
+ *        back (T = total tokens, instance i from token_offsets[i]);
+ *   out: device half [heads][T][head_dim].
+ * mcAttnBatchTune times the fused kernel's launch configurations (warps per
+ * CTA 4 / 8, ring stages 2 / 3, CTAs per SM unlimited / 2 / 4) on these
+ * buffers and keeps the fastest (the same bits for every choice).
+ * mcAttnBatchCapture records Run on `stream` (not the legacy default stream)
+ * into a CUDA graph; mcAttnBatchReplay launches that graph. */
+typedef struct mcAttnBatch mcAttnBatch;
+typedef struct mcAttnBatchDesc {
+    int n_instances;
+    const int* seq_lens;            /* tokens per instance, multiples of vec_length */
+    const int* const* row_offsets;  /* per instance, host: plain vector CSR, seq_len / vec_length + 1 entries */
+    const int* const* col_indices;  /* per instance, host: column vectors in [0, seq_len) */
+    int vec_length, heads, head_dim; /* V = 2, 4, 8; head_dim 64 */
+    int lhs_bits, rhs_bits;         /* probabilities, Q/K/V: (8, 8), (16, 8) or (8, 4) */
+    int requant;                    /* MC_REQUANT_FIXED or MC_REQUANT_ROWMAX (8-bit probabilities) */
+    float scale_qkv, scale_sfmx;    /* quantization scale of Q/K/V; fixed requantization scale */
+} mcAttnBatchDesc;
+int mcAttnBatchCreate(const mcAttnBatchDesc* desc, mcAttnBatch** batch);
+/* token_offsets: host array of n_instances + 1 entries. */
+int mcAttnBatchTokens(const mcAttnBatch* batch, long long* token_offsets);
+int mcAttnBatchRun(mcAttnBatch* batch, const void* qkv, void* out, cudaStream_t stream);
+int mcAttnBatchTune(mcAttnBatch* batch, const void* qkv, void* out, cudaStream_t stream, int* warps, int* stages,
+                    int* ctas_per_sm);
+int mcAttnBatchCapture(mcAttnBatch* batch, const void* qkv, void* out, cudaStream_t stream);
+int mcAttnBatchReplay(mcAttnBatch* batch, cudaStream_t stream);
+/* Synchronous: 0, or 1 if a row exceeded the fused kernel's limit. */
+int mcAttnBatchStatus(mcAttnBatch* batch, int* status);
+void mcAttnBatchDestroy(mcAttnBatch* batch);
+
 /* ---- Host-side format conversion (host pointers) ---------------------------
  * The reference's host packer (SpMM/SpMM/spmm_benchmark.cpp:177-377,
  * SDDMM/SDDMM/sddmm_benchmark.cpp:104-127) as library routines. */

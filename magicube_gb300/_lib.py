@@ -84,6 +84,14 @@ class McDevicePackDesc(ctypes.Structure):
     ]
 
 
+class McAttnBatchDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_instances", _c_int), ("seq_lens", _c_vp), ("row_offsets", _c_vp), ("col_indices", _c_vp),
+        ("vec_length", _c_int), ("heads", _c_int), ("head_dim", _c_int), ("lhs_bits", _c_int), ("rhs_bits", _c_int),
+        ("requant", _c_int), ("scale_qkv", _c_float), ("scale_sfmx", _c_float),
+    ]
+
+
 REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
 MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05, MMA_DP4A = 0, 1, 2, 3, 4
 KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA, KERNEL_DENSE_TILE = 0, 1, 2, 3, 4
@@ -117,6 +125,14 @@ _SIGNATURES = {
     "mcDeviceSortedRowSwizzle": (_c_int, [_c_int, _c_vp, _c_vp, _c_vp]),
     "mcDevicePack": (_c_int, [ctypes.POINTER(McDevicePackDesc), _c_vp]),
     "mcQkvProjectQuantize": (_c_int, [ctypes.POINTER(McQkvProjDesc), _c_vp]),
+    "mcAttnBatchCreate": (_c_int, [ctypes.POINTER(McAttnBatchDesc), ctypes.POINTER(_c_vp)]),
+    "mcAttnBatchTokens": (_c_int, [_c_vp, ctypes.POINTER(_c_ll)]),
+    "mcAttnBatchRun": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "mcAttnBatchTune": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _IP, _IP, _IP]),
+    "mcAttnBatchCapture": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "mcAttnBatchReplay": (_c_int, [_c_vp, _c_vp]),
+    "mcAttnBatchStatus": (_c_int, [_c_vp, _IP]),
+    "mcAttnBatchDestroy": (None, [_c_vp]),
 }
 # the diagnostics library (include/magicube_gb300_probe.h)
 _PROBE_SIGNATURES = {

@@ -310,3 +310,82 @@ class PerInstanceSparseAttention:
     def replay(self) -> list[torch.Tensor]:
         self._graph.replay()
         return [c.out for c in self.cores]
+
+
+class NativeBatchedSparseAttention:
+    """The same batched attention through the library's C++ engine
+    (mcAttnBatch*): the block-diagonal mask is built and packed by the
+    library, and every run is mcQuantize + the fused kernel, optionally
+    replayed from a CUDA graph the library records -- no PyTorch on the
+    path (torch only provides the device buffers here)."""
+
+    def __init__(self, masks: list[VectorSparse], heads: int, head_dim: int = 64, lhs_bits: int = 8,
+                 rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 32.0, device="cuda",
+                 requant: str = "fixed"):
+        self._ro = [np.ascontiguousarray(m.row_offsets, dtype=np.int32) for m in masks]
+        self._ci = [np.ascontiguousarray(m.col_indices if m.col_indices.size else np.zeros(1, np.int32),
+                                         dtype=np.int32) for m in masks]
+        lens = np.array([m.ncols for m in masks], dtype=np.int32)
+        ro_ptrs = (ctypes.c_void_p * len(masks))(*[a.ctypes.data for a in self._ro])
+        ci_ptrs = (ctypes.c_void_p * len(masks))(*[a.ctypes.data for a in self._ci])
+        d = _lib.McAttnBatchDesc(
+            n_instances=len(masks), seq_lens=lens.ctypes.data, row_offsets=ctypes.addressof(ro_ptrs),
+            col_indices=ctypes.addressof(ci_ptrs), vec_length=masks[0].vec_length, heads=heads, head_dim=head_dim,
+            lhs_bits=lhs_bits, rhs_bits=rhs_bits,
+            requant=_lib.REQUANT_ROWMAX if requant == "rowmax" else _lib.REQUANT_FIXED,
+            scale_qkv=scale_qkv, scale_sfmx=scale_sfmx)
+        self._h = ctypes.c_void_p()
+        _lib.check(_lib.lib().mcAttnBatchCreate(ctypes.byref(d), ctypes.byref(self._h)), "mcAttnBatchCreate")
+        offs = (ctypes.c_longlong * (len(masks) + 1))()
+        _lib.check(_lib.lib().mcAttnBatchTokens(self._h, offs), "mcAttnBatchTokens")
+        self.token_offsets = np.array(offs[:], dtype=np.int64)
+        T = int(self.token_offsets[-1])
+        self.qkv = torch.zeros((3, heads, T, head_dim), dtype=torch.float16, device=device)
+        self.out = torch.empty((heads, T, head_dim), dtype=torch.float16, device=device)
+        self.config: dict | None = None
+
+    @staticmethod
+    def _stream() -> ctypes.c_void_p:
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def __call__(self) -> torch.Tensor:
+        _lib.check(_lib.lib().mcAttnBatchRun(self._h, self.qkv.data_ptr(), self.out.data_ptr(), self._stream()),
+                   "mcAttnBatchRun")
+        return self.out
+
+    def tune(self) -> dict:
+        w, st, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.lib().mcAttnBatchTune(self._h, self.qkv.data_ptr(), self.out.data_ptr(), self._stream(),
+                                              ctypes.byref(w), ctypes.byref(st), ctypes.byref(c)), "mcAttnBatchTune")
+        self.config = {"warps": w.value, "stages": st.value, "ctas_per_sm": c.value}
+        return self.config
+
+    def capture(self) -> "NativeBatchedSparseAttention":
+        """Record the run in a CUDA graph on a side stream (the library's
+        capture needs a created stream)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            _lib.check(_lib.lib().mcAttnBatchCapture(self._h, self.qkv.data_ptr(), self.out.data_ptr(),
+                                                     self._stream()), "mcAttnBatchCapture")
+        torch.cuda.current_stream().wait_stream(s)
+        return self
+
+    def replay(self) -> torch.Tensor:
+        _lib.check(_lib.lib().mcAttnBatchReplay(self._h, self._stream()), "mcAttnBatchReplay")
+        return self.out
+
+    def status(self) -> int:
+        st = ctypes.c_int()
+        _lib.check(_lib.lib().mcAttnBatchStatus(self._h, ctypes.byref(st)), "mcAttnBatchStatus")
+        return st.value
+
+    def instance_output(self, i: int) -> torch.Tensor:
+        a, b = int(self.token_offsets[i]), int(self.token_offsets[i + 1])
+        return self.out[:, a:b]
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.lib().mcAttnBatchDestroy(h)
+            self._h = ctypes.c_void_p()

@@ -111,3 +111,36 @@ def test_check_entry_points_reject_bad_arguments():
     assert lib.mcCheckSmallIntConversions(0, 16, None, None) == 1
     assert lib.mcCheckSmallIntConversions(16, 8, ctypes.c_void_p(8), None) == 1  # lo > hi
     assert lib.mcCheckSmallIntConversions(0, 1 << 33, ctypes.c_void_p(8), None) == 1  # past 32-bit patterns
+
+
+def test_attention_batch_engine_rejects_bad_descriptors():
+    """mcAttnBatchCreate validates everything before touching a GPU."""
+    lib = _lib.lib()
+    h = ctypes.c_void_p()
+    ro = (ctypes.c_int * 3)(0, 1, 2)
+    ci = (ctypes.c_int * 2)(0, 1)
+    ro_p = (ctypes.c_void_p * 1)(ctypes.addressof(ro))
+    ci_p = (ctypes.c_void_p * 1)(ctypes.addressof(ci))
+    lens = (ctypes.c_int * 1)(16)
+
+    def desc(**kw):
+        base = dict(n_instances=1, seq_lens=ctypes.addressof(lens), row_offsets=ctypes.addressof(ro_p),
+                    col_indices=ctypes.addressof(ci_p), vec_length=8, heads=1, head_dim=64, lhs_bits=8,
+                    rhs_bits=8, requant=0, scale_qkv=1.0, scale_sfmx=1.0)
+        base.update(kw)
+        return _lib.McAttnBatchDesc(**base)
+
+    lens12 = (ctypes.c_int * 1)(12)
+    for kw, msg in ((dict(n_instances=0), b"instance"), (dict(vec_length=3), b"vec_length"),
+                    (dict(head_dim=128), b"head_dim"), (dict(lhs_bits=4, rhs_bits=4), b"pairs"),
+                    (dict(lhs_bits=16, requant=1), b"row-max"), (dict(scale_qkv=0.0), b"scales"),
+                    (dict(seq_lens=ctypes.addressof(lens12)), b"multiple of V")):
+        d = desc(**kw)
+        assert lib.mcAttnBatchCreate(ctypes.byref(d), ctypes.byref(h)) == 1
+        assert msg in lib.mcGetLastErrorString(), (kw, lib.mcGetLastErrorString())
+    bad = (ctypes.c_int * 2)(0, 99)
+    ci_bad = (ctypes.c_void_p * 1)(ctypes.addressof(bad))
+    d = desc(col_indices=ctypes.addressof(ci_bad))
+    assert lib.mcAttnBatchCreate(ctypes.byref(d), ctypes.byref(h)) == 1
+    assert b"outside" in lib.mcGetLastErrorString()
+    assert lib.mcAttnBatchReplay(None, None) == 1

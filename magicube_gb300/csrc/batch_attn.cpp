@@ -77,21 +77,15 @@ int check_desc(const mcAttnBatchDesc& d)
     return 0;
 }
 
-}  // namespace
-
-extern "C" {
-
-int mcAttnBatchCreate(const mcAttnBatchDesc* desc, mcAttnBatch** batch)
+// The instances' CSRs stacked into one block-diagonal plain CSR (host):
+// ro (m + 1 offsets), ci (columns offset by each instance's first token),
+// toks (token offsets, n_instances + 1).
+int stack_masks(const mcAttnBatchDesc& d, std::vector<int>& ro, std::vector<int>& ci, std::vector<long long>& toks)
 {
-    mc::clear_error();
-    if (!desc || !batch) return mc::fail(1, "mcAttnBatchCreate: null argument");
-    *batch = nullptr;
-    const mcAttnBatchDesc& d = *desc;
-    if (int rc = check_desc(d)) return rc;
     const int V = d.vec_length;
-    // stack the instances' CSRs (host)
-    std::vector<int> ro(1, 0), ci;
-    std::vector<long long> toks(1, 0);
+    ro.assign(1, 0);
+    ci.clear();
+    toks.assign(1, 0);
     for (int i = 0; i < d.n_instances; ++i) {
         const int L = d.seq_lens[i];
         if (L <= 0 || L % V) return mc::fail(1, "mcAttnBatchCreate: every length must be a positive multiple of V");
@@ -113,24 +107,15 @@ int mcAttnBatchCreate(const mcAttnBatchDesc* desc, mcAttnBatch** batch)
         toks.push_back(tok + L);
     }
     if (toks.back() > 0x7fffffffLL) return mc::fail(1, "mcAttnBatchCreate: too many tokens");
-    const int m = (int)(ro.size() - 1);
-    const int align = d.rhs_bits == 8 ? 16 : 32;
-    std::vector<int> pairs(2 * (size_t)m), ri(std::max(m, 1));
-    const int n_al = mcAlignRowOffsets(m, ro.data(), align, pairs.data());
-    if (n_al < 0) return mc::fail(1, "mcAttnBatchCreate: aligned slot count overflows");
-    std::vector<int> cols(std::max<size_t>((size_t)n_al, 1), -1);
-    if (int rc = mcPadColumnIndices(m, ro.data(), ci.empty() ? nullptr : ci.data(), pairs.data(), n_al, 0,
-                                    cols.data()))
-        return rc;
-    if (int rc = mcSortedRowSwizzle(m, ro.data(), ri.data())) return rc;
-    int longest = 0;
-    for (int v = 0; v < m; ++v) longest = std::max(longest, ro[v + 1] - ro[v]);
-    if (longest > 4096) return mc::fail(1, "mcAttnBatchCreate: rows of at most 4096 nonzero vectors");
+    return 0;
+}
 
+mcAttnBatch* new_batch(const mcAttnBatchDesc& d, int m, int longest, const std::vector<long long>& toks)
+{
     mcAttnBatch* b = new (std::nothrow) mcAttnBatch;
-    if (!b) return mc::fail(1, "mcAttnBatchCreate: out of host memory");
+    if (!b) return nullptr;
     b->n_instances = d.n_instances;
-    b->V = V;
+    b->V = d.vec_length;
     b->heads = d.heads;
     b->d = d.head_dim;
     b->lb = d.lhs_bits;
@@ -142,6 +127,45 @@ int mcAttnBatchCreate(const mcAttnBatchDesc* desc, mcAttnBatch** batch)
     b->max_row_nnz = longest;
     b->tokens = toks.back();
     b->token_offsets = toks;
+    return b;
+}
+
+int longest_row(const std::vector<int>& ro)
+{
+    int longest = 0;
+    for (size_t v = 0; v + 1 < ro.size(); ++v) longest = std::max(longest, ro[v + 1] - ro[v]);
+    return longest;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcAttnBatchCreate(const mcAttnBatchDesc* desc, mcAttnBatch** batch)
+{
+    mc::clear_error();
+    if (!desc || !batch) return mc::fail(1, "mcAttnBatchCreate: null argument");
+    *batch = nullptr;
+    const mcAttnBatchDesc& d = *desc;
+    if (int rc = check_desc(d)) return rc;
+    std::vector<int> ro, ci;
+    std::vector<long long> toks;
+    if (int rc = stack_masks(d, ro, ci, toks)) return rc;
+    const int m = (int)(ro.size() - 1);
+    const int align = d.rhs_bits == 8 ? 16 : 32;
+    std::vector<int> pairs(2 * (size_t)m), ri(std::max(m, 1));
+    const int n_al = mcAlignRowOffsets(m, ro.data(), align, pairs.data());
+    if (n_al < 0) return mc::fail(1, "mcAttnBatchCreate: aligned slot count overflows");
+    std::vector<int> cols(std::max<size_t>((size_t)n_al, 1), -1);
+    if (int rc = mcPadColumnIndices(m, ro.data(), ci.empty() ? nullptr : ci.data(), pairs.data(), n_al, 0,
+                                    cols.data()))
+        return rc;
+    if (int rc = mcSortedRowSwizzle(m, ro.data(), ri.data())) return rc;
+    const int longest = longest_row(ro);
+    if (longest > 4096) return mc::fail(1, "mcAttnBatchCreate: rows of at most 4096 nonzero vectors");
+
+    mcAttnBatch* b = new_batch(d, m, longest, toks);
+    if (!b) return mc::fail(1, "mcAttnBatchCreate: out of host memory");
     int rc = upload(&b->row_indices, ri);
     if (!rc) rc = upload(&b->pairs, pairs);
     if (!rc) rc = upload(&b->cols, std::vector<int>(cols.begin(), cols.begin() + n_al));

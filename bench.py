@@ -451,7 +451,8 @@ def run_gpu(args) -> None:
                               "verified": verify_sddmm(r, pa, pb, v, [B - 1])}
             del r
             torch.cuda.empty_cache()
-        for mma, var, tag in ((1, 0, MMA_NAMES[1]), (2, 0, MMA_NAMES[2]), (sync_mma, 1, "per_row_kernel")):
+        for mma, var, tag in ((1, 0, MMA_NAMES[1]), (1, 5, "resident_slice"), (2, 0, MMA_NAMES[2]),
+                              (sync_mma, 1, "per_row_kernel")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
         # small vectors: an int8 MMA computes 8 vector lanes of which V are
@@ -1194,7 +1195,7 @@ def run_profile_case(args) -> None:
         out = torch.empty((args.batch, M, N), dtype=torch.int32, device=dev)
         for _ in range(args.reps):
             ops.spmm(d, rhs, N, signed=True, out=out, batch=args.batch, values_stride=h.values.size,
-                     mma_kind=args.mma)
+                     mma_kind=args.mma, variant=args.spmm_kernel)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": args.profile, "batch": args.batch, "reps": args.reps}))
         return
@@ -1218,7 +1219,7 @@ def run_profile_case(args) -> None:
         out = torch.empty((args.batch, M, N), dtype=torch.int32, device=dev)
         for _ in range(args.reps):
             ops.spmm(d, rhs, N, signed=True, out=out, batch=args.batch, values_stride=h.values.size,
-                     mma_kind=args.mma)
+                     mma_kind=args.mma, variant=args.spmm_kernel)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": args.profile, "batch": args.batch, "reps": args.reps}))
 
@@ -1249,6 +1250,8 @@ def main() -> None:
                          "(all bit-exact; see include/magicube_gb300.h)")
     ap.add_argument("--sddmm-kernel", choices=["auto", "per_row", "stream", "dense"], default="auto",
                     help="SDDMM kernel variant of the --profile sddmm case")
+    ap.add_argument("--spmm-kernel", choices=["auto", "per_row", "stream", "tma", "resident"], default="auto",
+                    help="SpMM kernel variant of the --profile spmm and spmm-v2 cases")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", choices=["square", "full"], default=None,
                     help="run only the SpMM precision/shape sweep (M = K, or every M, K pair)")
@@ -1258,6 +1261,7 @@ def main() -> None:
         args.warmup = 3
     args.mma = {"int8": 1, "f16": 2, "tc": 3, "dp4a": 4}[args.mma]
     args.sddmm_kernel = {"auto": 0, "per_row": 1, "stream": 2, "dense": 4}[args.sddmm_kernel]
+    args.spmm_kernel = {"auto": 0, "per_row": 1, "stream": 2, "tma": 3, "resident": 5}[args.spmm_kernel]
     if args.sweep:
         run_sweep(args)
     elif args.profile:

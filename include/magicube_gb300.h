@@ -134,11 +134,22 @@ int mcSetDefaultMmaKind(int kind);
  *                    not read).  Wins where the mask is dense enough that a
  *                    dense tile costs less than per-nonzero gathers (about
  *                    sparsity <= 0.95 on GB300).
+ * MC_KERNEL_RESIDENT: SpMM only, on the int8 path: each CTA holds a K x 64-byte
+ *                    column slice of B in shared memory (loaded once by TMA)
+ *                    and its warps gather the rows of their vector-rows'
+ *                    nonzeros from there with ldmatrix (needs 8-bit B with
+ *                    n % 64 == 0 or 4-bit B with n % 128 == 0, 4-, 8- or
+ *                    16-bit A, k <= 3584, 16-byte aligned values,
+ *                    values_stride and rhs, rhs_stride a multiple of the B
+ *                    row bytes).
  * MC_KERNEL_AUTO:    SpMM: the TMA kernel where it applies, else the
  *                    streaming kernel (the warp-per-row one for the n == 64
  *                    attention shape), else per-row; SDDMM: the pipelined
  *                    kernel where it applies, else per-row. */
-enum { MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2, MC_KERNEL_TMA = 3, MC_KERNEL_DENSE_TILE = 4 };
+enum {
+    MC_KERNEL_AUTO = 0, MC_KERNEL_PER_ROW = 1, MC_KERNEL_STREAM = 2, MC_KERNEL_TMA = 3, MC_KERNEL_DENSE_TILE = 4,
+    MC_KERNEL_RESIDENT = 5
+};
 
 /* ---- Value layouts of the SpMM sparse operand --------------------------------
  * MC_VALUES_PACKED:  the reference host packer's layout (what
@@ -176,13 +187,22 @@ typedef struct mcSpmmDesc {
     const void* rhs;      long long rhs_stride;     /* bytes */
     void* out;            long long out_stride;     /* elements */
     int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
-    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM / _TMA */
+    int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM / _TMA / _RESIDENT */
     int value_layout;           /* MC_VALUES_PACKED / MC_VALUES_SOFTMAX */
     /* Optional, half output only: out[row][c] = half(acc / row_div[row]) per
      * output row (M = m_vec * vec_length floats per batch entry, e.g. the
      * divisors mcQuantSoftmax writes with MC_REQUANT_ROWMAX) instead of / scale. */
     const void* row_div;  long long row_div_stride;  /* floats between batch entries */
+    /* MC_KERNEL_RESIDENT only: slice width and CTA size (MC_RESIDENT_*);
+     * 0 = automatic.  Other variants ignore it. */
+    int kernel_config;
 } mcSpmmDesc;
+/* Configurations of MC_KERNEL_RESIDENT: 64-byte slice rows (64 columns of
+ * 8-bit B, 128 of 4-bit B) with 8 or 16 warps a CTA, 128-byte slice rows
+ * (k <= 1792, n a multiple of 128 / 256 columns) with 16 warps.  The
+ * 16-warp ones run V = 8 on the int8 tensor path, not with 16-bit A and
+ * 4-bit B; 128-byte slices with 4- or 8-bit A. */
+enum { MC_RESIDENT_AUTO = 0, MC_RESIDENT_S64_W8 = 1, MC_RESIDENT_S64_W16 = 2, MC_RESIDENT_S128_W16 = 3 };
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream);
 
 typedef struct mcSddmmDesc {

@@ -26,6 +26,7 @@ class McSpmmDesc(ctypes.Structure):
         ("out", _c_vp), ("out_stride", _c_ll),
         ("mma_kind", _c_int), ("kernel_variant", _c_int), ("value_layout", _c_int),
         ("row_div", _c_vp), ("row_div_stride", _c_ll),
+        ("kernel_config", _c_int),
     ]
 
 
@@ -94,7 +95,8 @@ class McAttnBatchDesc(ctypes.Structure):
 
 REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
 MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05, MMA_DP4A = 0, 1, 2, 3, 4
-KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA, KERNEL_DENSE_TILE = 0, 1, 2, 3, 4
+KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA, KERNEL_DENSE_TILE, KERNEL_RESIDENT = 0, 1, 2, 3, 4, 5
+RESIDENT_AUTO, RESIDENT_S64_W8, RESIDENT_S64_W16, RESIDENT_S128_W16 = 0, 1, 2, 3
 VALUES_PACKED, VALUES_SOFTMAX = 0, 1
 
 # name -> (restype, argtypes)

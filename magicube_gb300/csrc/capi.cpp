@@ -55,8 +55,11 @@ static int check_spmm(const mcSpmmDesc& d)
         return fail(1, "mcSpmm: invalid mma_kind (the SpMM runs on MC_MMA_INT8, MC_MMA_F16 or MC_MMA_DP4A)");
     if (d.mma_kind == MC_MMA_DP4A && (d.lhs_bits > 8 || d.rhs_bits > 8 || d.vec_length > 4))
         return fail(1, "mcSpmm: the dp4a SpMM computes V = 2 and 4 with 8-bit or 4-bit operands");
-    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_TMA)
+    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_RESIDENT ||
+        d.kernel_variant == MC_KERNEL_DENSE_TILE)
         return fail(1, "mcSpmm: invalid kernel_variant");
+    if (d.kernel_config < MC_RESIDENT_AUTO || d.kernel_config > MC_RESIDENT_S128_W16)
+        return fail(1, "mcSpmm: invalid kernel_config");
     if (d.m_vec == 0) return 0;
     if (!d.row_indices || !d.row_offsets || !d.column_indices || !d.values || !d.rhs || !d.out)
         return fail(1, "mcSpmm: null pointer");

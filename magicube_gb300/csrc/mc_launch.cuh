@@ -9,6 +9,7 @@
 #include "mc_sddmm_stream.cuh"
 #include "mc_spmm.cuh"
 #include "mc_spmm_stream.cuh"
+#include "mc_spmm_resident.cuh"
 #include "mc_spmm_tma.cuh"
 #include "mc_tma_host.h"
 
@@ -111,6 +112,119 @@ int spmm_launch_tma(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     else return spmm_launch_tma_cfg<V, PA, 8, S, H, 128, 6, 2, DP4A>(d, p, s);
 }
 
+// The resident-slice SpMM (mc_spmm_resident.cuh) applies on the int8 path to
+// 8-bit B with n % 64 == 0 and 4-bit B with n % 128 == 0 (64-byte slice
+// rows), 4-, 8- or 16-bit A (dp4a: V <= 4 with 4- or 8-bit A), k <= 3584 (a
+// slice of at most 14 boxes of 256 rows in shared memory), 16-byte aligned
+// values (and values_stride), column indices and rhs, and batch entries of B
+// a whole number of rows apart.
+constexpr int kResidentMaxBoxes = 14;
+
+inline bool spmm_resident_eligible(const mcSpmmDesc& d)
+{
+    const int kind = resolve_mma_kind(d.mma_kind);
+    if (kind != MC_MMA_INT8 && kind != MC_MMA_DP4A) return false;
+    if (!(d.lhs_bits == 4 || d.lhs_bits == 8 || d.lhs_bits == 16)) return false;
+    if (reinterpret_cast<uintptr_t>(d.column_indices) % 16) return false;
+    if (!((d.rhs_bits == 8 && d.n % 64 == 0) || (d.rhs_bits == 4 && d.n % 128 == 0))) return false;
+    if (d.k < 1 || (d.k + 255) / 256 > kResidentMaxBoxes) return false;
+    if (reinterpret_cast<uintptr_t>(d.values) % 16 || d.values_stride % 16) return false;
+    if (reinterpret_cast<uintptr_t>(d.rhs) % 16) return false;
+    const long long row_bytes = (long long)d.n * d.rhs_bits / 8;
+    if (d.batch > 1 && d.rhs_stride % row_bytes) return false;
+    const long long per_entry = d.batch > 1 ? d.rhs_stride / row_bytes : 0;
+    return per_entry * (d.batch - 1) + d.k <= 0x7fffffffLL;
+}
+
+// Configurations built per precision pair: 64-byte slices x 8 warps always;
+// 64-byte x 16 warps and 128-byte x 16 warps on the MMA path with V = 8,
+// where a 16-warp CTA's accumulators and step ring fit in its 128 registers
+// a thread (not 16-bit A x 4-bit B; 128-byte slices with 4- or 8-bit A).
+template <int V, int PA, int PB, bool DP4A>
+constexpr bool resident_config_built(int cfg)
+{
+    if (cfg == MC_RESIDENT_S64_W8) return true;
+    if (DP4A || V != 8) return false;
+    if (cfg == MC_RESIDENT_S64_W16) return !(PA == 16 && PB == 4);
+    if (cfg == MC_RESIDENT_S128_W16) return PA <= 8;
+    return false;
+}
+
+// The configuration of a launch: the requested one, or automatic (measured
+// on GB300 at V = 8, k from 1024 to 3072): 128-byte slices with 16 warps
+// where they are built and fit (k <= 1792, n a multiple of their width),
+// else 64-byte slices with 16 warps, else with 8.
+template <int V, int PA, int PB, bool DP4A>
+inline int resident_config(const mcSpmmDesc& d)
+{
+    if (d.kernel_config != MC_RESIDENT_AUTO) return d.kernel_config;
+    const int boxes = (d.k + 255) / 256;
+    const int nt128 = 128 * 8 / PB;
+    if (resident_config_built<V, PA, PB, DP4A>(MC_RESIDENT_S128_W16) && d.n % nt128 == 0 && boxes <= 7)
+        return MC_RESIDENT_S128_W16;
+    if (resident_config_built<V, PA, PB, DP4A>(MC_RESIDENT_S64_W16)) return MC_RESIDENT_S64_W16;
+    return MC_RESIDENT_S64_W8;
+}
+
+// MC_KERNEL_AUTO takes the resident-slice kernel over the TMA one where it
+// applies with V = 8, or with k <= 1024 (several CTAs an SM for V = 2 and 4);
+// measured on GB300, the TMA kernel wins at V <= 4 with larger k.
+inline bool spmm_resident_preferred(const mcSpmmDesc& d)
+{
+    return spmm_resident_eligible(d) && (d.vec_length == 8 || d.k <= 1024);
+}
+
+// One wave of resident CTAs, each at least 16 vector-rows of work, over the
+// flat (slice, vector-row) list; every warp runs 4 steps ahead (2 with the
+// dp4a consumers, whose rings carry every vector lane's words).
+template <int V, int PA, int PB, bool S, bool H, int ROWB, int WARPS, bool DP4A>
+int spmm_launch_resident_cfg(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
+{
+    constexpr int PF = DP4A ? 2 : 4;
+    using G = SpmmResidentGeom<PB, ROWB, WARPS>;
+    if (d.n % G::NT) return fail(1, "mcSpmm: n is not a multiple of the slice width of this configuration");
+    const int boxes = (d.k + G::BOX_ROWS - 1) / G::BOX_ROWS;
+    if (G::smem(boxes) > 232448) return fail(1, "mcSpmm: k too large for the slices of this configuration");
+    const int tiles = d.n / G::NT;
+    const long long units = (long long)d.batch * tiles * d.m_vec;
+    if ((long long)d.batch * tiles > 0x7fffffffLL) return fail(1, "mcSpmm: batch * column tiles too large");
+    const long long row_bytes = (long long)d.n * PB / 8;
+    const long long per_entry = d.batch > 1 ? d.rhs_stride / row_bytes : 0;
+    CUtensorMap map;
+    if (!encode_slice_u8(&map, d.rhs, per_entry * (d.batch - 1) + d.k, row_bytes, ROWB, G::BOX_ROWS))
+        return fail(1, "mcSpmm: TMA tensor map encoding failed");
+    unsigned int* timeouts = async_timeout_counter();
+    if (!timeouts) return fail(1, "mcSpmm: timeout counter unavailable");
+    auto kern = spmm_resident_kernel<V, PA, PB, S, H, H, ROWB, WARPS, PF, DP4A>;
+    const size_t smem = G::smem(boxes);
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return (int)cudaGetLastError();
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, G::THREADS, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    long long grid = (long long)per_sm * sm_count();
+    const long long by_work = (units + 15) / 16;
+    if (grid > by_work) grid = by_work;
+    if (grid < 1) grid = 1;
+    kern<<<(unsigned)grid, G::THREADS, smem, s>>>(map, p, tiles, units, (int)per_entry, boxes, timeouts);
+    return (int)cudaGetLastError();
+}
+
+template <int V, int PA, int PB, bool S, bool H, bool DP4A = false>
+int spmm_launch_resident(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
+{
+    const int cfg = resident_config<V, PA, PB, DP4A>(d);
+    if (!resident_config_built<V, PA, PB, DP4A>(cfg))
+        return fail(1, "mcSpmm: this resident-slice configuration is not built for the precision pair / path");
+    if constexpr (resident_config_built<V, PA, PB, DP4A>(MC_RESIDENT_S64_W16)) {
+        if (cfg == MC_RESIDENT_S64_W16) return spmm_launch_resident_cfg<V, PA, PB, S, H, 64, 16, DP4A>(d, p, s);
+    }
+    if constexpr (resident_config_built<V, PA, PB, DP4A>(MC_RESIDENT_S128_W16)) {
+        if (cfg == MC_RESIDENT_S128_W16) return spmm_launch_resident_cfg<V, PA, PB, S, H, 128, 16, DP4A>(d, p, s);
+    }
+    return spmm_launch_resident_cfg<V, PA, PB, S, H, 64, 8, DP4A>(d, p, s);
+}
+
 // n == 64, 8-bit x 8-bit, softmax value layout, half output (the attention's
 // P x V): persistent CTAs, k split over four warps (mc_spmm_n64.cuh).
 template <int V, bool S>
@@ -138,7 +252,8 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
     if constexpr (PB == 16) {
         // 16-bit B: the per-row kernel on the int8 path (the f16 path gives the
         // same integers; it is not built for four byte-plane products).
-        if (d.kernel_variant == MC_KERNEL_STREAM || d.kernel_variant == MC_KERNEL_TMA)
+        if (d.kernel_variant == MC_KERNEL_STREAM || d.kernel_variant == MC_KERNEL_TMA ||
+            d.kernel_variant == MC_KERNEL_RESIDENT)
             return fail(1, "mcSpmm: 16-bit B runs on the per-row kernel");
         if (d.n % 128 == 0) {
             dim3 grid((unsigned)d.m_vec, (unsigned)(d.n / 128), (unsigned)d.batch);
@@ -159,6 +274,14 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
             // CUDA-core dp4a consumers in the TMA kernel: V = 2 and 4 compute
             // no padding lanes (an int8 MMA always computes 8)
             if constexpr (V <= 4 && PA <= 8) {
+                if (d.kernel_variant == MC_KERNEL_RESIDENT ||
+                    (d.kernel_variant == MC_KERNEL_AUTO && spmm_resident_preferred(d))) {
+                    if (!spmm_resident_eligible(d))
+                        return fail(1, "mcSpmm: the resident-slice kernel needs n % 64 == 0 (8-bit B) or "
+                                       "n % 128 == 0 (4-bit B), k <= 3584, 16-byte aligned values, values_stride, "
+                                       "column indices and rhs, and rhs_stride a multiple of the B row bytes");
+                    return spmm_launch_resident<V, PA, PB, S, H, true>(d, p, s);
+                }
                 if (!spmm_tma_eligible(d))
                     return fail(1, "mcSpmm: the dp4a SpMM runs on the TMA kernel: n % 128 == 0 (8-bit B) or "
                                    "n % 256 == 0 (4-bit B), 16-byte aligned values, values_stride and rhs, and "
@@ -167,6 +290,18 @@ int spmm_launch_v(const mcSpmmDesc& d, const SpmmParams& p, cudaStream_t s)
                                       : spmm_launch_tma<V, PA, PB, S, H, 128, true>(d, p, s);
             } else {
                 return fail(1, "mcSpmm: the dp4a SpMM computes V = 2 and 4 with 8-bit or 4-bit values");
+            }
+        }
+        if (d.kernel_variant == MC_KERNEL_RESIDENT ||
+            (d.kernel_variant == MC_KERNEL_AUTO && spmm_resident_preferred(d))) {
+            if constexpr (PA == 4 || PA == 8 || PA == 16) {
+                if (!spmm_resident_eligible(d))
+                    return fail(1, "mcSpmm: the resident-slice kernel needs the int8 path, n % 64 == 0 (8-bit B) "
+                                   "or n % 128 == 0 (4-bit B), k <= 3584, 16-byte aligned values, values_stride, "
+                                   "column indices and rhs, and rhs_stride a multiple of the B row bytes");
+                return spmm_launch_resident<V, PA, PB, S, H>(d, p, s);
+            } else {
+                return fail(1, "mcSpmm: the resident-slice kernel computes 4-, 8- and 16-bit A");
             }
         }
         const bool stream_ok = (reinterpret_cast<uintptr_t>(d.values) % 16 == 0) && (d.values_stride % 16 == 0);

@@ -12,6 +12,12 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();
 // boxes of box_bytes x 1 (the tile::gather4 shape), 128-byte swizzle.
 bool encode_row_gather_u8(CUtensorMap* map, const void* base, long long rows, long long row_bytes, int box_bytes);
 
+// 2-D uint8 tensor of `rows` rows of `row_bytes` bytes (pitch = row_bytes),
+// boxes of box_bytes (64 or 128) x box_rows, swizzled at the box width (the
+// resident SpMM's slices).
+bool encode_slice_u8(CUtensorMap* map, const void* base, long long rows, long long row_bytes, int box_bytes,
+                     int box_rows);
+
 // Device address of the counter of bounded waits that ran out, and its value.
 unsigned int* async_timeout_counter();
 unsigned int async_timeouts();

@@ -366,7 +366,9 @@ typedef struct mcAttnBatchDesc {
     int vec_length, heads, head_dim; /* V = 2, 4, 8; head_dim 64 */
     int lhs_bits, rhs_bits;         /* probabilities, Q/K/V: (8, 8), (16, 8) or (8, 4) */
     int requant;                    /* MC_REQUANT_FIXED or MC_REQUANT_ROWMAX (8-bit probabilities) */
-    float scale_qkv, scale_sfmx;    /* quantization scale of Q/K/V; fixed requantization scale */
+    float scale_qkv, scale_sfmx;    /* quantization scale of Q/K/V; fixed requantization scale.  Scores
+                                       are dequantized by scale_qkv * scale_qkv rounded once to float
+                                       (the square of the float scale) */
 } mcAttnBatchDesc;
 int mcAttnBatchCreate(const mcAttnBatchDesc* desc, mcAttnBatch** batch);
 /* token_offsets: host array of n_instances + 1 entries. */

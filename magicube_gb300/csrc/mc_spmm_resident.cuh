@@ -46,14 +46,22 @@ struct SpmmResidentGeom {
     static constexpr size_t smem(int boxes) { return 1024 + (size_t)boxes * BOX_ROWS * ROW_BYTES + 64; }
 };
 
-// Byte offset of 16-byte chunk c of slice row r under the TMA swizzle of
+// Byte offset of 16-byte chunk 0 of slice row r under the TMA swizzle of
 // the row width: 64-byte rows, chunk bits 4-5 XOR address bits 7-8;
-// 128-byte rows, chunk bits 4-6 XOR address bits 7-9.
+// 128-byte rows, chunk bits 4-6 XOR address bits 7-9.  Chunk c of the row
+// is then at offset ^ (c << 4): the row's own bits 4-6 are the swizzle term.
 template <int ROWB>
-__device__ __forceinline__ uint32_t resident_offset(int r, int c)
+__device__ __forceinline__ uint32_t resident_row_offset(int r)
 {
-    if constexpr (ROWB == 64) return (uint32_t)r * 64u + ((uint32_t)(c ^ ((r >> 1) & 3)) << 4);
-    else return (uint32_t)r * 128u + ((uint32_t)(c ^ (r & 7)) << 4);
+    if constexpr (ROWB == 64) return (uint32_t)r * 64u + ((uint32_t)((r >> 1) & 3) << 4);
+    else return (uint32_t)r * 128u + ((uint32_t)(r & 7) << 4);
+}
+
+__device__ __forceinline__ void ldsm_x2_trans_b8_at(uint32_t (&r)[4], uint32_t saddr)
+{
+    asm volatile("ldmatrix.sync.aligned.m16n16.x2.trans.shared.b8 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(saddr));
 }
 
 template <int V, int PREA, int PREB, bool SIGNED, bool HALF_OUT, bool EXT, int ROWB = 64, int WARPS = 8,
@@ -79,6 +87,7 @@ spmm_resident_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams 
     const uint32_t slice_bytes = (uint32_t)boxes * G::BOX_ROWS * G::ROW_BYTES;
     uint64_t* bar = reinterpret_cast<uint64_t*>(slice + slice_bytes);
     int* counter = reinterpret_cast<int*>(bar + 1);
+    const uint32_t slice_s = saddr(slice);
 
     const int tid = threadIdx.x, lane = tid & 31;
     const int g = lane >> 2, t = lane & 3;
@@ -266,12 +275,14 @@ spmm_resident_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams 
                 int srow;
                 uint32_t vals[NV][2];
                 operands(cs, srow, vals);
+                // the slice is 1024-byte aligned: chunk c of the lane's row at rowa ^ (c << 4)
+                const uint32_t rowa = slice_s + resident_row_offset<ROWB>(srow);
                 // A fragments of the 16-column tiles from the lanes' slice rows
                 if constexpr (PREB == 8) {
 #pragma unroll
                     for (int m = 0; m < MT; ++m) {
                         uint32_t af[4];
-                        ldsm_x2_trans_b8(af, slice + resident_offset<ROWB>(srow, m));
+                        ldsm_x2_trans_b8_at(af, rowa ^ ((uint32_t)m << 4));
                         if constexpr (DP4A) {
 #pragma unroll
                             for (int v = 0; v < DV; ++v) {
@@ -296,7 +307,7 @@ spmm_resident_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmParams 
 #pragma unroll
                     for (int k = 0; k < MT / 2; ++k) {
                         uint32_t nb[4], af2[2][4];
-                        ldsm_x2_trans_b8(nb, slice + resident_offset<ROWB>(srow, k));
+                        ldsm_x2_trans_b8_at(nb, rowa ^ ((uint32_t)k << 4));
 #pragma unroll
                         for (int q = 0; q < 4; ++q) {
                             const uint32_t l = nb[q] & 0x0F0F0F0Fu, hg = (nb[q] >> 4) & 0x0F0F0F0Fu;

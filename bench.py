@@ -452,7 +452,7 @@ def run_gpu(args) -> None:
             del r
             torch.cuda.empty_cache()
         for mma, var, tag in ((1, 0, MMA_NAMES[1]), (1, 3, "tma_gather_kernel"), (2, 0, MMA_NAMES[2]),
-                              (sync_mma, 1, "per_row_kernel")):
+                              (sync_mma, 1, "per_row_kernel"), (0, 4, "dense_tile")):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
                 args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
         # small vectors: an int8 MMA computes 8 vector lanes of which V are
@@ -463,6 +463,16 @@ def run_gpu(args) -> None:
                     variants[f"spmm_L{pa}R{pb}_4096x4096x256_V{v}_s0.9_{MMA_NAMES[mma]}"] = spmm_point(
                         args, dev, stream, peaks, 4096, 4096, 256, v, pa, pb, mma)
                     torch.cuda.empty_cache()
+            # the dense-tile kernel (tcgen05 f16, every product of 256-row tiles):
+            # its speed does not depend on V
+            variants[f"spmm_L8R8_4096x4096x256_V{v}_s0.9_dense_tile"] = spmm_point(
+                args, dev, stream, peaks, 4096, 4096, 256, v, 8, 8, 0, variant=4)
+            torch.cuda.empty_cache()
+        for sp in (0.5, 0.7):
+            for var, tag in ((0, "default"), (4, "dense_tile")):
+                variants[f"spmm_L8R8_2048x2048x256_V8_s{sp}_{tag}"] = spmm_point(
+                    args, dev, stream, peaks, 2048, 2048, 256, 8, 8, 8, 0, sparsity=sp, variant=var)
+                torch.cuda.empty_cache()
     attention = serving_res = packer = projection = competitors = None
     if not args.headline_only and rank == 0:
         torch.cuda.empty_cache()
@@ -558,7 +568,7 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
 
 
 def spmm_point(args, dev, stream, peaks, M: int, K: int, N: int, V: int, pa: int, pb: int, mma: int,
-               sparsity: float = SPARSITY, seed: int = 17) -> dict:
+               sparsity: float = SPARSITY, seed: int = 17, variant: int = 0) -> dict:
     """One SpMM point of the precision/shape sweep (row lengths normal, cv
     0.3): enough instances per launch that a step moves more than 2.5x L2,
     median of `--steps` CUDA-event timings; the last instance is checked
@@ -579,7 +589,7 @@ def spmm_point(args, dev, stream, peaks, M: int, K: int, N: int, V: int, pa: int
     rhs = torch.from_numpy(rhs_h).to(dev)
     out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
     fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size,  # noqa: E731
-                          mma_kind=mma)
+                          mma_kind=mma, variant=variant)
     t = statistics.median(time_cuda(fn, args.steps, args.warmup, stream)) / 1e3
     opc = 2.0 * mask.nnz_vec * V * N * B
     byts = B * (mask.nnz_vec * V * pa / 8 + K * N * pb / 8 + M * N * 4) + 4 * mask.nnz_vec + 4 * (mask.m_vec + 1)
@@ -1033,7 +1043,7 @@ SWEEP_SIZES = (512, 1024, 2048, 4096)
 SWEEP_SPARSITY = (0.5, 0.7, 0.8, 0.9, 0.95, 0.98)
 SWEEP_PAIRS = ((16, 8), (8, 8), (8, 4), (4, 4), (16, 4))
 SWEEP_COLUMNS = ("M", "K", "N", "sparsity", "V", "pair", "batch", "nnz_vec", "us_per_instance", "tops", "gbs",
-                 "hbm_frac", "tensor_util", "roofline_frac", "bound")
+                 "hbm_frac", "tensor_util", "roofline_frac", "bound", "dense_tile_tops")
 
 
 def run_sweep(args) -> None:
@@ -1055,7 +1065,7 @@ def run_sweep(args) -> None:
     of a 16-bit A (4-bit operands run unpacked on the int8 MMA)."""
     import torch
 
-    from magicube_gb300 import formats, ops, synth
+    from magicube_gb300 import _lib, formats, ops, synth
     dev = torch.device("cuda:0")
     stream = torch.cuda.current_stream()
     peaks = _peaks()
@@ -1094,6 +1104,13 @@ def run_sweep(args) -> None:
                             fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=vstride)
                             t = statistics.median(time_cuda(fn, steps, warmup, stream)) / 1e3
                             opc = 2.0 * mask.nnz_vec * V * N * B
+                            dense_tops = None
+                            if (pa, pb) == (8, 8):
+                                # the dense-tile kernel on the same operands (its own column)
+                                fd = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B,  # noqa: E731
+                                                      values_stride=vstride, variant=_lib.KERNEL_DENSE_TILE)
+                                dense_tops = round(opc / (statistics.median(time_cuda(fd, steps, warmup, stream))
+                                                          / 1e3) / 1e12, 3)
                             mma_ops = opc * (2 if pa == 16 else 1)
                             byts = B * (mask.nnz_vec * V * pa / 8 + K * N * pb / 8 + M * N * 4) + idx_bytes
                             t_hbm, t_tc = byts / (peaks["hbm_gbs"] * 1e9), mma_ops / (int8_peak * 1e12)
@@ -1101,7 +1118,8 @@ def run_sweep(args) -> None:
                                          round(opc / t / 1e12, 3), round(byts / t / 1e9, 1),
                                          round(byts / t / 1e9 / peaks["hbm_gbs"], 4),
                                          round(mma_ops / t / 1e12 / int8_peak, 4),
-                                         round(max(t_hbm, t_tc) / t, 4), "hbm" if t_hbm >= t_tc else "tensor"])
+                                         round(max(t_hbm, t_tc) / t, 4), "hbm" if t_hbm >= t_tc else "tensor",
+                                         dense_tops])
                             del vals, rhs, out, d
             print(f"sweep: M={M} K={K} done, {len(rows)} points, {time.time() - t_start:.0f} s",
                   file=sys.stderr, flush=True)
@@ -1119,6 +1137,10 @@ def run_sweep(args) -> None:
             "max_gbs": max(r[col["gbs"]] for r in sel),
             "max_tops": max(r[col["tops"]] for r in sel),
             "median_roofline_frac": statistics.median(r[col["roofline_frac"]] for r in sel),
+            **({"dense_tile_faster_points": sum(r[col["dense_tile_tops"]] > r[col["tops"]] for r in sel),
+                "median_best_tops_ratio": statistics.median(max(r[col["dense_tile_tops"]], r[col["tops"]])
+                                                            / r[col["tops"]] for r in sel)}
+               if name == "L8-R8" else {}),
             "sparsity_ge_0.9": {
                 "points": len(hi),
                 "median_hbm_frac": statistics.median(r[col["hbm_frac"]] for r in hi) if hi else None,

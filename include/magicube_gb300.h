@@ -124,7 +124,7 @@ int mcSetDefaultMmaKind(int kind);
  *                    with n % 256 == 0, 16-byte aligned values,
  *                    values_stride and rhs, rhs_stride a multiple of the B
  *                    row bytes).
- * MC_KERNEL_DENSE_TILE: SDDMM only, 8-bit operands with k == 64: every score
+ * MC_KERNEL_DENSE_TILE: SDDMM, 8-bit operands with k == 64: every score
  *                    of 128-column x 256-row tiles on the tcgen05 f16 tensor
  *                    cores (exact: 64 products of int8 values sum below 2^24),
  *                    accumulators in TMEM, and an epilogue that stores the
@@ -134,6 +134,16 @@ int mcSetDefaultMmaKind(int kind);
  *                    not read).  Wins where the mask is dense enough that a
  *                    dense tile costs less than per-nonzero gathers (about
  *                    sparsity <= 0.95 on GB300).
+ *                    SpMM, L8-R8 with int32 output and n % 128 == 0: each
+ *                    256-row block of A is expanded into dense f16 tiles in
+ *                    shared memory, 64 columns of k at a time, and multiplied
+ *                    whole with B on the tcgen05 f16 tensor cores (exact:
+ *                    k is accumulated in segments of at most 1024 columns,
+ *                    256 with unsigned lanes, whose f32 sums stay within 2^24,
+ *                    and the segments are added in int32).  Needs the chunk
+ *                    table of mcSpmmChunkStarts (strictly increasing columns
+ *                    per vector-row) in chunk_starts; row_indices is not read.
+ *                    Its time does not depend on V or on the sparsity.
  * MC_KERNEL_RESIDENT: SpMM only, on the int8 path: each CTA holds a K x 64-byte
  *                    column slice of B in shared memory (loaded once by TMA)
  *                    and its warps gather the rows of their vector-rows'
@@ -196,6 +206,9 @@ typedef struct mcSpmmDesc {
     /* MC_KERNEL_RESIDENT only: slice width and CTA size (MC_RESIDENT_*);
      * 0 = automatic.  Other variants ignore it. */
     int kernel_config;
+    /* MC_KERNEL_DENSE_TILE only: the mask's chunk table (mcSpmmChunkStarts),
+     * m_vec x mcSpmmChunkStartsCount(k) ints.  Other variants ignore it. */
+    const int* chunk_starts;
 } mcSpmmDesc;
 /* Configurations of MC_KERNEL_RESIDENT: 64-byte slice rows (64 columns of
  * 8-bit B, 128 of 4-bit B) with 8 or 16 warps a CTA, 128-byte slice rows
@@ -204,6 +217,18 @@ typedef struct mcSpmmDesc {
  * 4-bit B; 128-byte slices with 4- or 8-bit A. */
 enum { MC_RESIDENT_AUTO = 0, MC_RESIDENT_S64_W8 = 1, MC_RESIDENT_S64_W16 = 2, MC_RESIDENT_S128_W16 = 3 };
 int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream);
+
+/* Chunk table of an SpMM mask for MC_KERNEL_DENSE_TILE: starts[R][c] is the
+ * first slot of vector-row R (an index into column_indices) whose column is
+ * >= 64 c, for c = 0 .. ceil(k / 64), so the slots of k chunk c are
+ * [starts[R][c], starts[R][c+1]).  Built on the device on `stream`; *status
+ * (device int) is set to 0, or to 1 if a vector-row's columns are not
+ * strictly increasing or lie outside [0, k) (that row's chunks are then left
+ * empty).  No reference counterpart: the reference's kernels walk the slots
+ * in order and need no table. */
+int mcSpmmChunkStartsCount(int k);  /* entries per vector-row: ceil(k / 64) + 1 */
+int mcSpmmChunkStarts(int m_vec, int k, const int* row_offsets, const int* column_indices, int* starts,
+                      int* status, cudaStream_t stream);
 
 typedef struct mcSddmmDesc {
     int m_vec, vec_length, n, k;

@@ -26,7 +26,7 @@ class McSpmmDesc(ctypes.Structure):
         ("out", _c_vp), ("out_stride", _c_ll),
         ("mma_kind", _c_int), ("kernel_variant", _c_int), ("value_layout", _c_int),
         ("row_div", _c_vp), ("row_div_stride", _c_ll),
-        ("kernel_config", _c_int),
+        ("kernel_config", _c_int), ("chunk_starts", _c_vp),
     ]
 
 
@@ -110,6 +110,8 @@ _SIGNATURES = {
     "mcSddmm": (_c_int, [ctypes.POINTER(McSddmmDesc), _c_vp]),
     "mcSddmmTileMaskWords": (_c_int, [_c_int]),
     "mcSddmmTileMask": (_c_int, [_c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "mcSpmmChunkStartsCount": (_c_int, [_c_int]),
+    "mcSpmmChunkStarts": (_c_int, [_c_int, _c_int, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
     "mcQuantize": (_c_int, [_c_vp, _c_vp, _c_ll, _c_int, _c_float, _c_vp]),
     "mcQuantSoftmax": (_c_int, [ctypes.POINTER(McSoftmaxDesc), _c_vp]),
     "mcSparseAttention": (_c_int, [ctypes.POINTER(McAttnDesc), _c_vp]),

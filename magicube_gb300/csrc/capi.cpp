@@ -55,9 +55,22 @@ static int check_spmm(const mcSpmmDesc& d)
         return fail(1, "mcSpmm: invalid mma_kind (the SpMM runs on MC_MMA_INT8, MC_MMA_F16 or MC_MMA_DP4A)");
     if (d.mma_kind == MC_MMA_DP4A && (d.lhs_bits > 8 || d.rhs_bits > 8 || d.vec_length > 4))
         return fail(1, "mcSpmm: the dp4a SpMM computes V = 2 and 4 with 8-bit or 4-bit operands");
-    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_RESIDENT ||
-        d.kernel_variant == MC_KERNEL_DENSE_TILE)
+    if (d.kernel_variant < MC_KERNEL_AUTO || d.kernel_variant > MC_KERNEL_RESIDENT)
         return fail(1, "mcSpmm: invalid kernel_variant");
+    if (d.kernel_variant == MC_KERNEL_DENSE_TILE) {
+        if (d.lhs_bits != 8 || d.rhs_bits != 8 || d.out_half)
+            return fail(1, "mcSpmm: the dense-tile kernel computes L8-R8 with int32 output");
+        if (d.n % 128) return fail(1, "mcSpmm: the dense-tile kernel needs n % 128 == 0");
+        if (d.mma_kind != MC_MMA_DEFAULT)
+            return fail(1, "mcSpmm: the dense-tile kernel runs on the tcgen05 f16 path (mma_kind must be "
+                           "MC_MMA_DEFAULT)");
+        if (d.m_vec > 0 && (!d.chunk_starts || !aligned(d.chunk_starts, 4)))
+            return fail(1, "mcSpmm: the dense-tile kernel needs the mask's chunk table (mcSpmmChunkStarts)");
+        if (d.batch > 1 && d.rhs_stride % d.n)
+            return fail(1, "mcSpmm: the dense-tile kernel needs rhs_stride a multiple of the B row bytes");
+        if (!aligned(d.column_indices, 16))
+            return fail(1, "mcSpmm: the dense-tile kernel needs 16-byte aligned column indices");
+    }
     if (d.kernel_config < MC_RESIDENT_AUTO || d.kernel_config > MC_RESIDENT_S128_W16)
         return fail(1, "mcSpmm: invalid kernel_config");
     if (d.m_vec == 0) return 0;
@@ -133,6 +146,7 @@ int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream)
     const mcSpmmDesc& d = *desc;
     if (int rc = mc::check_spmm(d)) return rc;
     if (d.m_vec == 0) return 0;
+    if (d.kernel_variant == MC_KERNEL_DENSE_TILE) return mc::spmm_dense_launch(d, stream);
     if (d.lhs_bits == 12) {
         // 12-bit values use the 16-bit layouts with the top 4 bits clear
         // (spmm_benchmark.cpp:288-358): the 16-bit kernels compute them.

@@ -41,5 +41,6 @@ int sddmm_launch_8_8(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_launch_16_8(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_launch_16_16(const mcSddmmDesc& d, cudaStream_t s);
 int sddmm_dense_launch(const mcSddmmDesc& d, cudaStream_t s);
+int spmm_dense_launch(const mcSpmmDesc& d, cudaStream_t s);
 
 }  // namespace mc

@@ -58,6 +58,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long l
     return true;
 }
 
+// As mbar_wait, sleeping `ns` nanoseconds between polls: for roles that wait
+// long (an epilogue for its accumulator, producers running ahead), so their
+// polling does not take issue slots from the warps that do the work.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, long long limit_cycles, unsigned ns)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > limit_cycles) return false;
+        __nanosleep(ns);
+    }
+    return true;
+}
+
 // ---- TMA --------------------------------------------------------------------
 
 // 2-D tiled load of the box at (x, y) (x innermost, in elements) into shared
@@ -90,6 +104,14 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      saddr(dst)),
                  "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+
+// Prefetch of `bytes` contiguous bytes (a multiple of 16, 16-byte aligned)
+// from global memory into L2.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<uint64_t>(src)), "r"(bytes)
                  : "memory");
 }
 

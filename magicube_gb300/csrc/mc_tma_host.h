@@ -18,6 +18,12 @@ bool encode_row_gather_u8(CUtensorMap* map, const void* base, long long rows, lo
 bool encode_slice_u8(CUtensorMap* map, const void* base, long long rows, long long row_bytes, int box_bytes,
                      int box_rows);
 
+// 2-D uint8 tensor of `rows` rows of `row_bytes` bytes (pitch = row_bytes),
+// unswizzled boxes of box_bytes x box_rows (the dense-tile SpMM's B chunks);
+// rows past the end read as zero.
+bool encode_box_u8(CUtensorMap* map, const void* base, long long rows, long long row_bytes, int box_bytes,
+                   int box_rows);
+
 // Device address of the counter of bounded waits that ran out, and its value.
 unsigned int* async_timeout_counter();
 unsigned int async_timeouts();

@@ -57,6 +57,22 @@ bool encode_slice_u8(CUtensorMap* map, const void* base, long long rows, long lo
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+bool encode_box_u8(CUtensorMap* map, const void* base, long long rows, long long row_bytes, int box_bytes,
+                   int box_rows)
+{
+    auto fn = tensor_map_encoder();
+    if (!fn || rows <= 0 || row_bytes < box_bytes || row_bytes % 16 || box_bytes % 16 || box_bytes > 256 ||
+        box_rows < 1 || box_rows > 256)
+        return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)row_bytes, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)row_bytes};
+    const cuuint32_t box[2] = {(cuuint32_t)box_bytes, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // Device address of g_async_timeouts on the current device, looked up once
 // per device under a lock (the library assumes the primary context of a
 // device is never reset while it is loaded).

@@ -38,6 +38,8 @@ class DeviceSpmmLhs:
     col_indices: torch.Tensor
     values: torch.Tensor
 
+    _chunks: torch.Tensor | None = None
+
     @classmethod
     def from_host(cls, h: SpmmLhs, device="cuda") -> "DeviceSpmmLhs":
         cols = h.col_indices if h.col_indices.size else np.full(1, -1, np.int32)
@@ -45,6 +47,25 @@ class DeviceSpmmLhs:
         return cls(h.mask.m_vec, h.mask.vec_length, h.mask.ncols, h.lhs_bits, h.rhs_bits,
                    _to_dev(h.row_indices, device), _to_dev(h.row_offsets, device),
                    _to_dev(cols, device), _to_dev(vals, device))
+
+    def chunk_starts(self, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+        """The mask's k-chunk table for the dense-tile SpMM kernel, built on
+        the device once (mcSpmmChunkStarts) and cached.  Synchronises once to
+        read the status; raises MagicubeError if a vector-row's columns are
+        not strictly increasing inside [0, k)."""
+        if self._chunks is None:
+            dev = self.row_offsets.device
+            per = _lib.lib().mcSpmmChunkStartsCount(self.k)
+            starts = torch.empty((max(1, self.m_vec), per), dtype=torch.int32, device=dev)
+            status = torch.empty(1, dtype=torch.int32, device=dev)
+            _lib.check(_lib.lib().mcSpmmChunkStarts(self.m_vec, self.k, self.row_offsets.data_ptr(),
+                                                    self.col_indices.data_ptr(), starts.data_ptr(),
+                                                    status.data_ptr(), _stream_handle(stream)), "mcSpmmChunkStarts")
+            if int(status.item()) != 0:
+                raise _lib.MagicubeError("mcSpmmChunkStarts: the mask's columns are not strictly increasing "
+                                         "inside [0, k) per vector-row; the dense-tile SpMM cannot use it")
+            self._chunks = starts
+        return self._chunks
 
 
 @dataclass
@@ -114,6 +135,8 @@ def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, 
         rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride, mma_kind=mma_kind,
         kernel_variant=variant, value_layout=_lib.VALUES_SOFTMAX if out_half else _lib.VALUES_PACKED,
         kernel_config=config)
+    if variant == _lib.KERNEL_DENSE_TILE:
+        d.chunk_starts = lhs.chunk_starts(stream).data_ptr()
     _lib.check(_lib.lib().mcSpmm(ctypes.byref(d), _stream_handle(stream)), "mcSpmm")
     return out
 

@@ -97,6 +97,36 @@ def test_sddmm_new_path_errors(fields, msg):
     assert msg in _lib.lib().mcGetLastErrorString()
 
 
+@pytest.mark.parametrize("fields,msg", [
+    (dict(lhs_bits=16), b"L8-R8 with int32 output"),
+    (dict(n=192), b"n % 128 == 0"),
+    (dict(mma_kind=_lib.MMA_INT8), b"tcgen05 f16 path"),
+    (dict(), b"chunk table"),
+    (dict(batch=2, rhs_stride=64 * 128 + 16), b"rhs_stride"),
+])
+def test_spmm_dense_tile_errors(fields, msg):
+    """The dense-tile SpMM rejects what it cannot compute, before any device
+    work: other pairs, n not a multiple of 128, another tensor path, a
+    missing chunk table, a B stride that is not whole rows."""
+    d = _lib.McSpmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1, scale=1.0,
+                        kernel_variant=_lib.KERNEL_DENSE_TILE)
+    if "chunk" not in msg.decode():
+        d.chunk_starts = 16
+    for k, v in fields.items():
+        setattr(d, k, v)
+    assert _lib.lib().mcSpmm(ctypes.byref(d), None) == 1
+    assert msg in _lib.lib().mcGetLastErrorString()
+
+
+def test_chunk_starts_count_and_argument_errors():
+    lib = _lib.lib()
+    assert [lib.mcSpmmChunkStartsCount(k) for k in (0, 1, 64, 65, 1024)] == [0, 2, 2, 3, 17]
+    assert lib.mcSpmmChunkStarts(4, 0, None, None, None, None, None) == 1
+    assert b"k > 0" in lib.mcGetLastErrorString()
+    assert lib.mcSpmmChunkStarts(4, 64, None, None, None, None, None) == 1
+    assert b"null status" in lib.mcGetLastErrorString()
+
+
 def test_tile_mask_words_and_argument_errors():
     lib = _lib.lib()
     assert [lib.mcSddmmTileMaskWords(n) for n in (0, 1, 128, 129, 4096)] == [0, 4, 4, 8, 128]

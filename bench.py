@@ -1043,7 +1043,7 @@ SWEEP_SIZES = (512, 1024, 2048, 4096)
 SWEEP_SPARSITY = (0.5, 0.7, 0.8, 0.9, 0.95, 0.98)
 SWEEP_PAIRS = ((16, 8), (8, 8), (8, 4), (4, 4), (16, 4))
 SWEEP_COLUMNS = ("M", "K", "N", "sparsity", "V", "pair", "batch", "nnz_vec", "us_per_instance", "tops", "gbs",
-                 "hbm_frac", "tensor_util", "roofline_frac", "bound", "dense_tile_tops")
+                 "hbm_frac", "tensor_util", "roofline_frac", "bound")
 
 
 def run_sweep(args) -> None:
@@ -1065,7 +1065,7 @@ def run_sweep(args) -> None:
     of a 16-bit A (4-bit operands run unpacked on the int8 MMA)."""
     import torch
 
-    from magicube_gb300 import _lib, formats, ops, synth
+    from magicube_gb300 import formats, ops, synth
     dev = torch.device("cuda:0")
     stream = torch.cuda.current_stream()
     peaks = _peaks()
@@ -1104,13 +1104,6 @@ def run_sweep(args) -> None:
                             fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=vstride)
                             t = statistics.median(time_cuda(fn, steps, warmup, stream)) / 1e3
                             opc = 2.0 * mask.nnz_vec * V * N * B
-                            dense_tops = None
-                            if (pa, pb) == (8, 8):
-                                # the dense-tile kernel on the same operands (its own column)
-                                fd = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B,  # noqa: E731
-                                                      values_stride=vstride, variant=_lib.KERNEL_DENSE_TILE)
-                                dense_tops = round(opc / (statistics.median(time_cuda(fd, steps, warmup, stream))
-                                                          / 1e3) / 1e12, 3)
                             mma_ops = opc * (2 if pa == 16 else 1)
                             byts = B * (mask.nnz_vec * V * pa / 8 + K * N * pb / 8 + M * N * 4) + idx_bytes
                             t_hbm, t_tc = byts / (peaks["hbm_gbs"] * 1e9), mma_ops / (int8_peak * 1e12)
@@ -1118,8 +1111,7 @@ def run_sweep(args) -> None:
                                          round(opc / t / 1e12, 3), round(byts / t / 1e9, 1),
                                          round(byts / t / 1e9 / peaks["hbm_gbs"], 4),
                                          round(mma_ops / t / 1e12 / int8_peak, 4),
-                                         round(max(t_hbm, t_tc) / t, 4), "hbm" if t_hbm >= t_tc else "tensor",
-                                         dense_tops])
+                                         round(max(t_hbm, t_tc) / t, 4), "hbm" if t_hbm >= t_tc else "tensor"])
                             del vals, rhs, out, d
             print(f"sweep: M={M} K={K} done, {len(rows)} points, {time.time() - t_start:.0f} s",
                   file=sys.stderr, flush=True)
@@ -1137,10 +1129,6 @@ def run_sweep(args) -> None:
             "max_gbs": max(r[col["gbs"]] for r in sel),
             "max_tops": max(r[col["tops"]] for r in sel),
             "median_roofline_frac": statistics.median(r[col["roofline_frac"]] for r in sel),
-            **({"dense_tile_faster_points": sum(r[col["dense_tile_tops"]] > r[col["tops"]] for r in sel),
-                "median_best_tops_ratio": statistics.median(max(r[col["dense_tile_tops"]], r[col["tops"]])
-                                                            / r[col["tops"]] for r in sel)}
-               if name == "L8-R8" else {}),
             "sparsity_ge_0.9": {
                 "points": len(hi),
                 "median_hbm_frac": statistics.median(r[col["hbm_frac"]] for r in hi) if hi else None,
@@ -1243,7 +1231,7 @@ def run_profile_case(args) -> None:
         out = torch.empty((args.batch, M, N), dtype=torch.int32, device=dev)
         for _ in range(args.reps):
             ops.spmm(d, rhs, N, signed=True, out=out, batch=args.batch, values_stride=h.values.size,
-                     mma_kind=args.mma, variant=args.spmm_kernel)
+                     mma_kind=0 if args.spmm_kernel == 4 else args.mma, variant=args.spmm_kernel)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": args.profile, "batch": args.batch, "reps": args.reps}))
 
@@ -1274,7 +1262,7 @@ def main() -> None:
                          "(all bit-exact; see include/magicube_gb300.h)")
     ap.add_argument("--sddmm-kernel", choices=["auto", "per_row", "stream", "dense"], default="auto",
                     help="SDDMM kernel variant of the --profile sddmm case")
-    ap.add_argument("--spmm-kernel", choices=["auto", "per_row", "stream", "tma", "resident"], default="auto",
+    ap.add_argument("--spmm-kernel", choices=["auto", "per_row", "stream", "tma", "resident", "dense"], default="auto",
                     help="SpMM kernel variant of the --profile spmm and spmm-v2 cases")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", choices=["square", "full"], default=None,
@@ -1285,7 +1273,7 @@ def main() -> None:
         args.warmup = 3
     args.mma = {"int8": 1, "f16": 2, "tc": 3, "dp4a": 4}[args.mma]
     args.sddmm_kernel = {"auto": 0, "per_row": 1, "stream": 2, "dense": 4}[args.sddmm_kernel]
-    args.spmm_kernel = {"auto": 0, "per_row": 1, "stream": 2, "tma": 3, "resident": 5}[args.spmm_kernel]
+    args.spmm_kernel = {"auto": 0, "per_row": 1, "stream": 2, "tma": 3, "resident": 5, "dense": 4}[args.spmm_kernel]
     if args.sweep:
         run_sweep(args)
     elif args.profile:

@@ -83,7 +83,7 @@ def test_device_sddmm_mask_equals_host(cuda, alignment):
     np.testing.assert_array_equal(dm.col_indices.cpu().numpy(), h.col_indices)
 
 
-@pytest.mark.parametrize("m_vec", [1, 1023, 1024, 1025, 2048, 4095, 4096, 4097, 9000, 20011])
+@pytest.mark.parametrize("m_vec", [1, 1023, 1024, 1025, 2048, 4095, 4096, 4097, 9000, 16383, 16384, 16385, 20011])
 def test_multi_tile_scan(cuda, m_vec):
     """Row counts on and across the 1,024-row scan tiles of the align step."""
     m = synth.normal_mask(m_vec, 512, 4, 0.95, seed=m_vec)

@@ -473,7 +473,7 @@ def run_gpu(args) -> None:
                 variants[f"spmm_L8R8_2048x2048x256_V8_s{sp}_{tag}"] = spmm_point(
                     args, dev, stream, peaks, 2048, 2048, 256, 8, 8, 8, 0, sparsity=sp, variant=var)
                 torch.cuda.empty_cache()
-    attention = serving_res = packer = projection = competitors = None
+    attention = serving_res = packer = projection = competitors = native_server = None
     if not args.headline_only and rank == 0:
         torch.cuda.empty_cache()
         packer = packer_suite(args, dev, peaks)
@@ -483,6 +483,8 @@ def run_gpu(args) -> None:
         competitors = competitor_suite(args, dev)
         torch.cuda.empty_cache()
         attention = attention_suite(args, dev)
+        torch.cuda.empty_cache()
+        native_server = native_server_suite(args, dev)
         torch.cuda.empty_cache()
         if args.serving_requests > 0:
             serving_res = serving_suite(args, dev)
@@ -523,6 +525,7 @@ def run_gpu(args) -> None:
             "clocks": head["clocks"],
             "variants": variants,
             "batched_attention": attention,
+            "attention_server": native_server,
             "serving": serving_res,
             "device_packer": packer,
             "qkv_projection": projection,
@@ -914,6 +917,54 @@ def formats_align(mask, alignment):
     pairs, n = formats.align_row_offsets(mask, alignment)
     cols = formats.pad_column_indices(mask, pairs, n, False)
     return (pairs, cols), n
+
+
+def native_server_suite(args, dev) -> dict:
+    """The C++ request loop (mcAttnServer*) on the batched-attention workload
+    as a stream of requests: 64 sequences, lengths uniform in [512, 4096],
+    band 256 + random V=8 vectors at sparsity 0.9, 4 heads of 64, row-max
+    requantization; Q/K/V and masks resident on the device.  Arrivals all at
+    once, and Poisson at 100,000 and 20,000 requests/s.  Continuous batching
+    (batches of up to 32,768 tokens, two on the device) against one request
+    at a time (one request per batch, one batch on the device); each server
+    is run once untimed on the same requests first.  The outputs of the two
+    modes are compared bit for bit."""
+    import torch
+
+    from magicube_gb300 import batched, synth
+    rng = np.random.default_rng(11)
+    n, H = 64, 4
+    lens = (rng.integers(512, 4097, size=n) // 64 * 64).clip(512, 4096).tolist()
+    masks = [synth.band_random_mask(L, VEC, 256, 0.9, seed=100 + i) for i, L in enumerate(lens)]
+    g = torch.Generator().manual_seed(12)
+    qkvs = [(torch.randn(3, H, L, 64, generator=g) * 0.5).half().to(dev) for L in lens]
+    amax = max(float(q.abs().max()) for q in qkvs)
+    sq = float(np.float32(127.0 / amax))
+    modes = {"continuous": dict(max_batch_tokens=32768, max_inflight=2),
+             "one_at_a_time": dict(max_batch_tokens=1, max_inflight=1)}
+    arr_rng = np.random.default_rng(5)
+    runs, outs_by_mode = [], {}
+    for rate in (None, 100000.0, 20000.0):
+        arrivals = np.zeros(n) if rate is None else np.cumsum(arr_rng.exponential(1.0 / rate, size=n))
+        run = {"arrival_rate": "all at once" if rate is None else rate}
+        for mode, kw in modes.items():
+            srv = batched.NativeAttentionServer(heads=H, scale_qkv=sq, scale_sfmx=127.0, requant="rowmax", **kw)
+            outs = [torch.empty((H, L, 64), dtype=torch.float16, device=dev) for L in lens]
+            made = [srv.request(m, q, o, float(a), dev) for m, q, o, a in zip(masks, qkvs, outs, arrivals)]
+            reqs = [r for r, _ in made]
+            srv.run(reqs)
+            lat, st = srv.run(reqs)
+            run[mode] = {"req_per_s": st["req_per_s"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                         "batches": st["batches"], "max_inflight_seen": st["max_inflight_seen"],
+                         "served": st["served"], "rejected": st["rejected"]}
+            outs_by_mode[mode] = outs
+            del srv, made
+        run["ratio_req_per_s"] = run["continuous"]["req_per_s"] / max(run["one_at_a_time"]["req_per_s"], 1e-9)
+        runs.append(run)
+    same = all(torch.equal(a, b) for a, b in zip(outs_by_mode["continuous"], outs_by_mode["one_at_a_time"]))
+    return {"config": f"{n} sequences x {H} heads, d=64, L ~ U[512,4096], band 256 + random V=8, sparsity 0.9, "
+                      "int8 Q/K/V, row-max requantization; C++ request loop (mcAttnServer)",
+            "runs": runs, "outputs_identical_across_modes": bool(same)}
 
 
 def serving_suite(args, dev) -> dict:

@@ -407,6 +407,64 @@ int mcAttnBatchReplay(mcAttnBatch* batch, cudaStream_t stream);
 int mcAttnBatchStatus(mcAttnBatch* batch, int* status);
 void mcAttnBatchDestroy(mcAttnBatch* batch);
 
+/* ---- Attention request server (host C++, no PyTorch) ------------------------
+ * A continuous-batching request loop for sparse attention, the serving path
+ * that the reference does not have (its end-to-end script runs one sequence
+ * at a time, end_to_end.py:47-85).  Each request is one sequence: its plain
+ * vector CSR mask and half Q/K/V stay resident in device memory, owned by the
+ * caller, and the server writes its half output.  mcAttnServerRun plays the
+ * requests at their arrival times on the host clock and, while requests are
+ * waiting and fewer than max_inflight batches are on the device, admits the
+ * waiting ones in arrival order (up to max_batch_tokens tokens, at least one
+ * request) as one batch, provided the batch's device memory fits the free
+ * memory (cudaMemGetInfo, plus what the default stream-ordered pool holds
+ * unused) less hbm_reserve_bytes and less the batches already in flight,
+ * each charged at its full footprint; a request that does not
+ * fit even with nothing in flight is rejected (latency -1) and never
+ * launched.  A batch is built on the device on its own stream with
+ * stream-ordered allocations: the requests' masks stacked block-diagonally
+ * (one kernel), packed by mcDevicePack (aligned pairs, padded columns,
+ * longest-first rows), Q/K/V staged with one 2-D copy per request, then
+ * mcQuantize and the fused mcSparseAttention, and the outputs copied back
+ * into each request's buffer.  Each request's output equals its output when
+ * served alone, bit for bit.  Latency = host-observed completion of the
+ * request's batch minus its arrival.  No reference counterpart. */
+typedef struct mcAttnServer mcAttnServer;
+typedef struct mcAttnServerDesc {
+    int vec_length, heads, head_dim;  /* V = 2, 4, 8; head_dim 64 */
+    int lhs_bits, rhs_bits;           /* (8, 8), (16, 8) or (8, 4) */
+    int requant;                      /* MC_REQUANT_FIXED or MC_REQUANT_ROWMAX */
+    float scale_qkv, scale_sfmx;
+    long long max_batch_tokens;       /* tokens per batch (a longer single request is admitted alone) */
+    int max_inflight;                 /* batches on the device at once, 1 .. 8 */
+    long long hbm_reserve_bytes;      /* free device memory admission leaves untouched */
+} mcAttnServerDesc;
+typedef struct mcAttnRequest {
+    int seq_len;                      /* tokens, a positive multiple of vec_length */
+    int nnz_vec, max_row_nnz;         /* the mask's nonzero vectors and longest vector-row (<= 4096) */
+    const int* row_offsets;           /* device: seq_len / V + 1 plain CSR offsets, starting at 0 */
+    const int* col_indices;           /* device: nnz_vec column indices in [0, seq_len), increasing per row */
+    const void* qkv;                  /* device half [3][heads][seq_len][head_dim] */
+    void* out;                        /* device half [heads][seq_len][head_dim] */
+    double arrival_s;                 /* arrival time, seconds after the run starts */
+} mcAttnRequest;
+typedef struct mcAttnServeStats {
+    double makespan_s, req_per_s, p50_ms, p99_ms, mean_ms;
+    int served, rejected, batches, max_inflight_seen, held_back;
+} mcAttnServeStats;
+int mcAttnServerCreate(const mcAttnServerDesc* desc, mcAttnServer** server);
+/* Serves `n` requests; latency_ms (host, n entries) receives each request's
+ * latency or -1 if rejected.  Returns when every request is done. */
+int mcAttnServerRun(mcAttnServer* server, const mcAttnRequest* requests, int n, double* latency_ms,
+                    mcAttnServeStats* stats);
+/* The device bytes admission charges for one batch of the n requests
+ * (batch_bytes) and the current admission budget: free device memory plus
+ * what the default stream-ordered pool holds unused, less the reserve
+ * (available_bytes).  Either output may be null. */
+int mcAttnServerMemory(const mcAttnServer* server, const mcAttnRequest* requests, int n, long long* batch_bytes,
+                       long long* available_bytes);
+void mcAttnServerDestroy(mcAttnServer* server);
+
 /* ---- Host-side format conversion (host pointers) ---------------------------
  * The reference's host packer (SpMM/SpMM/spmm_benchmark.cpp:177-377,
  * SDDMM/SDDMM/sddmm_benchmark.cpp:104-127) as library routines. */

@@ -67,6 +67,29 @@ class McAttnDesc(ctypes.Structure):
     ]
 
 
+class McAttnServerDesc(ctypes.Structure):
+    _fields_ = [
+        ("vec_length", _c_int), ("heads", _c_int), ("head_dim", _c_int), ("lhs_bits", _c_int), ("rhs_bits", _c_int),
+        ("requant", _c_int), ("scale_qkv", _c_float), ("scale_sfmx", _c_float), ("max_batch_tokens", _c_ll),
+        ("max_inflight", _c_int), ("hbm_reserve_bytes", _c_ll),
+    ]
+
+
+class McAttnRequest(ctypes.Structure):
+    _fields_ = [
+        ("seq_len", _c_int), ("nnz_vec", _c_int), ("max_row_nnz", _c_int), ("row_offsets", _c_vp),
+        ("col_indices", _c_vp), ("qkv", _c_vp), ("out", _c_vp), ("arrival_s", ctypes.c_double),
+    ]
+
+
+class McAttnServeStats(ctypes.Structure):
+    _fields_ = [
+        ("makespan_s", ctypes.c_double), ("req_per_s", ctypes.c_double), ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double), ("served", _c_int), ("rejected", _c_int),
+        ("batches", _c_int), ("max_inflight_seen", _c_int), ("held_back", _c_int),
+    ]
+
+
 class McQkvProjDesc(ctypes.Structure):
     _fields_ = [
         ("tokens", _c_int), ("hidden", _c_int), ("heads", _c_int), ("head_dim", _c_int), ("bits", _c_int),
@@ -137,6 +160,12 @@ _SIGNATURES = {
     "mcAttnBatchReplay": (_c_int, [_c_vp, _c_vp]),
     "mcAttnBatchStatus": (_c_int, [_c_vp, _IP]),
     "mcAttnBatchDestroy": (None, [_c_vp]),
+    "mcAttnServerCreate": (_c_int, [ctypes.POINTER(McAttnServerDesc), ctypes.POINTER(_c_vp)]),
+    "mcAttnServerRun": (_c_int, [_c_vp, ctypes.POINTER(McAttnRequest), _c_int, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(McAttnServeStats)]),
+    "mcAttnServerMemory": (_c_int, [_c_vp, ctypes.POINTER(McAttnRequest), _c_int, ctypes.POINTER(_c_ll),
+                                    ctypes.POINTER(_c_ll)]),
+    "mcAttnServerDestroy": (None, [_c_vp]),
 }
 # the diagnostics library (include/magicube_gb300_probe.h)
 _PROBE_SIGNATURES = {

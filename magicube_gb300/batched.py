@@ -389,3 +389,65 @@ class NativeBatchedSparseAttention:
         if h is not None and h.value:
             _lib.lib().mcAttnBatchDestroy(h)
             self._h = ctypes.c_void_p()
+
+
+class NativeAttentionServer:
+    """Continuous batching of sparse-attention requests in the library's C++
+    request loop (mcAttnServer*): every request keeps its plain vector CSR
+    mask and half Q/K/V on the device; the loop admits waiting requests as
+    batches by arrival and free device memory, builds and packs each batch
+    on the device and runs the fused kernel, several batches in flight on
+    their own streams.  torch only provides the device buffers here."""
+
+    def __init__(self, vec_length: int = 8, heads: int = 4, head_dim: int = 64, lhs_bits: int = 8,
+                 rhs_bits: int = 8, scale_qkv: float = 36.0, scale_sfmx: float = 127.0, requant: str = "rowmax",
+                 max_batch_tokens: int = 16384, max_inflight: int = 2, hbm_reserve_bytes: int = 0):
+        self.desc = _lib.McAttnServerDesc(
+            vec_length=vec_length, heads=heads, head_dim=head_dim, lhs_bits=lhs_bits, rhs_bits=rhs_bits,
+            requant=_lib.REQUANT_ROWMAX if requant == "rowmax" else _lib.REQUANT_FIXED, scale_qkv=scale_qkv,
+            scale_sfmx=scale_sfmx, max_batch_tokens=max_batch_tokens, max_inflight=max_inflight,
+            hbm_reserve_bytes=hbm_reserve_bytes)
+        self._h = ctypes.c_void_p()
+        _lib.check(_lib.lib().mcAttnServerCreate(ctypes.byref(self.desc), ctypes.byref(self._h)),
+                   "mcAttnServerCreate")
+
+    @staticmethod
+    def request(mask: VectorSparse, qkv: torch.Tensor, out: torch.Tensor, arrival_s: float = 0.0,
+                device="cuda") -> tuple:
+        """(ctypes request, device buffers it points at) for one sequence:
+        qkv half [3][heads][L][64], out half [heads][L][64]."""
+        ro = torch.from_numpy(np.ascontiguousarray(mask.row_offsets, dtype=np.int32)).to(device)
+        ci = torch.from_numpy(np.ascontiguousarray(mask.col_indices if mask.col_indices.size
+                                                   else np.zeros(1, np.int32), dtype=np.int32)).to(device)
+        lens = np.diff(mask.row_offsets)
+        r = _lib.McAttnRequest(seq_len=mask.ncols, nnz_vec=mask.nnz_vec,
+                               max_row_nnz=int(lens.max()) if lens.size else 0, row_offsets=ro.data_ptr(),
+                               col_indices=ci.data_ptr(), qkv=qkv.data_ptr(), out=out.data_ptr(),
+                               arrival_s=float(arrival_s))
+        return r, (ro, ci, qkv, out)
+
+    def memory(self, reqs: list) -> tuple[int, int]:
+        """(bytes admission charges for one batch of `reqs`, current budget)."""
+        arr = (_lib.McAttnRequest * max(1, len(reqs)))(*reqs)
+        need, avail = ctypes.c_longlong(), ctypes.c_longlong()
+        _lib.check(_lib.lib().mcAttnServerMemory(self._h, arr, len(reqs), ctypes.byref(need), ctypes.byref(avail)),
+                   "mcAttnServerMemory")
+        return int(need.value), int(avail.value)
+
+    def run(self, reqs: list) -> tuple[np.ndarray, dict]:
+        """Serves the requests; returns (latency in ms per request, -1 if
+        rejected) and the run's statistics."""
+        arr = (_lib.McAttnRequest * max(1, len(reqs)))(*reqs)
+        lat = np.zeros(max(1, len(reqs)), dtype=np.float64)
+        st = _lib.McAttnServeStats()
+        torch.cuda.synchronize()
+        _lib.check(_lib.lib().mcAttnServerRun(self._h, arr, len(reqs),
+                                              lat.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                              ctypes.byref(st)), "mcAttnServerRun")
+        stats = {f: getattr(st, f) for f, _ in _lib.McAttnServeStats._fields_}
+        return lat[:len(reqs)], stats
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            _lib.lib().mcAttnServerDestroy(self._h)
+            self._h = ctypes.c_void_p()

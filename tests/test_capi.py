@@ -127,6 +127,25 @@ def test_chunk_starts_count_and_argument_errors():
     assert b"null status" in lib.mcGetLastErrorString()
 
 
+@pytest.mark.parametrize("fields,msg", [
+    (dict(vec_length=3), b"vec_length"), (dict(head_dim=128), b"head_dim"), (dict(lhs_bits=4), b"pairs"),
+    (dict(requant=2), b"requant"), (dict(lhs_bits=16, requant=1), b"row-max"), (dict(scale_qkv=0.0), b"scales"),
+    (dict(max_batch_tokens=0), b"max_batch_tokens"), (dict(max_inflight=9), b"max_inflight"),
+    (dict(hbm_reserve_bytes=-1), b"reserve"),
+])
+def test_attn_server_rejects_bad_descriptors(fields, msg):
+    """The request server checks its descriptor before touching a GPU."""
+    d = _lib.McAttnServerDesc(vec_length=8, heads=4, head_dim=64, lhs_bits=8, rhs_bits=8, requant=1,
+                              scale_qkv=40.0, scale_sfmx=127.0, max_batch_tokens=4096, max_inflight=2)
+    for k, v in fields.items():
+        setattr(d, k, v)
+    h = ctypes.c_void_p()
+    assert _lib.lib().mcAttnServerCreate(ctypes.byref(d), ctypes.byref(h)) == 1
+    assert msg in _lib.lib().mcGetLastErrorString()
+    assert _lib.lib().mcAttnServerRun(None, None, 0, None, None) == 1
+    assert _lib.lib().mcAttnServerMemory(None, None, 0, None, None) == 1
+
+
 def test_tile_mask_words_and_argument_errors():
     lib = _lib.lib()
     assert [lib.mcSddmmTileMaskWords(n) for n in (0, 1, 128, 129, 4096)] == [0, 4, 4, 8, 128]

@@ -451,10 +451,13 @@ def run_gpu(args) -> None:
                               "verified": verify_sddmm(r, pa, pb, v, [B - 1])}
             del r
             torch.cuda.empty_cache()
-        for mma, var, tag in ((1, 0, MMA_NAMES[1]), (1, 3, "tma_gather_kernel"), (2, 0, MMA_NAMES[2]),
-                              (sync_mma, 1, "per_row_kernel"), (0, 4, "dense_tile")):
+        # the dense-tile kernel reads packed values, or the slot-major layout the
+        # packer also writes (its builders then load whole slots)
+        for mma, var, tag, lay in ((1, 0, MMA_NAMES[1], 0), (1, 3, "tma_gather_kernel", 0), (2, 0, MMA_NAMES[2], 0),
+                                   (sync_mma, 1, "per_row_kernel", 0), (0, 4, "dense_tile", 0),
+                                   (0, 4, "dense_tile_slot_major", 2)):
             variants[f"spmm_L8R8_1024x1024x256_{tag}"] = spmm_variant(
-                args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var)
+                args, dev, stream, peaks, world, sync_all, max_over_ranks, mma, var, lay)
         # small vectors: an int8 MMA computes 8 vector lanes of which V are
         # used; the dp4a consumers compute only the V lanes
         for v in (2, 4):
@@ -465,13 +468,13 @@ def run_gpu(args) -> None:
                     torch.cuda.empty_cache()
             # the dense-tile kernel (tcgen05 f16, every product of 256-row tiles):
             # its speed does not depend on V
-            variants[f"spmm_L8R8_4096x4096x256_V{v}_s0.9_dense_tile"] = spmm_point(
-                args, dev, stream, peaks, 4096, 4096, 256, v, 8, 8, 0, variant=4)
+            variants[f"spmm_L8R8_4096x4096x256_V{v}_s0.9_dense_tile_slot_major"] = spmm_point(
+                args, dev, stream, peaks, 4096, 4096, 256, v, 8, 8, 0, variant=4, layout=2)
             torch.cuda.empty_cache()
         for sp in (0.5, 0.7):
-            for var, tag in ((0, "default"), (4, "dense_tile")):
+            for var, tag, lay in ((0, "default", 0), (4, "dense_tile_slot_major", 2)):
                 variants[f"spmm_L8R8_2048x2048x256_V8_s{sp}_{tag}"] = spmm_point(
-                    args, dev, stream, peaks, 2048, 2048, 256, 8, 8, 8, 0, sparsity=sp, variant=var)
+                    args, dev, stream, peaks, 2048, 2048, 256, 8, 8, 8, 0, sparsity=sp, variant=var, layout=lay)
                 torch.cuda.empty_cache()
     attention = serving_res = packer = projection = competitors = native_server = None
     if not args.headline_only and rank == 0:
@@ -537,7 +540,8 @@ def run_gpu(args) -> None:
     reps.close()
 
 
-def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma: int, variant: int = 0) -> dict:
+def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma: int, variant: int = 0,
+                 layout: int = 0) -> dict:
     """SpMM L8-R8: A 1024x1024 V=8 sparsity 0.9, B 1024x256, 256 instances per
     launch (own B and C each, one value set) so a step exceeds 2x L2.
     Algorithmic bytes on the true nonzeros: values nnz V, B K N and C M N 4 per
@@ -549,14 +553,14 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
     from magicube_gb300 import formats, ops
     M, K, N, B = SPMM_M, SPMM_K, SPMM_N, 256
     mask, vals, rng = spmm_operands()
-    h = formats.prepare_spmm(mask, vals, 8, 8)
+    h = formats.prepare_spmm(mask, vals, 8, 8, layout=layout)
     d = ops.DeviceSpmmLhs.from_host(h, dev)
     d.values = d.values.repeat(B)  # one value set per instance
     rhs_h = rng.integers(0, 256, size=(B, K * N), dtype=np.uint8)
     rhs = torch.from_numpy(rhs_h).to(dev)
     out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
     fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size, mma_kind=mma,
-                          variant=variant)
+                          variant=variant, value_layout=layout)
     sync_all()
     ms = time_cuda(fn, args.steps, args.warmup, stream)
     sync_all()
@@ -571,7 +575,7 @@ def spmm_variant(args, dev, stream, peaks, world, sync_all, max_over_ranks, mma:
 
 
 def spmm_point(args, dev, stream, peaks, M: int, K: int, N: int, V: int, pa: int, pb: int, mma: int,
-               sparsity: float = SPARSITY, seed: int = 17, variant: int = 0) -> dict:
+               sparsity: float = SPARSITY, seed: int = 17, variant: int = 0, layout: int = 0) -> dict:
     """One SpMM point of the precision/shape sweep (row lengths normal, cv
     0.3): enough instances per launch that a step moves more than 2.5x L2,
     median of `--steps` CUDA-event timings; the last instance is checked
@@ -582,7 +586,7 @@ def spmm_point(args, dev, stream, peaks, M: int, K: int, N: int, V: int, pa: int
     from magicube_gb300 import formats, ops, synth
     mask = synth.normal_mask(M // V, K, V, sparsity, cv=0.3, seed=seed)
     vals = synth.random_bytes(mask.nnz_vec * V * pa // 8, seed + 1)
-    h = formats.prepare_spmm(mask, vals, pa, pb)
+    h = formats.prepare_spmm(mask, vals, pa, pb, layout=layout)
     l2 = int(getattr(torch.cuda.get_device_properties(dev), "L2_cache_size", 0)) or 129 * 2 ** 20
     per_inst = h.values.size + K * N * pb // 8 + M * N * 4
     B = max(1, min(1024, -(-int(2.5 * l2) // per_inst)))
@@ -592,7 +596,7 @@ def spmm_point(args, dev, stream, peaks, M: int, K: int, N: int, V: int, pa: int
     rhs = torch.from_numpy(rhs_h).to(dev)
     out = torch.empty((B, M, N), dtype=torch.int32, device=dev)
     fn = lambda: ops.spmm(d, rhs, N, signed=True, out=out, batch=B, values_stride=h.values.size,  # noqa: E731
-                          mma_kind=mma, variant=variant)
+                          mma_kind=mma, variant=variant, value_layout=layout)
     t = statistics.median(time_cuda(fn, args.steps, args.warmup, stream)) / 1e3
     opc = 2.0 * mask.nnz_vec * V * N * B
     byts = B * (mask.nnz_vec * V * pa / 8 + K * N * pb / 8 + M * N * 4) + 4 * mask.nnz_vec + 4 * (mask.m_vec + 1)

@@ -142,7 +142,11 @@ int mcSetDefaultMmaKind(int kind);
  *                    256 with unsigned lanes, whose f32 sums stay within 2^24,
  *                    and the segments are added in int32).  Needs the chunk
  *                    table of mcSpmmChunkStarts (strictly increasing columns
- *                    per vector-row) in chunk_starts; row_indices is not read.
+ *                    per vector-row) in chunk_starts and 16-byte aligned
+ *                    column indices; it reads MC_VALUES_PACKED or
+ *                    MC_VALUES_SLOT_MAJOR values (the latter 16-byte aligned
+ *                    with values_stride a multiple of 16); row_indices is not
+ *                    read.
  *                    Its time does not depend on V or on the sparsity.
  * MC_KERNEL_RESIDENT: SpMM only, on the int8 path: each CTA holds a K x 64-byte
  *                    column slice of B in shared memory (loaded once by TMA)
@@ -172,7 +176,13 @@ enum {
  *                    column indices unshuffled.
  * int32 output is provided with MC_VALUES_PACKED, half output with
  * MC_VALUES_SOFTMAX (the combinations the reference uses). */
-enum { MC_VALUES_PACKED = 0, MC_VALUES_SOFTMAX = 1 };
+/* MC_VALUES_SLOT_MAJOR: 8-bit values as [aligned slot][V] bytes (the V lanes
+ *                    of a slot contiguous; column indices unshuffled), what
+ *                    mcPackSpmmValuesEx writes for that layout; read only by
+ *                    MC_KERNEL_DENSE_TILE, whose builders then load whole
+ *                    slots instead of one byte per lane and chunk row.  No
+ *                    reference counterpart. */
+enum { MC_VALUES_PACKED = 0, MC_VALUES_SOFTMAX = 1, MC_VALUES_SLOT_MAJOR = 2 };
 
 /* ---- Extended entry points: batch, stream, signedness, dequantised output --
  * These generalise the reference's batched extension kernels

@@ -120,7 +120,7 @@ REQUANT_FIXED, REQUANT_ROWMAX = 0, 1
 MMA_DEFAULT, MMA_INT8, MMA_F16, MMA_TCGEN05, MMA_DP4A = 0, 1, 2, 3, 4
 KERNEL_AUTO, KERNEL_PER_ROW, KERNEL_STREAM, KERNEL_TMA, KERNEL_DENSE_TILE, KERNEL_RESIDENT = 0, 1, 2, 3, 4, 5
 RESIDENT_AUTO, RESIDENT_S64_W8, RESIDENT_S64_W16, RESIDENT_S128_W16 = 0, 1, 2, 3
-VALUES_PACKED, VALUES_SOFTMAX = 0, 1
+VALUES_PACKED, VALUES_SOFTMAX, VALUES_SLOT_MAJOR = 0, 1, 2
 
 # name -> (restype, argtypes)
 _IP = ctypes.POINTER(ctypes.c_int)

@@ -43,9 +43,10 @@ static int check_spmm(const mcSpmmDesc& d)
     if (d.n / 64 > 65535) return fail(1, "mcSpmm: n too large");
     if (d.batch < 1 || d.batch > 65535) return fail(1, "mcSpmm: batch must be in [1, 65535]");
     if (d.out_half && !d.is_signed) return fail(1, "mcSpmm: half output requires is_signed = 1");
-    if (d.value_layout != (d.out_half ? MC_VALUES_SOFTMAX : MC_VALUES_PACKED))
+    const bool slot_major = d.value_layout == MC_VALUES_SLOT_MAJOR && d.kernel_variant == MC_KERNEL_DENSE_TILE;
+    if (d.value_layout != (d.out_half ? MC_VALUES_SOFTMAX : MC_VALUES_PACKED) && !slot_major)
         return fail(1, "mcSpmm: half output is built for the softmax value layout and int32 output for the "
-                       "packer layout");
+                       "packer layout (or, for the dense-tile kernel, the slot-major layout)");
     if (d.out_half && !d.row_div && !(d.scale != 0.0f))
         return fail(1, "mcSpmm: half output requires a nonzero scale or row divisors");
     if (d.row_div && !d.out_half) return fail(1, "mcSpmm: row divisors apply to half output only");
@@ -70,6 +71,8 @@ static int check_spmm(const mcSpmmDesc& d)
             return fail(1, "mcSpmm: the dense-tile kernel needs rhs_stride a multiple of the B row bytes");
         if (!aligned(d.column_indices, 16))
             return fail(1, "mcSpmm: the dense-tile kernel needs 16-byte aligned column indices");
+        if (slot_major && (!aligned(d.values, 16) || d.values_stride % 16))
+            return fail(1, "mcSpmm: slot-major values must be 16-byte aligned with values_stride % 16 == 0");
     }
     if (d.kernel_config < MC_RESIDENT_AUTO || d.kernel_config > MC_RESIDENT_S128_W16)
         return fail(1, "mcSpmm: invalid kernel_config");

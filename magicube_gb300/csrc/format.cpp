@@ -100,9 +100,26 @@ extern "C" int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int r
     const int V = vec_length;
     if (m_vec < 0 || !(V == 2 || V == 4 || V == 8) || !valid_pair(lhs_bits, rhs_bits) || !row_offsets ||
         !aligned_pairs || !out || aligned_nnz < 0 ||
-        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX) ||
-        (lhs_bits == 12 && value_layout != MC_VALUES_PACKED))
+        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX &&
+         value_layout != MC_VALUES_SLOT_MAJOR) ||
+        (lhs_bits == 12 && value_layout != MC_VALUES_PACKED) ||
+        (value_layout == MC_VALUES_SLOT_MAJOR && (lhs_bits != 8 || rhs_bits != 8)))
         return mc::fail(1, "mcPackSpmmValues: invalid arguments");
+    if (value_layout == MC_VALUES_SLOT_MAJOR) {
+        // [aligned slot][V] bytes: the lanes of a slot side by side
+        const uint8_t* src = static_cast<const uint8_t*>(values);
+        uint8_t* dst = static_cast<uint8_t*>(out);
+        std::memset(dst, 0, (size_t)aligned_nnz * V);
+        for (int i = 0; i < m_vec; ++i) {
+            const int b = row_offsets[i], e = row_offsets[i + 1];
+            for (int j = b; j < e; ++j) {
+                const long long slot = (long long)aligned_pairs[2 * i] + (j - b);
+                if (slot >= aligned_nnz) return mc::fail(1, "mcPackSpmmValues: aligned_nnz too small");
+                std::memcpy(dst + slot * V, src + (long long)j * V, (size_t)V);
+            }
+        }
+        return 0;
+    }
     // 12-bit values sit in 16-bit containers and use the 16-bit layouts with
     // the top 4 bits cleared (spmm_benchmark.cpp:288-358).
     const uint32_t vmask = lhs_bits == 12 ? 0xFFFu : 0xFFFFFFFFu;

@@ -109,7 +109,7 @@ __device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t smem_addr, uint32_t m
     return d;
 }
 
-template <int V, bool SIGNED>
+template <int V, bool SIGNED, bool SLOTMAJOR = false>
 __global__ void __launch_bounds__(sdense::THREADS, 1)
 spmm_dense_tc_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmDenseParams dp, unsigned int* timeouts)
 {
@@ -365,15 +365,37 @@ spmm_dense_tc_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmDensePa
                         for (int i = 0; i < QU; ++i) {
                             const int j0 = (qb + G * i < qhi ? qb + G * i : qb) * 4;
                             c4[i] = ldg_nc_v4(p.col_indices + j0);
-                            const uint8_t* src = vals + (long long)(j0 >> 4) * (16 * V) + (j0 & 15);
+                            if constexpr (SLOTMAJOR) {
+                                // the quad's 4 x V bytes, already slot by slot: w[s] (and
+                                // w[4 + s]) as the transposes below leave them
+                                const uint8_t* src = vals + (long long)j0 * V;
+                                if constexpr (V == 8) {
+                                    const int4 a = ldg_nc_v4(src), b = ldg_nc_v4(src + 16);
+                                    w[i][0] = (uint32_t)a.x; w[i][4] = (uint32_t)a.y;
+                                    w[i][1] = (uint32_t)a.z; w[i][5] = (uint32_t)a.w;
+                                    w[i][2] = (uint32_t)b.x; w[i][6] = (uint32_t)b.y;
+                                    w[i][3] = (uint32_t)b.z; w[i][7] = (uint32_t)b.w;
+                                } else if constexpr (V == 4) {
+                                    const int4 a = ldg_nc_v4(src);
+                                    w[i][0] = (uint32_t)a.x; w[i][1] = (uint32_t)a.y;
+                                    w[i][2] = (uint32_t)a.z; w[i][3] = (uint32_t)a.w;
+                                } else {
+                                    const int2 a = ldg_nc_v2(src);  // slots 0-1 in a.x, 2-3 in a.y
+                                    w[i][0] = (uint32_t)a.x;
+                                    w[i][1] = (uint32_t)a.y;
+                                }
+                            } else {
+                                const uint8_t* src = vals + (long long)(j0 >> 4) * (16 * V) + (j0 & 15);
 #pragma unroll
-                            for (int v = 0; v < V; ++v) w[i][v] = __ldg(reinterpret_cast<const uint32_t*>(src + 16 * v));
+                                for (int v = 0; v < V; ++v)
+                                    w[i][v] = __ldg(reinterpret_cast<const uint32_t*>(src + 16 * v));
+                            }
                         }
 #pragma unroll
                         for (int i = 0; i < QU; ++i) {
                             if (qb + G * i >= qhi) break;
                             const int j0 = (qb + G * i) * 4;
-                            if constexpr (V >= 4) {
+                            if constexpr (V >= 4 && !SLOTMAJOR) {
                                 // w[v] holds lane v of the four slots; after this w[s] holds
                                 // lanes 0-3 of slot s (and w[4 + s] lanes 4-7)
                                 uint32_t a[4] = {w[i][0], w[i][1], w[i][2], w[i][3]};
@@ -404,7 +426,11 @@ spmm_dense_tc_kernel(const __grid_constant__ CUtensorMap tmap, const SpmmDensePa
                                     bytes_to_h2<SIGNED>(w[i][e], h0, h1);
                                     *reinterpret_cast<uint2*>(dst) = make_uint2(h0, h1);
                                 } else {
-                                    bytes_to_h2<SIGNED>(prmt(w[i][0], w[i][1], (uint32_t)(e | ((e + 4) << 4))), h0, h1);
+                                    // slot-major: slot e's two lanes are bytes 2e, 2e + 1 of the
+                                    // 8 loaded bytes; packed: byte e of lane 0's and lane 1's word
+                                    const uint32_t x = SLOTMAJOR ? (w[i][e >> 1] >> (16 * (e & 1)))
+                                                                 : prmt(w[i][0], w[i][1], (uint32_t)(e | ((e + 4) << 4)));
+                                    bytes_to_h2<SIGNED>(x, h0, h1);
                                     *reinterpret_cast<uint32_t*>(dst) = h0;
                                 }
                                 nm |= 1ull << kk;

@@ -6,10 +6,10 @@
 
 namespace mc {
 
-template <int V, bool S>
+template <int V, bool S, bool SM>
 static int spmm_dense_launch_t(const CUtensorMap& map, const SpmmDenseParams& dp, cudaStream_t s)
 {
-    auto kern = spmm_dense_tc_kernel<V, S>;
+    auto kern = spmm_dense_tc_kernel<V, S, SM>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, sdense::SMEM) != cudaSuccess)
         return fail((int)cudaGetLastError(), "mcSpmm: cannot reserve shared memory for the dense-tile kernel");
     unsigned int* timeouts = async_timeout_counter();
@@ -46,11 +46,17 @@ int spmm_dense_launch(const mcSpmmDesc& d, cudaStream_t s)
     if (!encode_box_u8(&map, d.rhs, (long long)dp.rows_per_entry * (d.batch - 1) + d.k, row_bytes, sdense::BN,
                        sdense::KC))
         return fail(1, "mcSpmm: TMA tensor map encoding failed");
+    const bool sm = d.value_layout == MC_VALUES_SLOT_MAJOR;
+#define MC_DENSE_V(VV)                                                                              \
+    if (sm) return d.is_signed ? spmm_dense_launch_t<VV, true, true>(map, dp, s)                     \
+                               : spmm_dense_launch_t<VV, false, true>(map, dp, s);                   \
+    return d.is_signed ? spmm_dense_launch_t<VV, true, false>(map, dp, s) : spmm_dense_launch_t<VV, false, false>(map, dp, s);
     switch (d.vec_length) {
-        case 2: return d.is_signed ? spmm_dense_launch_t<2, true>(map, dp, s) : spmm_dense_launch_t<2, false>(map, dp, s);
-        case 4: return d.is_signed ? spmm_dense_launch_t<4, true>(map, dp, s) : spmm_dense_launch_t<4, false>(map, dp, s);
-        default: return d.is_signed ? spmm_dense_launch_t<8, true>(map, dp, s) : spmm_dense_launch_t<8, false>(map, dp, s);
+        case 2: { MC_DENSE_V(2) }
+        case 4: { MC_DENSE_V(4) }
+        default: { MC_DENSE_V(8) }
     }
+#undef MC_DENSE_V
 }
 
 }  // namespace mc

@@ -74,7 +74,7 @@ def pad_column_indices(mask: VectorSparse, pairs: np.ndarray, aligned_nnz: int, 
     return out[:aligned_nnz]
 
 
-VALUES_PACKED, VALUES_SOFTMAX = 0, 1
+VALUES_PACKED, VALUES_SOFTMAX, VALUES_SLOT_MAJOR = 0, 1, 2
 
 
 def pack_spmm_values(mask: VectorSparse, pairs: np.ndarray, aligned_nnz: int, values: np.ndarray,

@@ -112,13 +112,16 @@ class DeviceSddmmMask:
 def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, out: torch.Tensor | None = None,
          out_half: bool = False, scale: float = 1.0, batch: int = 1, values_stride: int = 0,
          rhs_stride: int | None = None, out_stride: int | None = None, mma_kind: int = 0, variant: int = 0,
-         config: int = 0, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
+         config: int = 0, stream: torch.cuda.Stream | None = None, value_layout: int | None = None) -> torch.Tensor:
     """C = A * B for a batch of `batch` entries (shared mask).
 
     rhs: packed B, k rows of n*rhs_bits/8 bytes per batch entry, contiguous.
     Strides are in bytes for values/rhs and elements for out; a zero stride
     shares the operand across the batch.  `config` picks the slice width and
-    CTA size of variant KERNEL_RESIDENT (RESIDENT_*; 0 = automatic)."""
+    CTA size of variant KERNEL_RESIDENT (RESIDENT_*; 0 = automatic).
+    `value_layout` names the layout of lhs.values when it is not the default
+    (VALUES_SOFTMAX with half output, VALUES_PACKED otherwise):
+    VALUES_SLOT_MAJOR values go to the dense-tile kernel."""
     M = lhs.m_vec * lhs.vec_length
     if rhs_stride is None:
         rhs_stride = lhs.k * n * lhs.rhs_bits // 8 if batch > 1 else 0
@@ -133,7 +136,9 @@ def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, 
         row_indices=lhs.row_indices.data_ptr(), row_offsets=lhs.row_offsets.data_ptr(),
         column_indices=lhs.col_indices.data_ptr(), values=lhs.values.data_ptr(), values_stride=values_stride,
         rhs=rhs.data_ptr(), rhs_stride=rhs_stride, out=out.data_ptr(), out_stride=out_stride, mma_kind=mma_kind,
-        kernel_variant=variant, value_layout=_lib.VALUES_SOFTMAX if out_half else _lib.VALUES_PACKED,
+        kernel_variant=variant,
+        value_layout=(value_layout if value_layout is not None
+                      else _lib.VALUES_SOFTMAX if out_half else _lib.VALUES_PACKED),
         kernel_config=config)
     if variant == _lib.KERNEL_DENSE_TILE:
         d.chunk_starts = lhs.chunk_starts(stream).data_ptr()

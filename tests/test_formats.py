@@ -73,3 +73,19 @@ def test_pack_then_decode_wide_pairs(pa, pb, V):
         a = oracle.spmm_host(vals, rhs, m.row_offsets, m.col_indices, m.m_vec, V, K, N, 16, pb, mode, preA_cut=pa)
         b = oracle.spmm_device(h.row_offsets, h.col_indices, h.values, rhs, m.m_vec, V, K, N, 16, pb, mode)
         np.testing.assert_array_equal(a, b)
+
+
+def test_slot_major_layout_on_the_host():
+    """The slot-major layout is the plain values of each slot side by side at
+    the slot's aligned position, zeros in the padding slots."""
+    V, K = 4, 256
+    mask = synth.lengths_mask([3, 0, 17, 5], K, V, seed=2)
+    vals = synth.random_bytes(mask.nnz_vec * V, 3)
+    h = formats.prepare_spmm(mask, vals, 8, 8, layout=formats.VALUES_SLOT_MAJOR)
+    got = h.values.reshape(-1, V)
+    for r in range(mask.m_vec):
+        start, n = h.row_offsets[2 * r], mask.row_offsets[r + 1] - mask.row_offsets[r]
+        want = vals.reshape(-1, V)[mask.row_offsets[r]:mask.row_offsets[r + 1]]
+        np.testing.assert_array_equal(got[start:start + n], want)
+        end = h.aligned_nnz if r == mask.m_vec - 1 else h.row_offsets[2 * r + 2]
+        assert not got[start + n:end].any()

@@ -21,27 +21,33 @@ def _ref(mask, vals, rhs, V, K, N, signed):
                             oracle.SIGNED if signed else oracle.UNSIGNED)
 
 
-def _dev(cuda, mask, vals):
-    return ops.DeviceSpmmLhs.from_host(formats.prepare_spmm(mask, vals, 8, 8), cuda)
+SLOT = formats.VALUES_SLOT_MAJOR
+
+
+def _dev(cuda, mask, vals, layout=formats.VALUES_PACKED):
+    return ops.DeviceSpmmLhs.from_host(formats.prepare_spmm(mask, vals, 8, 8, layout=layout), cuda)
 
 
 @pytest.mark.parametrize("V", [2, 4, 8])
 @pytest.mark.parametrize("signed", [False, True])
 @pytest.mark.parametrize("N", [128, 384])
-def test_dense_ragged(cuda, V, signed, N):
+@pytest.mark.parametrize("layout", [formats.VALUES_PACKED, formats.VALUES_SLOT_MAJOR])
+def test_dense_ragged(cuda, V, signed, N, layout):
     """Row lengths around every chunk boundary, empty rows, a row count that
-    leaves the last 256-row block partly empty."""
+    leaves the last 256-row block partly empty; packed and slot-major values."""
     K = 256
     mask = synth.lengths_mask(RAGGED, K, V, seed=V + 11)
     vals = synth.random_bytes(mask.nnz_vec * V, 40 + V)
     rhs = synth.random_bytes(K * N, 41 + V)
-    out = ops.spmm(_dev(cuda, mask, vals), torch.from_numpy(rhs).to(cuda), N, signed=signed, variant=DENSE)
+    out = ops.spmm(_dev(cuda, mask, vals, layout), torch.from_numpy(rhs).to(cuda), N, signed=signed, variant=DENSE,
+                   value_layout=layout)
     np.testing.assert_array_equal(out.cpu().numpy(), _ref(mask, vals, rhs, V, K, N, signed))
 
 
 @pytest.mark.parametrize("signed", [False, True])
 @pytest.mark.parametrize("K", [40, 64, 100, 257, 1024, 1100, 2500])
-def test_dense_k_segments(cuda, signed, K):
+@pytest.mark.parametrize("layout", [formats.VALUES_PACKED, formats.VALUES_SLOT_MAJOR])
+def test_dense_k_segments(cuda, signed, K, layout):
     """k not a multiple of 64 (the last chunk's B rows reach past the matrix
     or into the next batch entry), k across accumulation segments (1024
     columns signed, 256 unsigned), two batch entries with their own A values
@@ -52,12 +58,12 @@ def test_dense_k_segments(cuda, signed, K):
     mask = synth.lengths_mask(lengths, K, V, seed=K + 1)
     vals = [synth.random_bytes(mask.nnz_vec * V, 50 + b) for b in range(B)]
     rhs = [synth.random_bytes(K * N, 60 + b) for b in range(B)]
-    h = [formats.prepare_spmm(mask, v, 8, 8) for v in vals]
+    h = [formats.prepare_spmm(mask, v, 8, 8, layout=layout) for v in vals]
     d = ops.DeviceSpmmLhs.from_host(h[0], cuda)
     vstride = h[0].values.size
     d.values = torch.from_numpy(np.concatenate([x.values for x in h])).to(cuda)
     out = ops.spmm(d, torch.from_numpy(np.concatenate(rhs)).to(cuda), N, signed=signed, batch=B,
-                   values_stride=vstride, variant=DENSE)
+                   values_stride=vstride, variant=DENSE, value_layout=layout)
     for b in range(B):
         np.testing.assert_array_equal(out[b].cpu().numpy(), _ref(mask, vals[b], rhs[b], V, K, N, signed))
 

@@ -1279,14 +1279,15 @@ def run_profile_case(args) -> None:
         N = 256
         mask = synth.uniform_mask(M // VEC, K, VEC, SPARSITY, seed=7)
         vals = np.random.default_rng(8).integers(0, 256, size=mask.nnz_vec * VEC, dtype=np.uint8)
-        h = formats.prepare_spmm(mask, vals, 8, 8)
+        layout = formats.VALUES_SLOT_MAJOR if args.spmm_values == "slot_major" else formats.VALUES_PACKED
+        h = formats.prepare_spmm(mask, vals, 8, 8, layout=layout)
         d = ops.DeviceSpmmLhs.from_host(h, dev)
         d.values = d.values.repeat(args.batch)
         rhs = torch.randint(0, 256, (args.batch, K * N), dtype=torch.uint8, device=dev)
         out = torch.empty((args.batch, M, N), dtype=torch.int32, device=dev)
         for _ in range(args.reps):
             ops.spmm(d, rhs, N, signed=True, out=out, batch=args.batch, values_stride=h.values.size,
-                     mma_kind=0 if args.spmm_kernel == 4 else args.mma, variant=args.spmm_kernel)
+                     mma_kind=0 if args.spmm_kernel == 4 else args.mma, variant=args.spmm_kernel, value_layout=layout)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": args.profile, "batch": args.batch, "reps": args.reps}))
 
@@ -1319,6 +1320,8 @@ def main() -> None:
                     help="SDDMM kernel variant of the --profile sddmm case")
     ap.add_argument("--spmm-kernel", choices=["auto", "per_row", "stream", "tma", "resident", "dense"], default="auto",
                     help="SpMM kernel variant of the --profile spmm and spmm-v2 cases")
+    ap.add_argument("--spmm-values", choices=["packed", "slot_major"], default="packed",
+                    help="value layout of the --profile spmm case (slot-major: the dense-tile kernel's own)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sweep", choices=["square", "full"], default=None,
                     help="run only the SpMM precision/shape sweep (M = K, or every M, K pair)")

@@ -178,8 +178,9 @@ enum {
  * MC_VALUES_SOFTMAX (the combinations the reference uses). */
 /* MC_VALUES_SLOT_MAJOR: 8-bit values as [aligned slot][V] bytes (the V lanes
  *                    of a slot contiguous; column indices unshuffled), what
- *                    mcPackSpmmValuesEx writes for that layout; read only by
- *                    MC_KERNEL_DENSE_TILE, whose builders then load whole
+ *                    mcPackSpmmValuesEx / mcDevicePack write for that
+ *                    layout; read only by MC_KERNEL_DENSE_TILE (which
+ *                    MC_KERNEL_AUTO then picks), whose builders load whole
  *                    slots instead of one byte per lane and chunk row.  No
  *                    reference counterpart. */
 enum { MC_VALUES_PACKED = 0, MC_VALUES_SOFTMAX = 1, MC_VALUES_SLOT_MAJOR = 2 };
@@ -208,7 +209,7 @@ typedef struct mcSpmmDesc {
     void* out;            long long out_stride;     /* elements */
     int mma_kind;               /* MC_MMA_DEFAULT / MC_MMA_INT8 / MC_MMA_F16 */
     int kernel_variant;         /* MC_KERNEL_AUTO / _PER_ROW / _STREAM / _TMA / _RESIDENT */
-    int value_layout;           /* MC_VALUES_PACKED / MC_VALUES_SOFTMAX */
+    int value_layout;           /* MC_VALUES_PACKED / _SOFTMAX / _SLOT_MAJOR */
     /* Optional, half output only: out[row][c] = half(acc / row_div[row]) per
      * output row (M = m_vec * vec_length floats per batch entry, e.g. the
      * divisors mcQuantSoftmax writes with MC_REQUANT_ROWMAX) instead of / scale. */
@@ -494,7 +495,8 @@ int mcPadColumnIndices(int m_vec, const int* row_offsets, const int* col_indices
  * aligned_nnz*V*lhs_bits/8 bytes (16 bits per lane for 12-bit values). */
 int mcPackSpmmValues(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
                      const int* aligned_pairs, int aligned_nnz, const void* values, void* out);
-/* Same, for either value layout (MC_VALUES_PACKED or MC_VALUES_SOFTMAX). */
+/* Same, for any value layout (MC_VALUES_PACKED, MC_VALUES_SOFTMAX, or
+ * MC_VALUES_SLOT_MAJOR for 8-bit values of the L8-R8 pair). */
 int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
                        const int* aligned_pairs, int aligned_nnz, const void* values, void* out,
                        int value_layout);
@@ -542,7 +544,8 @@ int mcDevicePadColumnIndices(int m_vec, const int* row_offsets, const int* col_i
                              const int* aligned_pairs, const int* aligned_nnz, int shuffle8, int* out_cols,
                              long long capacity, int* status, cudaStream_t stream);
 /* Values into the SpMM device layout (as mcPackSpmmValuesEx); out 4-byte
- * aligned, capacity_bytes its size.  Row slots must be whole value chunks. */
+ * aligned (16-byte for MC_VALUES_SLOT_MAJOR), capacity_bytes its size.  Row
+ * slots must be whole value chunks (16 slots for the slot-major layout). */
 int mcDevicePackSpmmValues(int m_vec, int vec_length, int lhs_bits, int rhs_bits, const int* row_offsets,
                            const int* aligned_pairs, const int* aligned_nnz, const void* values, void* out,
                            long long capacity_bytes, int value_layout, int* status, cudaStream_t stream);
@@ -559,7 +562,7 @@ typedef struct mcDevicePackDesc {
     int lhs_bits, rhs_bits;       /* the SpMM pair, or lhs_bits = 0 */
     int alignment;
     int shuffle8;                 /* 8-shuffle the columns (packed layout with a 4-bit operand) */
-    int value_layout;             /* MC_VALUES_PACKED / MC_VALUES_SOFTMAX */
+    int value_layout;             /* MC_VALUES_PACKED / _SOFTMAX / _SLOT_MAJOR (L8-R8) */
     int sort_rows;                /* 1: longest-first row_indices; 0: row_indices untouched */
     const int* row_offsets;       /* m_vec + 1 */
     const int* col_indices;
@@ -567,7 +570,7 @@ typedef struct mcDevicePackDesc {
     int* aligned_pairs;           /* 2 * m_vec, 8-byte aligned */
     int* aligned_nnz;             /* one device int */
     int* out_cols;       long long cols_capacity;         /* elements */
-    void* out_values;    long long values_capacity_bytes; /* 4-byte aligned */
+    void* out_values;    long long values_capacity_bytes; /* 4-byte aligned (slot-major: 16) */
     int* row_indices;             /* m_vec */
     int* status;                  /* optional device int, set to 1 on inconsistent rows */
 } mcDevicePackDesc;

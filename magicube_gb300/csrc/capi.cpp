@@ -146,7 +146,10 @@ int mcSpmm(const mcSpmmDesc* desc, cudaStream_t stream)
 {
     mc::clear_error();
     if (!desc) return mc::fail(1, "mcSpmm: null descriptor");
-    const mcSpmmDesc& d = *desc;
+    mcSpmmDesc d = *desc;
+    // slot-major values are read by the dense-tile kernel alone
+    if (d.kernel_variant == MC_KERNEL_AUTO && d.value_layout == MC_VALUES_SLOT_MAJOR)
+        d.kernel_variant = MC_KERNEL_DENSE_TILE;
     if (int rc = mc::check_spmm(d)) return rc;
     if (d.m_vec == 0) return 0;
     if (d.kernel_variant == MC_KERNEL_DENSE_TILE) return mc::spmm_dense_launch(d, stream);

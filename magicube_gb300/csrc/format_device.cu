@@ -378,6 +378,54 @@ fill_rows_kernel(int m_vec, const int* __restrict__ ro, const int* __restrict__ 
     }
 }
 
+// MC_VALUES_SLOT_MAJOR, 8-bit lanes ([aligned slot][V] bytes): slot s of a
+// row's aligned range takes the row's vector s - start whole, the padding
+// slots zeros.  ALIGNED: the source is V-byte aligned, one load per vector.
+template <int V, bool ALIGNED>
+__global__ void __launch_bounds__(256)
+fill_rows_slot_kernel(int m_vec, const int* __restrict__ ro, const int* __restrict__ pairs,
+                      const int* __restrict__ total, int unit, long long cap, const int* __restrict__ cols,
+                      int shuffle8, int* __restrict__ cols_out, const uint8_t* __restrict__ src,
+                      uint8_t* __restrict__ vals_out, int* status)
+{
+    using Vec = typename std::conditional<V == 8, uint2, typename std::conditional<V == 4, uint32_t, uint16_t>::type>::type;
+    const int rows = m_vec > 0 ? m_vec : 1;
+    const int lane = threadIdx.x & 31;
+    const int nwarps = gridDim.x * (blockDim.x >> 5);
+    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < rows; i += nwarps) {
+        RowSpan r;
+        if (!row_span(i, m_vec, ro, pairs, total, unit, cap, r)) {
+            if (status && lane == 0) *status = 1;
+            continue;
+        }
+        if (cols_out) pad_row_columns(r, cols, shuffle8 != 0, cols_out, lane);
+        for (long long s0 = r.lo + lane; s0 < r.hi; s0 += 32 * kUnroll) {
+            Vec x[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const long long jr = s0 + 32 * u - r.start;
+                x[u] = Vec{};
+                if (s0 + 32 * u < r.hi && jr >= 0 && jr < r.len) {
+                    const uint8_t* p = src + (r.src + jr) * V;
+                    if constexpr (ALIGNED) {
+                        x[u] = __ldg(reinterpret_cast<const Vec*>(p));
+                    } else {
+                        uint8_t b[V];
+#pragma unroll
+                        for (int v = 0; v < V; ++v) b[v] = __ldg(p + v);
+                        memcpy(&x[u], b, V);
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; ++u) {
+                const long long s = s0 + 32 * u;
+                if (s < r.hi) *reinterpret_cast<Vec*>(vals_out + s * V) = x[u];
+            }
+        }
+    }
+}
+
 __global__ void row_keys_kernel(int m_vec, const int* __restrict__ ro, int* __restrict__ len,
                                 int* __restrict__ idx)
 {
@@ -433,9 +481,27 @@ int fill_launch(const FillArgs& a, cudaStream_t s)
     return (int)cudaGetLastError();
 }
 
+// Slot-major 8-bit values: rows aligned to 16 slots, as the packed L8-R8
+// layout, so one set of aligned pairs serves both.
+template <int V>
+int fill_slot(const FillArgs& a, cudaStream_t s)
+{
+    const int grid = grid_for_warps(a.m_vec > 0 ? a.m_vec : 1);
+    long long cap = a.vals_cap_bytes / V;
+    if (a.cols_out && a.cols_cap < cap) cap = a.cols_cap;
+    if (reinterpret_cast<uintptr_t>(a.src) % V == 0)
+        fill_rows_slot_kernel<V, true><<<grid, 256, 0, s>>>(a.m_vec, a.ro, a.pairs, a.total, 16, cap, a.cols,
+                                                            a.shuffle8, a.cols_out, a.src, a.vals_out, a.status);
+    else
+        fill_rows_slot_kernel<V, false><<<grid, 256, 0, s>>>(a.m_vec, a.ro, a.pairs, a.total, 16, cap, a.cols,
+                                                             a.shuffle8, a.cols_out, a.src, a.vals_out, a.status);
+    return (int)cudaGetLastError();
+}
+
 template <int V>
 int fill_v(int lhs_bits, int rhs_bits, int layout, const FillArgs& a, cudaStream_t s)
 {
+    if (layout == MC_VALUES_SLOT_MAJOR) return fill_slot<V>(a, s);
     const bool four = lhs_bits == 4 || rhs_bits == 4;
     if (layout == MC_VALUES_SOFTMAX) {
         if (lhs_bits == 4) return fill_launch<V, 4, 32, false>(a, s);
@@ -617,10 +683,14 @@ extern "C" int mcDevicePackSpmmValues(int m_vec, int vec_length, int lhs_bits, i
     mc::clear_error();
     if (m_vec < 0 || !(vec_length == 2 || vec_length == 4 || vec_length == 8) || !mc::valid_pair(lhs_bits, rhs_bits) ||
         !row_offsets || !aligned_nnz || !out || capacity_bytes < 0 ||
-        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX) || (m_vec > 0 && !aligned_pairs) ||
-        (lhs_bits == 12 && value_layout != MC_VALUES_PACKED))
+        (value_layout != MC_VALUES_PACKED && value_layout != MC_VALUES_SOFTMAX &&
+         value_layout != MC_VALUES_SLOT_MAJOR) ||
+        (m_vec > 0 && !aligned_pairs) || (lhs_bits == 12 && value_layout != MC_VALUES_PACKED))
         return mc::fail(1, "mcDevicePackSpmmValues: invalid arguments");
-    if (reinterpret_cast<uintptr_t>(out) % 4) return mc::fail(1, "mcDevicePackSpmmValues: out must be 4-byte aligned");
+    if (value_layout == MC_VALUES_SLOT_MAJOR && (lhs_bits != 8 || rhs_bits != 8))
+        return mc::fail(1, "mcDevicePackSpmmValues: the slot-major layout holds 8-bit values of the L8-R8 pair");
+    if (reinterpret_cast<uintptr_t>(out) % (value_layout == MC_VALUES_SLOT_MAJOR ? 16 : 4))
+        return mc::fail(1, "mcDevicePackSpmmValues: out must be 4-byte aligned (16 for slot-major values)");
     mc::FillArgs a{m_vec, row_offsets, aligned_pairs, aligned_nnz, nullptr, 0, nullptr, 0,
                    static_cast<const uint8_t*>(values), static_cast<uint8_t*>(out), capacity_bytes, status,
                    0xFFFFFFFFu};
@@ -666,11 +736,15 @@ extern "C" int mcDevicePack(const mcDevicePackDesc* d, cudaStream_t stream)
     if (values) {
         if (!(d->vec_length == 2 || d->vec_length == 4 || d->vec_length == 8) ||
             !mc::valid_pair(d->lhs_bits, d->rhs_bits) ||
-            (d->value_layout != MC_VALUES_PACKED && d->value_layout != MC_VALUES_SOFTMAX) || !d->out_values ||
-            d->values_capacity_bytes < 0 || reinterpret_cast<uintptr_t>(d->out_values) % 4)
+            (d->value_layout != MC_VALUES_PACKED && d->value_layout != MC_VALUES_SOFTMAX &&
+             d->value_layout != MC_VALUES_SLOT_MAJOR) ||
+            !d->out_values || d->values_capacity_bytes < 0 || reinterpret_cast<uintptr_t>(d->out_values) % 4)
             return mc::fail(1, "mcDevicePack: invalid value arguments (pair, vec_length, layout, 4-byte aligned out)");
         if (d->lhs_bits == 12 && d->value_layout != MC_VALUES_PACKED)
             return mc::fail(1, "mcDevicePack: 12-bit values use the packed layout");
+        if (d->value_layout == MC_VALUES_SLOT_MAJOR &&
+            (d->lhs_bits != 8 || d->rhs_bits != 8 || reinterpret_cast<uintptr_t>(d->out_values) % 16))
+            return mc::fail(1, "mcDevicePack: slot-major values are L8-R8 with out_values 16-byte aligned");
         const int chunk = (d->value_layout == MC_VALUES_SOFTMAX) ? (d->lhs_bits == 4 ? 32 : 16)
                                                                    : ((d->lhs_bits == 4 || d->rhs_bits == 4) ? 32 : 16);
         if (alignment == 0) alignment = (d->lhs_bits == 4 || d->rhs_bits == 4) ? 32 : 16;

@@ -22,7 +22,7 @@ import ctypes
 import torch
 
 from . import _lib
-from .formats import VALUES_PACKED, VALUES_SOFTMAX, lane_bits, spmm_chunk
+from .formats import VALUES_PACKED, VALUES_SLOT_MAJOR, VALUES_SOFTMAX, lane_bits, spmm_chunk
 from .ops import DeviceSddmmMask, DeviceSpmmLhs
 
 
@@ -169,4 +169,4 @@ def prepare_sddmm(row_offsets: torch.Tensor, col_indices: torch.Tensor, vec_leng
 
 
 __all__ = ["align_row_offsets", "pad_column_indices", "pack_spmm_values", "sorted_row_swizzle", "prepare_spmm",
-           "prepare_sddmm", "PackError", "VALUES_PACKED", "VALUES_SOFTMAX"]
+           "prepare_sddmm", "PackError", "VALUES_PACKED", "VALUES_SOFTMAX", "VALUES_SLOT_MAJOR"]

@@ -140,7 +140,7 @@ def spmm(lhs: DeviceSpmmLhs, rhs: torch.Tensor, n: int, *, signed: bool = True, 
         value_layout=(value_layout if value_layout is not None
                       else _lib.VALUES_SOFTMAX if out_half else _lib.VALUES_PACKED),
         kernel_config=config)
-    if variant == _lib.KERNEL_DENSE_TILE:
+    if variant == _lib.KERNEL_DENSE_TILE or (variant == _lib.KERNEL_AUTO and d.value_layout == _lib.VALUES_SLOT_MAJOR):
         d.chunk_starts = lhs.chunk_starts(stream).data_ptr()
     _lib.check(_lib.lib().mcSpmm(ctypes.byref(d), _stream_handle(stream)), "mcSpmm")
     return out

@@ -118,6 +118,21 @@ def test_spmm_dense_tile_errors(fields, msg):
     assert msg in _lib.lib().mcGetLastErrorString()
 
 
+@pytest.mark.parametrize("fields,msg", [
+    (dict(rhs_bits=4), b"L8-R8 with int32 output"),
+    (dict(), b"chunk table"),
+])
+def test_spmm_auto_with_slot_major_values_takes_dense_tile(fields, msg):
+    """Slot-major values under MC_KERNEL_AUTO go to the dense-tile kernel
+    (its checks answer), since no other kernel reads that layout."""
+    d = _lib.McSpmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1, scale=1.0,
+                        kernel_variant=_lib.KERNEL_AUTO, value_layout=_lib.VALUES_SLOT_MAJOR)
+    for k, v in fields.items():
+        setattr(d, k, v)
+    assert _lib.lib().mcSpmm(ctypes.byref(d), None) == 1
+    assert msg in _lib.lib().mcGetLastErrorString()
+
+
 def test_chunk_starts_count_and_argument_errors():
     lib = _lib.lib()
     assert [lib.mcSpmmChunkStartsCount(k) for k in (0, 1, 64, 65, 1024)] == [0, 2, 2, 3, 17]
@@ -125,6 +140,28 @@ def test_chunk_starts_count_and_argument_errors():
     assert b"k > 0" in lib.mcGetLastErrorString()
     assert lib.mcSpmmChunkStarts(4, 64, None, None, None, None, None) == 1
     assert b"null status" in lib.mcGetLastErrorString()
+
+
+def test_device_slot_major_pack_argument_errors():
+    """The device packers take slot-major values for L8-R8 only, into a
+    16-byte aligned buffer; both checks run before any GPU work."""
+    lib = _lib.lib()
+    one = ctypes.c_int(0)
+    ro = (ctypes.c_int * 2)(0, 0)
+    rc = lib.mcDevicePackSpmmValues(1, 8, 8, 4, ctypes.addressof(ro), ctypes.addressof(ro), ctypes.addressof(one),
+                                    None, 64, 64, _lib.VALUES_SLOT_MAJOR, None, None)
+    assert rc == 1 and b"L8-R8" in lib.mcGetLastErrorString()
+    rc = lib.mcDevicePackSpmmValues(1, 8, 8, 8, ctypes.addressof(ro), ctypes.addressof(ro), ctypes.addressof(one),
+                                    None, 68, 64, _lib.VALUES_SLOT_MAJOR, None, None)
+    assert rc == 1 and b"16 for slot-major" in lib.mcGetLastErrorString()
+    d = _lib.McDevicePackDesc(m_vec=1, vec_length=8, lhs_bits=8, rhs_bits=4, value_layout=_lib.VALUES_SLOT_MAJOR,
+                              row_offsets=ctypes.addressof(ro), aligned_nnz=ctypes.addressof(one), out_cols=64,
+                              aligned_pairs=64, row_indices=64, out_values=64, values_capacity_bytes=64)
+    assert lib.mcDevicePack(ctypes.byref(d), None) == 1
+    assert b"slot-major" in lib.mcGetLastErrorString()
+    d.rhs_bits, d.out_values = 8, 68
+    assert lib.mcDevicePack(ctypes.byref(d), None) == 1
+    assert b"16-byte aligned" in lib.mcGetLastErrorString()
 
 
 @pytest.mark.parametrize("fields,msg", [

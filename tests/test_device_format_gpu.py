@@ -4,9 +4,10 @@ import numpy as np
 import pytest
 import torch
 
+import oracle
 from golden_util import load, names, unpack_spmm_values
 from magicube_gb300 import device_format as dfm
-from magicube_gb300 import formats, ops, synth
+from magicube_gb300 import _lib, formats, ops, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -44,6 +45,45 @@ def test_device_packer_equals_host_packer(cuda, pa, pb, V, layout):
     m = synth.lengths_mask([0, 1, 15, 16, 17, 31, 32, 33, 100, 0, 7, 64], 256, V, seed=pa * 7 + pb + V)
     vals = synth.random_bytes(m.nnz_vec * V * formats.lane_bits(pa) // 8, V + pa)
     _check_spmm(m, vals, pa, pb, layout, cuda)
+
+
+@pytest.mark.parametrize("V", [2, 4, 8])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_device_slot_major_equals_host(cuda, V, offset):
+    """Slot-major 8-bit values ([aligned slot][V] bytes, zero padding) from the
+    GPU packer equal the host packer's, from an aligned and an odd source
+    address; the separate values entry point writes the same bytes."""
+    m = synth.lengths_mask([0, 1, 15, 16, 17, 31, 32, 33, 100, 0, 7, 64, 250], 256, V, seed=V + 3)
+    vals = synth.random_bytes(m.nnz_vec * V, V + 21)
+    buf = torch.zeros(vals.size + offset, dtype=torch.uint8, device=cuda)
+    buf[offset:] = _dev(vals, cuda)
+    h = formats.prepare_spmm(m, vals, 8, 8, layout=formats.VALUES_SLOT_MAJOR)
+    d = dfm.prepare_spmm(_dev(m.row_offsets, cuda), _dev(m.col_indices, cuda), buf[offset:], V, m.ncols, 8, 8,
+                         layout=formats.VALUES_SLOT_MAJOR)
+    np.testing.assert_array_equal(d.row_offsets.cpu().numpy(), h.row_offsets)
+    np.testing.assert_array_equal(d.col_indices.cpu().numpy(), h.col_indices)
+    np.testing.assert_array_equal(d.values.cpu().numpy(), h.values)
+    n = torch.tensor([h.aligned_nnz], dtype=torch.int32, device=cuda)
+    sep = dfm.pack_spmm_values(_dev(m.row_offsets, cuda), d.row_offsets, n, buf[offset:], V, 8, 8, h.aligned_nnz,
+                               layout=formats.VALUES_SLOT_MAJOR)
+    np.testing.assert_array_equal(sep.cpu().numpy(), h.values)
+
+
+def test_device_slot_major_feeds_dense_tile_spmm(cuda):
+    """A slot-major operand packed on the GPU gives the dense-tile SpMM the
+    oracle's result bit for bit, named or picked by MC_KERNEL_AUTO."""
+    V, K, N = 8, 512, 256
+    m = synth.uniform_mask(96, K, V, 0.8, seed=17)
+    vals = synth.random_bytes(m.nnz_vec * V, 18)
+    rhs = synth.random_bytes(K * N, 19)
+    d = dfm.prepare_spmm(_dev(m.row_offsets, cuda), _dev(m.col_indices, cuda), _dev(vals, cuda), V, m.ncols, 8, 8,
+                         layout=formats.VALUES_SLOT_MAJOR)
+    out = ops.spmm(d, _dev(rhs, cuda), N, signed=True, variant=_lib.KERNEL_DENSE_TILE,
+                   value_layout=formats.VALUES_SLOT_MAJOR)
+    ref = oracle.spmm_host(vals, rhs, m.row_offsets, m.col_indices, m.m_vec, V, K, N, 8, 8, oracle.SIGNED)
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
+    auto = ops.spmm(d, _dev(rhs, cuda), N, signed=True, value_layout=formats.VALUES_SLOT_MAJOR)
+    assert torch.equal(auto, out)
 
 
 @pytest.mark.parametrize("name", names("ref_spmm_"))

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <new>
@@ -170,6 +171,11 @@ int check_request(const mcAttnServerDesc& d, const mcAttnRequest& r)
     if (!r.row_offsets || (r.nnz_vec > 0 && !r.col_indices) || !r.qkv || !r.out)
         return mc::fail(1, "mcAttnServerRun: null request pointer");
     if (!(r.arrival_s >= 0.0)) return mc::fail(1, "mcAttnServerRun: arrival times must be >= 0");
+    // the stacked CSR and the packer's aligned count are int: one request's
+    // nonzeros with its rows' alignment padding must fit
+    const long long align = d.rhs_bits == 8 ? 16 : 32;
+    if (r.nnz_vec + (long long)(r.seq_len / d.vec_length) * align > INT_MAX)
+        return mc::fail(1, "mcAttnServerRun: a request's aligned nonzero count exceeds the int range");
     return 0;
 }
 
@@ -359,6 +365,8 @@ int mcAttnServerRun(mcAttnServer* sv, const mcAttnRequest* reqs, int n, double* 
             for (int r : queue) {
                 const mcAttnRequest& q = reqs[r];
                 if (!ids.empty() && tokens + q.seq_len > d.max_batch_tokens) break;
+                const long long align = d.rhs_bits == 8 ? 16 : 32;
+                if (!ids.empty() && nnz + q.nnz_vec + (rows + q.seq_len / d.vec_length) * align > INT_MAX) break;
                 ids.push_back(r);
                 tokens += q.seq_len;
                 rows += q.seq_len / d.vec_length;
@@ -410,7 +418,12 @@ int mcAttnServerRun(mcAttnServer* sv, const mcAttnRequest* reqs, int n, double* 
             if (!rc) rc = rf;
             if (!rc) rc = (int)cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming);
             if (!rc) rc = (int)cudaEventRecord(f.done, s);
-            if (rc) break;
+            if (rc) {
+                // what this batch queued is not tracked: let it drain before returning
+                cudaStreamSynchronize(s);
+                if (f.done) cudaEventDestroy(f.done);
+                break;
+            }
             slot_busy[slot] = 1;
             inflight.push_back(f);
             queue.erase(queue.begin(), queue.begin() + (long)ids.size());

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 import torch
 
-from magicube_gb300 import batched, synth
+from magicube_gb300 import _lib, batched, synth
 
 pytestmark = pytest.mark.gpu
 
@@ -98,3 +98,12 @@ def test_admission_rejects_a_request_that_cannot_fit(cuda):
     torch.cuda.synchronize()
     assert st["rejected"] == 2 and st["served"] == 0 and (lat == -1).all()
     assert all(torch.isnan(o).all() for o in outs)
+
+
+def test_request_beyond_int_offsets_is_refused(cuda):
+    """A request whose aligned nonzero count leaves the int range of the
+    stacked CSR is refused before any batch is launched."""
+    masks, qkvs, outs, reqs, _keep = _requests(cuda, [256], seed=41)
+    reqs[0].nnz_vec = (1 << 31) - 64
+    with pytest.raises(_lib.MagicubeError, match="int range"):
+        _server(max_batch_tokens=4096, max_inflight=1).run(reqs)

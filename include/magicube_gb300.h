@@ -189,7 +189,8 @@ enum { MC_VALUES_PACKED = 0, MC_VALUES_SOFTMAX = 1, MC_VALUES_SLOT_MAJOR = 2 };
  * These generalise the reference's batched extension kernels
  * (batched_wmmaSpmm_* in sparse_transformer_magicube/src/cuda/deq_spmm_kernel.cu,
  * batched_wmmaSddmm_* in deq_sddmm_kernel.cu): batch entries share one mask and
- * advance each operand by its stride (a zero stride shares the operand).
+ * advance each operand by its stride (a zero stride shares the operand;
+ * negative strides are rejected).
  * is_signed = 1 reads every lane as two's complement (16-bit values: signed
  * high byte, unsigned low byte); 0 reads lanes unsigned, as the reference's
  * GPU kernels do.  out_half = 1 writes half(float(acc) / scale). */

@@ -340,6 +340,8 @@ extern "C" int mcQuantSoftmax(const mcSoftmaxDesc* d, cudaStream_t stream)
         return mc::fail(1, "mcQuantSoftmax: scores must be 16-byte aligned, stride a multiple of 8 halves");
     if (reinterpret_cast<uintptr_t>(d->out) % 2 || d->out_stride % 2)  // slot pairs are stored as 16-bit words
         return mc::fail(1, "mcQuantSoftmax: out must be 2-byte aligned, stride a multiple of 2 bytes");
+    if (d->batch > 1 && (d->scores_stride < 0 || d->out_stride < 0))
+        return mc::fail(1, "mcQuantSoftmax: negative stride");
     if (d->requant != MC_REQUANT_FIXED && d->requant != MC_REQUANT_ROWMAX)
         return mc::fail(1, "mcQuantSoftmax: requant must be MC_REQUANT_FIXED or MC_REQUANT_ROWMAX");
     if (d->requant == MC_REQUANT_ROWMAX &&

@@ -30,6 +30,8 @@ extern "C" int mcSparseAttention(const mcAttnDesc* d, cudaStream_t stream)
     auto al = [](const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; };
     if (!al(d->q) || !al(d->k) || !al(d->v) || d->head_stride % 16 || !al(d->out) || d->out_head_stride % 8)
         return mc::fail(1, "mcSparseAttention: q, k, v, out must be 16-byte aligned with 16-byte strides");
+    if (d->heads > 1 && (d->head_stride < 0 || d->out_head_stride < 0))
+        return mc::fail(1, "mcSparseAttention: negative head stride");
     mc::AttnParams p;
     p.m_vec = d->m_vec;
     p.heads = d->heads;

@@ -126,6 +126,8 @@ static int check_sddmm(const mcSddmmDesc& d)
     if (!aligned(d.lhs, 16) || d.lhs_stride % 16) return fail(1, "mcSddmm: lhs must be 16-byte aligned");
     if (!aligned(d.rhs, 16) || d.rhs_stride % 16) return fail(1, "mcSddmm: rhs must be 16-byte aligned");
     if (!aligned(d.out, 8) || d.out_stride % 2) return fail(1, "mcSddmm: output must be 8-byte aligned");
+    if (d.batch > 1 && (d.lhs_stride < 0 || d.rhs_stride < 0 || d.out_stride < 0))
+        return fail(1, "mcSddmm: negative stride");
     return 0;
 }
 

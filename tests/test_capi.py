@@ -67,6 +67,31 @@ def test_sddmm_argument_errors(field, value, msg):
     assert msg in _lib.lib().mcGetLastErrorString()
 
 
+@pytest.mark.parametrize("field", ["lhs_stride", "rhs_stride", "out_stride"])
+def test_sddmm_negative_batch_stride_rejected(field):
+    """As for the SpMM: batch strides are non-negative (zero shares)."""
+    d = _lib.McSddmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=2, scale=1.0,
+                         row_indices=256, row_offsets=256, column_indices=256, lhs=256, rhs=256, out=256)
+    setattr(d, field, -64)
+    assert _lib.lib().mcSddmm(ctypes.byref(d), None) == 1
+    assert b"negative stride" in _lib.lib().mcGetLastErrorString()
+
+
+def test_softmax_and_fused_attention_reject_negative_strides():
+    """Batch (softmax) and head (fused attention) strides are non-negative;
+    both checks run before any GPU work."""
+    lib = _lib.lib()
+    sm = _lib.McSoftmaxDesc(m_vec=4, vec_length=8, batch=2, bits=8, scaling=0.125, scale=127.0, row_indices=256,
+                            row_offsets=256, scores=256, scores_stride=-64, out=256, out_stride=64)
+    assert lib.mcQuantSoftmax(ctypes.byref(sm), None) == 1
+    assert b"negative stride" in lib.mcGetLastErrorString()
+    a = _lib.McAttnDesc(m_vec=4, vec_length=8, heads=2, head_dim=64, max_row_nnz=32, lhs_bits=8, rhs_bits=8,
+                        requant=_lib.REQUANT_FIXED, row_indices=256, row_offsets=256, column_indices=256, q=256,
+                        k=256, v=256, head_stride=64, out=256, out_head_stride=-64)
+    assert lib.mcSparseAttention(ctypes.byref(a), None) == 1
+    assert b"negative head stride" in lib.mcGetLastErrorString()
+
+
 def test_null_pointers_rejected():
     d = _lib.McSpmmDesc(m_vec=4, vec_length=8, n=128, k=64, lhs_bits=8, rhs_bits=8, batch=1)
     assert _lib.lib().mcSpmm(ctypes.byref(d), None) == 1

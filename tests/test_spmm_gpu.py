@@ -118,7 +118,8 @@ def test_spmm_half_output(cuda, pa, pb, V, variant):
     d = ops.DeviceSpmmLhs.from_host(h, cuda)
     out = ops.spmm(d, torch.from_numpy(rhs).to(cuda), N, signed=True, out_half=True, scale=scale, variant=variant)
     acc = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb, oracle.SIGNED)
-    ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
+    with np.errstate(over="ignore"):  # 16-bit A: sums beyond the half range round to inf, as on the GPU
+        ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
     np.testing.assert_array_equal(out.cpu().numpy().view(np.uint16), ref.view(np.uint16))
 
 

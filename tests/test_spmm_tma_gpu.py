@@ -130,7 +130,8 @@ def test_tma_half_output_equals_stream(cuda, pa, pb, V):
             for v in (_lib.KERNEL_TMA, _lib.KERNEL_STREAM)]
     assert torch.equal(outs[0], outs[1])
     acc = oracle.spmm_host(vals, rhs, mask.row_offsets, mask.col_indices, mask.m_vec, V, K, N, pa, pb, oracle.SIGNED)
-    ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
+    with np.errstate(over="ignore"):  # 16-bit A: sums beyond the half range round to inf, as on the GPU
+        ref = (acc.astype(np.float32) / np.float32(scale)).astype(np.float16)
     np.testing.assert_array_equal(outs[0].cpu().numpy().view(np.uint16), ref.view(np.uint16))
 
 

@@ -6,7 +6,7 @@ library's.  Operands are raw packed integer payloads (uint8 / int32 tensors).
 from __future__ import annotations
 
 import ctypes
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 import torch
@@ -38,7 +38,8 @@ class DeviceSpmmLhs:
     col_indices: torch.Tensor
     values: torch.Tensor
 
-    _chunks: torch.Tensor | None = None
+    _chunks: torch.Tensor | None = field(default=None, repr=False, compare=False)
+    _chunks_key: tuple | None = field(default=None, repr=False, compare=False)
 
     @classmethod
     def from_host(cls, h: SpmmLhs, device="cuda") -> "DeviceSpmmLhs":
@@ -50,10 +51,13 @@ class DeviceSpmmLhs:
 
     def chunk_starts(self, stream: torch.cuda.Stream | None = None) -> torch.Tensor:
         """The mask's k-chunk table for the dense-tile SpMM kernel, built on
-        the device once (mcSpmmChunkStarts) and cached.  Synchronises once to
+        the device (mcSpmmChunkStarts) and cached until the mask's tensors
+        are replaced or modified in place.  Synchronises once per build to
         read the status; raises MagicubeError if a vector-row's columns are
         not strictly increasing inside [0, k)."""
-        if self._chunks is None:
+        key = (self.m_vec, self.k, self.row_offsets.data_ptr(), self.row_offsets._version,
+               self.col_indices.data_ptr(), self.col_indices._version)
+        if self._chunks is None or self._chunks_key != key:
             dev = self.row_offsets.device
             per = _lib.lib().mcSpmmChunkStartsCount(self.k)
             starts = torch.empty((max(1, self.m_vec), per), dtype=torch.int32, device=dev)
@@ -64,7 +68,7 @@ class DeviceSpmmLhs:
             if int(status.item()) != 0:
                 raise _lib.MagicubeError("mcSpmmChunkStarts: the mask's columns are not strictly increasing "
                                          "inside [0, k) per vector-row; the dense-tile SpMM cannot use it")
-            self._chunks = starts
+            self._chunks, self._chunks_key = starts, key
         return self._chunks
 
 

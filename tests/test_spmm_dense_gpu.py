@@ -145,3 +145,20 @@ def test_chunk_starts_table(cuda):
         cols = mask.col_indices[mask.row_offsets[r]:mask.row_offsets[r + 1]]
         want = [start + int(np.searchsorted(cols, 64 * c)) for c in range(nchunks + 1)]
         assert got[r].tolist() == want
+
+
+def test_chunk_table_cache_follows_the_mask(cuda):
+    """The chunk table is cached, and rebuilt when the mask's columns are
+    modified in place or replaced."""
+    V, K = 8, 256
+    mask = synth.lengths_mask([5, 9, 40], K, V, seed=2)
+    d = _dev(cuda, mask, synth.random_bytes(mask.nnz_vec * V, 3))
+    t1 = d.chunk_starts()
+    assert d.chunk_starts() is t1
+    first = d.col_indices[:2].clone()
+    d.col_indices[:2] = first.flip(0)  # the first row's columns out of order
+    with pytest.raises(_lib.MagicubeError):
+        d.chunk_starts()
+    d.col_indices = d.col_indices.clone()
+    d.col_indices[:2] = first
+    assert torch.equal(d.chunk_starts(), t1)

@@ -84,7 +84,8 @@ class DeviceSddmmMask:
     row_offsets: torch.Tensor
     col_indices: torch.Tensor
 
-    _tile: tuple | None = None
+    _tile: tuple | None = field(default=None, repr=False, compare=False)
+    _tile_key: tuple | None = field(default=None, repr=False, compare=False)
 
     @classmethod
     def from_host(cls, h: SddmmMask, device="cuda") -> "DeviceSddmmMask":
@@ -94,10 +95,13 @@ class DeviceSddmmMask:
 
     def tile_mask(self, stream: torch.cuda.Stream | None = None) -> tuple[torch.Tensor, torch.Tensor]:
         """(bitmap, prefix) of the mask for the dense-tile SDDMM kernel, built
-        on the device once (mcSddmmTileMask) and cached.  Synchronises once to
+        on the device (mcSddmmTileMask) and cached until the mask's tensors
+        are replaced or modified in place.  Synchronises once per build to
         read the status; raises MagicubeError if a vector-row's columns are
         not strictly increasing."""
-        if self._tile is None:
+        key = (self.m_vec, self.n, self.row_offsets.data_ptr(), self.row_offsets._version,
+               self.col_indices.data_ptr(), self.col_indices._version)
+        if self._tile is None or self._tile_key != key:
             dev = self.row_offsets.device
             words = _lib.lib().mcSddmmTileMaskWords(self.n)
             bitmap = torch.empty((max(1, self.m_vec), words), dtype=torch.int32, device=dev)
@@ -109,7 +113,7 @@ class DeviceSddmmMask:
             if int(status.item()) != 0:
                 raise _lib.MagicubeError("mcSddmmTileMask: the mask's columns are not strictly increasing per "
                                          "vector-row; the dense-tile SDDMM cannot use it")
-            self._tile = (bitmap, prefix)
+            self._tile, self._tile_key = (bitmap, prefix), key
         return self._tile
 
 

@@ -142,6 +142,25 @@ def test_tile_mask_refuses_unsorted(cuda):
         dm.tile_mask()
 
 
+def test_tile_mask_cache_follows_the_mask(cuda):
+    """The bitmap is cached, and rebuilt when the mask's columns are modified
+    in place (here: two columns swapped, then swapped back)."""
+    V, N = 8, 256
+    mask, _, _ = _case(V, N, [16, 40], seed=6)
+    hm = formats.prepare_sddmm(mask)
+    dm = ops.DeviceSddmmMask.from_host(hm, cuda)
+    t1 = dm.tile_mask()
+    assert dm.tile_mask() is t1
+    s = int(hm.row_offsets[0])
+    first = dm.col_indices[s:s + 2].clone()
+    dm.col_indices[s:s + 2] = first.flip(0)
+    with pytest.raises(_lib.MagicubeError, match="strictly increasing"):
+        dm.tile_mask()
+    dm.col_indices[s:s + 2] = first
+    b2, p2 = dm.tile_mask()
+    assert torch.equal(b2, t1[0]) and torch.equal(p2, t1[1])
+
+
 def test_dense_tile_rejects(cuda):
     V, N = 8, 256
     mask, lhs, rhs = _case(V, N, [16, 16], seed=3)

@@ -89,3 +89,24 @@ def test_slot_major_layout_on_the_host():
         np.testing.assert_array_equal(got[start:start + n], want)
         end = h.aligned_nnz if r == mask.m_vec - 1 else h.row_offsets[2 * r + 2]
         assert not got[start + n:end].any()
+
+
+def test_slot_major_host_packer_refusals():
+    """The host packer writes slot-major values for L8-R8 only, and refuses an
+    aligned count that the rows' slots overrun."""
+    import ctypes
+    from magicube_gb300 import _lib
+    lib = _lib.lib()
+    ro = np.array([0, 3], np.int32)
+    pairs = np.array([0, 3], np.int32)
+    vals = np.arange(3 * 8, dtype=np.uint8)
+    out = np.zeros(16 * 8, np.uint8)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rc = lib.mcPackSpmmValuesEx(1, 8, 8, 4, p(ro), p(pairs), 16, p(vals), p(out), _lib.VALUES_SLOT_MAJOR)
+    assert rc == 1 and b"invalid arguments" in lib.mcGetLastErrorString()
+    rc = lib.mcPackSpmmValuesEx(1, 8, 8, 8, p(ro), p(pairs), 2, p(vals), p(out), _lib.VALUES_SLOT_MAJOR)
+    assert rc == 1 and b"aligned_nnz too small" in lib.mcGetLastErrorString()
+    rc = lib.mcPackSpmmValuesEx(1, 8, 8, 8, p(ro), p(pairs), 16, p(vals), p(out), _lib.VALUES_SLOT_MAJOR)
+    assert rc == 0
+    np.testing.assert_array_equal(out[:24], vals)
+    assert not out[24:].any()

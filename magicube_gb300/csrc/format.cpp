@@ -53,11 +53,12 @@ extern "C" int mcAlignRowOffsets(int m_vec, const int* row_offsets, int alignmen
         return mc::fail(-1, "mcAlignRowOffsets: invalid arguments");
     long long aligned = 0;
     for (int i = 0; i < m_vec; ++i) {
-        int len = row_offsets[i + 1] - row_offsets[i];
+        const long long len = (long long)row_offsets[i + 1] - row_offsets[i];
         if (len < 0) return mc::fail(-1, "mcAlignRowOffsets: row_offsets not monotone");
+        if (aligned + len > 0x7fffffffLL) return mc::fail(-1, "mcAlignRowOffsets: aligned size overflows int");
         aligned_pairs[2 * i] = (int)aligned;
         aligned_pairs[2 * i + 1] = (int)(aligned + len);
-        aligned += (long long)(len + alignment - 1) / alignment * alignment;
+        aligned += (len + alignment - 1) / alignment * alignment;
         if (aligned > 0x7fffffffLL) return mc::fail(-1, "mcAlignRowOffsets: aligned size overflows int");
     }
     return (int)aligned;
@@ -73,9 +74,12 @@ extern "C" int mcPadColumnIndices(int m_vec, const int* row_offsets, const int* 
     std::vector<int> plain((size_t)aligned_nnz, -1);
     for (int i = 0; i < m_vec; ++i) {
         const int b = row_offsets[i], e = row_offsets[i + 1];
-        const int dst = aligned_pairs[2 * i];
-        if (dst + (e - b) > aligned_nnz) return mc::fail(1, "mcPadColumnIndices: aligned_nnz too small");
-        for (int j = b; j < e; ++j) plain[(size_t)dst + (j - b)] = col_indices[j];
+        const long long dst = aligned_pairs[2 * i];
+        if (e > b && !col_indices) return mc::fail(1, "mcPadColumnIndices: null col_indices");
+        if (dst < 0) return mc::fail(1, "mcPadColumnIndices: negative aligned start");
+        if (e > b && dst + ((long long)e - b) > aligned_nnz)
+            return mc::fail(1, "mcPadColumnIndices: aligned_nnz too small");
+        for (int j = b; j < e; ++j) plain[(size_t)(dst + (j - b))] = col_indices[j];
     }
     if (!shuffle8) {
         std::memcpy(out_cols, plain.data(), sizeof(int) * (size_t)aligned_nnz);
@@ -112,6 +116,8 @@ extern "C" int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int r
         std::memset(dst, 0, (size_t)aligned_nnz * V);
         for (int i = 0; i < m_vec; ++i) {
             const int b = row_offsets[i], e = row_offsets[i + 1];
+            if (e > b && (!src || aligned_pairs[2 * i] < 0))
+                return mc::fail(1, "mcPackSpmmValues: null values or negative aligned start");
             for (int j = b; j < e; ++j) {
                 const long long slot = (long long)aligned_pairs[2 * i] + (j - b);
                 if (slot >= aligned_nnz) return mc::fail(1, "mcPackSpmmValues: aligned_nnz too small");
@@ -142,6 +148,8 @@ extern "C" int mcPackSpmmValuesEx(int m_vec, int vec_length, int lhs_bits, int r
     const uint32_t pmask = (1u << plane_bits) - 1u;
     for (int i = 0; i < m_vec; ++i) {
         const int b = row_offsets[i], e = row_offsets[i + 1];
+        if (e > b && (!src || aligned_pairs[2 * i] < 0))
+            return mc::fail(1, "mcPackSpmmValues: null values or negative aligned start");
         for (int j = b; j < e; ++j) {
             const long long slot = (long long)aligned_pairs[2 * i] + (j - b);
             if (slot >= aligned_nnz) return mc::fail(1, "mcPackSpmmValues: aligned_nnz too small");
@@ -164,7 +172,7 @@ extern "C" int mcSortedRowSwizzle(int m_vec, const int* row_offsets, int* row_in
     std::vector<int> idx((size_t)m_vec);
     std::iota(idx.begin(), idx.end(), 0);
     std::sort(idx.begin(), idx.end(), [row_offsets](int a, int b) {
-        return (row_offsets[a + 1] - row_offsets[a]) > (row_offsets[b + 1] - row_offsets[b]);
+        return ((long long)row_offsets[a + 1] - row_offsets[a]) > ((long long)row_offsets[b + 1] - row_offsets[b]);
     });
     std::memcpy(row_indices, idx.data(), sizeof(int) * (size_t)m_vec);
     return 0;

@@ -110,3 +110,35 @@ def test_slot_major_host_packer_refusals():
     assert rc == 0
     np.testing.assert_array_equal(out[:24], vals)
     assert not out[24:].any()
+
+
+def test_host_packer_refuses_bad_offsets_without_writing_out_of_bounds():
+    """Negative aligned starts, missing arrays and sizes beyond the int range
+    are refused before any write."""
+    import ctypes
+    from magicube_gb300 import _lib
+    lib = _lib.lib()
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    ro = np.array([0, 3], np.int32)
+    cols = np.array([1, 5, 9], np.int32)
+    bad_pairs = np.array([-16, -13], np.int32)
+    out_cols = np.zeros(16, np.int32)
+    assert lib.mcPadColumnIndices(1, p(ro), p(cols), p(bad_pairs), 16, 0, p(out_cols)) == 1
+    assert b"negative aligned start" in lib.mcGetLastErrorString()
+    pairs = np.array([0, 3], np.int32)
+    assert lib.mcPadColumnIndices(1, p(ro), None, p(pairs), 16, 0, p(out_cols)) == 1
+    assert b"null col_indices" in lib.mcGetLastErrorString()
+    vals = np.zeros(3 * 8, np.uint8)
+    out = np.zeros(16 * 8, np.uint8)
+    for layout in (_lib.VALUES_PACKED, _lib.VALUES_SLOT_MAJOR):
+        assert lib.mcPackSpmmValuesEx(1, 8, 8, 8, p(ro), p(bad_pairs), 16, p(vals), p(out), layout) == 1
+        assert b"negative aligned start" in lib.mcGetLastErrorString()
+        assert lib.mcPackSpmmValuesEx(1, 8, 8, 8, p(ro), p(pairs), 16, None, p(out), layout) == 1
+        assert b"null values" in lib.mcGetLastErrorString()
+    huge = np.array([0, 2_147_483_641], np.int32)  # rounds up past the int range
+    apairs = np.zeros(4, np.int32)
+    assert lib.mcAlignRowOffsets(1, p(huge), 16, p(apairs)) == -1
+    assert b"overflows int" in lib.mcGetLastErrorString()
+    spread = np.array([-2_000_000_000, 2_000_000_000], np.int32)  # a length beyond the int range
+    assert lib.mcAlignRowOffsets(1, p(spread), 16, p(apairs)) == -1
+    assert b"overflows int" in lib.mcGetLastErrorString()

@@ -85,7 +85,8 @@ def build_cli() -> list[Path]:
     outs = []
     for src in sorted(CLI.glob("*.cpp")):
         exe = BIN / src.stem
-        if not exe.exists() or any(p.stat().st_mtime > exe.stat().st_mtime for p in [src, LIB, *INCLUDE.glob("*.h")]):
+        if not exe.exists() or any(p.stat().st_mtime > exe.stat().st_mtime
+                                      for p in [src, LIB, *INCLUDE.glob("*.h"), *CLI.glob("*.h")]):
             _run(["g++", "-O2", "-std=c++17", "-Wall", "-I", str(INCLUDE), "-I", _cuda_include(), str(src),
                   "-o", str(exe), "-L", str(PKG), "-lmagicube_gb300", "-L", _cuda_lib(), "-lcudart",
                   "-Wl,-rpath,$ORIGIN/..", "-Wl,-rpath," + _cuda_lib()])

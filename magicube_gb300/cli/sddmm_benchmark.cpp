@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "magicube_gb300.h"
+#include "smtx_reader.h"
 
 namespace {
 
@@ -67,21 +68,15 @@ int main(int argc, char** argv)
         std::printf("Unsupported vec_length!\n");
         return 1;
     }
-    std::ifstream in(bm);
-    if (!in) {
-        std::fprintf(stderr, "cannot read %s\n", bm.c_str());
+    Smtx s;
+    std::string err;
+    if (!read_smtx(bm, s, err)) {
+        std::fprintf(stderr, "%s\n", err.c_str());
         return 1;
     }
-    std::string tok;
-    std::getline(in, tok, ',');
-    const int m_vec = std::stoi(tok);
-    std::getline(in, tok, ',');
-    const int N = std::stoi(tok);
-    std::getline(in, tok, '\n');
-    const int nnz = std::stoi(tok);
-    std::vector<int> offsets(m_vec + 1), cols(nnz);
-    for (auto& x : offsets) in >> x;
-    for (auto& x : cols) in >> x;
+    const int m_vec = s.m_vec, N = s.ncols, nnz = s.nnz;
+    std::vector<int>& offsets = s.offsets;
+    std::vector<int>& cols = s.cols;
     const int M = m_vec * V, alignment = 8;
     std::printf("PreA: %d, PreB: %d, vec_len: %d, M: %d, M_vec: %d, N: %d, nnz: %d, K: %d\n", preA, preB, V, M, m_vec, N,
                 nnz * V, K);

@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "magicube_gb300.h"
+#include "smtx_reader.h"
 
 namespace {
 
@@ -61,29 +62,6 @@ void make_dense(long long count, T* out, std::default_random_engine gen)
             out[i] = (T)(127.0 * dist(gen));
         }
     }
-}
-
-struct Smtx {
-    int m_vec = 0, ncols = 0, nnz = 0;
-    std::vector<int> offsets, cols;
-};
-
-bool read_smtx(const std::string& path, Smtx& s)
-{
-    std::ifstream in(path);
-    if (!in) return false;
-    std::string tok;
-    if (!std::getline(in, tok, ',')) return false;
-    s.m_vec = std::stoi(tok);
-    std::getline(in, tok, ',');
-    s.ncols = std::stoi(tok);
-    std::getline(in, tok, '\n');
-    s.nnz = std::stoi(tok);
-    s.offsets.resize(s.m_vec + 1);
-    s.cols.resize(s.nnz);
-    for (auto& x : s.offsets) in >> x;
-    for (auto& x : s.cols) in >> x;
-    return (bool)in || in.eof();
 }
 
 // Container type of one vector's values and the number of containers per
@@ -162,8 +140,9 @@ int main(int argc, char** argv)
         return 1;
     }
     Smtx s;
-    if (!read_smtx(bm, s)) {
-        std::fprintf(stderr, "cannot read %s\n", bm.c_str());
+    std::string err;
+    if (!read_smtx(bm, s, err)) {
+        std::fprintf(stderr, "%s\n", err.c_str());
         return 1;
     }
     const int K = s.ncols, M = s.m_vec * V;

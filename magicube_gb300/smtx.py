@@ -34,6 +34,8 @@ def read(path: str | Path, vec_length: int) -> VectorSparse:
     text = Path(path).read_text()
     head, rest = text.split("\n", 1)
     m_vec, ncols, nnz = (int(x) for x in head.split(","))
+    if m_vec < 0 or ncols <= 0 or nnz < 0:
+        raise ValueError(f"{path}: header out of range (rows >= 0, columns > 0, nonzeros >= 0)")
     toks = rest.split()
     if len(toks) < m_vec + 1 + nnz:
         raise ValueError(f"{path}: expected {m_vec + 1} offsets and {nnz} column indices")

@@ -23,6 +23,9 @@ def test_smtx_rejects_malformed(tmp_path):
     p.write_text("1, 4, 2\n0 2\n1 9\n")
     with pytest.raises(ValueError):
         smtx.read(p, 2)
+    p.write_text("-1, 4, 0\n0\n\n")
+    with pytest.raises(ValueError, match="header out of range"):
+        smtx.read(p, 2)
 
 
 @pytest.mark.parametrize("alignment", [8, 16, 32])
